@@ -1,0 +1,300 @@
+// Reference-side driver for the CPU oracle.
+//
+// Test infrastructure only.  Compiled (by oracle/ref/Makefile) against the
+// unmodified Dendro-KT sources, a single-rank MPI stand-in and two LAPACK
+// routines; writes everything the parity tests pin:
+//   * the balanced tree      SFC_Tree::locTreeBalancing   (src/tsort.cpp:826-854)
+//   * the DA node list       ot::DA::construct            (src/oda.cpp:52-151)
+//   * boundary node ids      (src/oda.cpp:145-150)
+//   * feMatrix::matVec output (FEM/include/feMatrix.h:189-259) for
+//       op 0: identity eleOp as in test/testMatvec.cpp:187-198
+//       op 1: HeatEq::HeatMat<dim> (FEM/examples/src/heatMat.cpp:45-139)
+//       op 2: Laplacian + mass, a restatement built from the reference's
+//             RefElement 1D operators (the reference has no valid 4D operator)
+//   * the raw fem::matvec output (FEM/include/matvec.h:231-240), no pre/post
+//   * the RefElement 1D matrices (FEM/src/refel.cpp:75-220)
+//
+// Binary formats are documented in oracle/ref/README.md.
+#include <mpi.h>
+#include "treeNode.h"
+#include "tsort.h"
+#include "nsort.h"
+#include "oda.h"
+#include "hcurvedata.h"
+#include "feMatrix.h"
+#include "matvec.h"
+#include "refel.h"
+#include "heatMat.h"
+
+#include <chrono>
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include <algorithm>
+#include <functional>
+#include <vector>
+#include <string>
+#include <cmath>
+
+namespace {
+
+// Counter-based uniform in [-1,1): the same function the product, the port
+// oracle and the tests use to make nodal vectors from a seed.
+inline uint64_t splitmix64(uint64_t z)
+{
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+inline double uniform_pm1(uint64_t seed, uint64_t i)
+{
+  uint64_t r = splitmix64(seed * 0xD1B54A32D192ED03ull + i);
+  return 2.0 * ((double) (r >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+}
+
+struct Reader {
+  FILE *f;
+  template <typename X> X get() { X x; if (fread(&x, sizeof(X), 1, f) != 1) { fprintf(stderr, "short read\n"); exit(2); } return x; }
+  template <typename X> void arr(X *p, size_t n) { if (n && fread(p, sizeof(X), n, f) != n) { fprintf(stderr, "short read\n"); exit(2); } }
+};
+struct Writer {
+  FILE *f;
+  template <typename X> void put(X x) { fwrite(&x, sizeof(X), 1, f); }
+  template <typename X> void arr(const X *p, size_t n) { if (n) fwrite(p, sizeof(X), n, f); }
+};
+
+// Identity eleOp (test/testMatvec.cpp:187-198).
+template <unsigned int dim>
+class IdentityMat : public feMatrix<IdentityMat<dim>, dim> {
+ public:
+  using feMatrix<IdentityMat<dim>, dim>::feMatrix;
+  void elementalMatVec(const VECType *in, VECType *out, double *, double) override
+  {
+    const RefElement *refEl = feMat<dim>::m_uiOctDA->getReferenceElement();
+    const unsigned int nPe = intPow(refEl->getOrder() + 1, dim);
+    for (unsigned int i = 0; i < nPe; i++) out[i] = in[i];
+  }
+};
+
+// y[..j..] = sum_k A[k*M+j] x[..k..] along `axis` (axis 0 varies fastest), the
+// convention of DENDRO_TENSOR_IIAX_APPLY_ELEM (FEM/src/tensor.cpp:44-60).
+template <unsigned int dim>
+void apply_axis(unsigned M, const double *A, const double *x, double *y, unsigned axis)
+{
+  unsigned stride = 1;
+  for (unsigned a = 0; a < axis; a++) stride *= M;
+  unsigned n = 1;
+  for (unsigned a = 0; a < dim; a++) n *= M;
+  for (unsigned idx = 0; idx < n; idx++) {
+    unsigned j = (idx / stride) % M;
+    unsigned base = idx - j * stride;
+    double s = 0.0;
+    for (unsigned k = 0; k < M; k++) s += A[k * M + j] * x[base + k * stride];
+    y[idx] = s;
+  }
+}
+
+// Laplacian + mass on a cube element of side h, J = h/2:
+//   K_e = J^(d-2) sum_a (Dg^T W Dg)_a (x) (Q^T W Q)_others  +  J^d (Q^T W Q)^(x)d
+// using the reference's Gauss quadrature 1D operators (RefElement::getQ1d,
+// getDg1d, getWgq), with HeatMat's boundary conditions (heatMat.cpp:119-139).
+template <unsigned int dim>
+class LapMassMat : public feMatrix<LapMassMat<dim>, dim> {
+ public:
+  using feMatrix<LapMassMat<dim>, dim>::feMatrix;
+  void elementalMatVec(const VECType *in, VECType *out, double *coords, double scale) override
+  {
+    const RefElement *refEl = feMat<dim>::m_uiOctDA->getReferenceElement();
+    const unsigned p = refEl->getOrder(), M = p + 1;
+    const unsigned nPe = intPow(M, dim);
+    const double *Q = refEl->getQ1d(), *QT = refEl->getQT1d();
+    const double *D = refEl->getDg1d(), *DT = refEl->getDgT1d();
+    const double *W = refEl->getWgq();
+    const double h = coords[(nPe - 1) * dim + 0] - coords[0];
+    const double J = 0.5 * h;
+    double Jdm2 = 1.0, Jd = 1.0;
+    for (unsigned a = 0; a + 2 < dim; a++) Jdm2 *= J;
+    for (unsigned a = 0; a < dim; a++) Jd *= J;
+    if (dim < 2) Jdm2 = 1.0 / J;
+    std::vector<double> a(nPe), b(nPe), acc(nPe, 0.0), wq(nPe);
+    for (unsigned idx = 0; idx < nPe; idx++) {
+      double w = 1.0; unsigned r = idx;
+      for (unsigned d = 0; d < dim; d++) { w *= W[r % M]; r /= M; }
+      wq[idx] = w;
+    }
+    for (int term = -1; term < (int) dim; term++) {
+      std::copy(in, in + nPe, a.begin());
+      for (unsigned d = 0; d < dim; d++) {
+        apply_axis<dim>(M, ((int) d == term) ? D : Q, a.data(), b.data(), d);
+        std::swap(a, b);
+      }
+      for (unsigned idx = 0; idx < nPe; idx++) a[idx] *= wq[idx];
+      for (unsigned d = 0; d < dim; d++) {
+        apply_axis<dim>(M, ((int) d == term) ? DT : QT, a.data(), b.data(), d);
+        std::swap(a, b);
+      }
+      const double f = (term < 0) ? Jd : Jdm2;
+      for (unsigned idx = 0; idx < nPe; idx++) acc[idx] += f * a[idx];
+    }
+    for (unsigned idx = 0; idx < nPe; idx++) out[idx] = scale * acc[idx];
+  }
+  bool preMatVec(const VECType *, VECType *out, double)
+  {
+    std::vector<unsigned int> bdy;
+    feMat<dim>::m_uiOctDA->getBoundaryNodeIndices(bdy);
+    for (unsigned int i : bdy) out[i] = 0.0;
+    return true;
+  }
+  bool postMatVec(const VECType *, VECType *out, double)
+  {
+    std::vector<unsigned int> bdy;
+    feMat<dim>::m_uiOctDA->getBoundaryNodeIndices(bdy);
+    for (unsigned int i : bdy) out[i] = 0.0;
+    return true;
+  }
+};
+
+double now_s()
+{
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+template <unsigned int dim>
+int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind, int nCalls, uint64_t seed)
+{
+  using TN = ot::TreeNode<unsigned int, dim>;
+  m_uiMaxDepth = maxDepth;
+  _InitializeHcurve(dim);
+
+  const uint64_t n = in.get<uint64_t>();
+  std::vector<unsigned int> c(n * dim);
+  std::vector<uint8_t> lev(n, (uint8_t) maxDepth);
+  in.arr(c.data(), c.size());
+  if (inputKind != 0) in.arr(lev.data(), lev.size());
+  const uint64_t nxIn = in.get<uint64_t>();
+  std::vector<double> xIn(nxIn);
+  in.arr(xIn.data(), nxIn);
+
+  std::vector<TN> tree;
+  double t0 = now_s();
+  if (inputKind == 0) {
+    std::vector<TN> pts;
+    pts.reserve(n);
+    for (uint64_t i = 0; i < n; i++) {
+      std::array<unsigned int, dim> a;
+      for (unsigned d = 0; d < dim; d++) a[d] = c[i * dim + d];
+      pts.push_back(TN(a, maxDepth));
+    }
+    ot::SFC_Tree<unsigned int, dim>::locTreeBalancing(pts, tree, 1);
+  } else {
+    for (uint64_t i = 0; i < n; i++) {
+      std::array<unsigned int, dim> a;
+      for (unsigned d = 0; d < dim; d++) a[d] = c[i * dim + d];
+      tree.push_back(TN(a, lev[i]));
+    }
+    if (inputKind == 2)
+      ot::SFC_Tree<unsigned int, dim>::locTreeSort(tree.data(), 0, (ot::RankI) tree.size(), 1, maxDepth, 0);
+  }
+  double t1 = now_s();
+
+  ot::DA<dim> *da = new ot::DA<dim>(tree.data(), (unsigned int) tree.size(), MPI_COMM_WORLD, order);
+  double t2 = now_s();
+
+  const unsigned nLocal = da->getLocalNodalSz();
+  const unsigned nTotal = da->getTotalNodalSz();
+  const TN *nodes = da->getTNCoords() + da->getLocalNodeBegin();
+  std::vector<unsigned int> bdy;
+  da->getBoundaryNodeIndices(bdy);
+
+  std::vector<double> x(nLocal), y(nLocal, 0.0), yraw(nTotal, 0.0);
+  if (nxIn == nLocal) x = xIn;
+  else for (unsigned i = 0; i < nLocal; i++) x[i] = uniform_pm1(seed, i);
+
+  std::function<void(const double *, double *)> mv;
+  IdentityMat<dim> idm(da, 1);
+  HeatEq::HeatMat<dim> heat(da, 1);
+  LapMassMat<dim> lm(da, 1);
+  std::array<double, dim> lo, hi;
+  lo.fill(0.0);
+  hi.fill(1.0);
+  Point<dim> pmin(lo), pmax(hi);   // problem domain [0,1]^dim
+  heat.setProblemDimensions(pmin, pmax);
+  lm.setProblemDimensions(pmin, pmax);
+  if (op == 0) mv = [&](const double *a, double *b) { idm.matVec(a, b, 1.0); };
+  else if (op == 1) mv = [&](const double *a, double *b) { heat.matVec(a, b, 1.0); };
+  else mv = [&](const double *a, double *b) { lm.matVec(a, b, 1.0); };
+
+  std::vector<double> times;
+  for (int k = 0; k < std::max(nCalls, 1); k++) {
+    double ta = now_s();
+    mv(x.data(), y.data());
+    times.push_back(now_s() - ta);
+  }
+  std::sort(times.begin(), times.end());
+  const double tMed = times[times.size() / 2];
+
+  // Raw traversal, no boundary zeroing, on the ghosted layout (1 rank: identity).
+  {
+    std::vector<double> xg(nTotal, 0.0);
+    std::copy(x.begin(), x.end(), xg.begin() + da->getLocalNodeBegin());
+    using namespace std::placeholders;
+    fem::EleOpT<double> eop;
+    if (op == 0) eop = std::bind(&IdentityMat<dim>::elementalMatVec, &idm, _1, _2, _3, _4);
+    else if (op == 1) eop = std::bind(&HeatEq::HeatMat<dim>::elementalMatVec, &heat, _1, _2, _3, _4);
+    else eop = std::bind(&LapMassMat<dim>::elementalMatVec, &lm, _1, _2, _3, _4);
+    fem::matvec(xg.data(), yraw.data(), da->getTNCoords(), nTotal, *da->getTreePartFront(), *da->getTreePartBack(),
+                eop, 1.0, da->getReferenceElement());
+  }
+
+  out.put<char>('D'); out.put<char>('K'); out.put<char>('T'); out.put<char>('O');
+  out.put<uint64_t>(tree.size());
+  for (const TN &t : tree) for (unsigned d = 0; d < dim; d++) out.put<uint32_t>(t.getX(d));
+  for (const TN &t : tree) out.put<uint8_t>((uint8_t) t.getLevel());
+  out.put<uint64_t>(nLocal);
+  for (unsigned i = 0; i < nLocal; i++) for (unsigned d = 0; d < dim; d++) out.put<uint32_t>(nodes[i].getX(d));
+  for (unsigned i = 0; i < nLocal; i++) out.put<uint8_t>((uint8_t) nodes[i].getLevel());
+  out.put<uint64_t>(bdy.size());
+  for (unsigned i : bdy) out.put<uint32_t>(i);
+  out.put<uint64_t>(nLocal); out.arr(x.data(), nLocal);
+  out.put<uint64_t>(nLocal); out.arr(y.data(), nLocal);
+  out.put<uint64_t>(nTotal); out.arr(yraw.data(), nTotal);
+  out.put<double>(t1 - t0); out.put<double>(t2 - t1); out.put<double>(tMed);
+  const RefElement *re = da->getReferenceElement();
+  const int M = order + 1;
+  out.put<int32_t>(M);
+  out.arr(re->getIMChild0(), M * M);
+  out.arr(re->getIMChild1(), M * M);
+  out.arr(re->getQ1d(), M * M);
+  out.arr(re->getDg1d(), M * M);
+  out.arr(re->getWgq(), M);
+  delete da;
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+  if (argc != 3) { fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]); return 1; }
+  MPI_Init(&argc, &argv);
+  FILE *fi = fopen(argv[1], "rb");
+  FILE *fo = fopen(argv[2], "wb");
+  if (!fi || !fo) { fprintf(stderr, "cannot open files\n"); return 1; }
+  Reader in{fi};
+  Writer out{fo};
+  char magic[4];
+  in.arr(magic, 4);
+  if (std::memcmp(magic, "DKTI", 4) != 0) { fprintf(stderr, "bad magic\n"); return 1; }
+  const int dim = in.get<int32_t>(), maxDepth = in.get<int32_t>(), order = in.get<int32_t>();
+  const int op = in.get<int32_t>(), inputKind = in.get<int32_t>(), nCalls = in.get<int32_t>();
+  const uint64_t seed = in.get<uint64_t>();
+  int rc = 1;
+  if (dim == 2) rc = run<2>(in, out, maxDepth, order, op, inputKind, nCalls, seed);
+  else if (dim == 3) rc = run<3>(in, out, maxDepth, order, op, inputKind, nCalls, seed);
+  else if (dim == 4) rc = run<4>(in, out, maxDepth, order, op, inputKind, nCalls, seed);
+  fclose(fi);
+  fclose(fo);
+  MPI_Finalize();
+  return rc;
+}

@@ -1,0 +1,94 @@
+"""Generate the golden fixtures in this folder from the reference build.
+
+Runs only where the reference sources exist: builds oracle/ref (the
+unmodified Dendro-KT sources + single-rank MPI stand-in) and records, for a
+set of small meshes, the reference's own outputs:
+  tree (SFC order), DA node list (coords, levels), boundary node ids,
+  input vector x, feMatrix::matVec output y, raw fem::matvec output y_raw,
+  and the RefElement 1D operators.
+Usage:  python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+import refio  # noqa: E402
+import trees  # noqa: E402
+
+REF_DIR = os.path.join(REPO, "oracle", "_ref")
+
+
+def build_ref():
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j2"], check=True)
+
+
+def run_ref(curve, dim, md, order, op, coords, levels, kind, seed, x=None):
+    exe = os.path.join(REF_DIR, "ref_driver_" + curve)
+    inp = os.path.join("/tmp", "dkt_golden_in.bin")
+    out = os.path.join("/tmp", "dkt_golden_out.bin")
+    refio.write_input(inp, dim, md, order, op, coords, levels, input_kind=kind, seed=seed, x=x)
+    subprocess.run([exe, inp, out], check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    return refio.read_output(out, dim)
+
+
+def cases():
+    # (name, curve, dim, md, order, op, source)
+    out = []
+    for curve in ("morton", "hilbert"):
+        for dim in (2, 3, 4):
+            md = 6 if dim < 4 else 5
+            for order in (1, 2):
+                lv = {2: (4, 3, 3), 3: (4, 3, 3), 4: (3, 2, 3)}[dim]
+                if dim == 4 and order == 2:
+                    lv = (3, 2, 2)
+                for ex, L in zip(("ex1", "ex2", "ex3"), lv):
+                    for op in (0, 2):
+                        out.append((f"{curve}_d{dim}_p{order}_op{op}_{ex}L{L}", curve, dim, md, order, op, (ex, L)))
+        # Gaussian point clouds through locTreeBalancing
+        for dim, n, md in ((2, 200, 8), (3, 300, 8), (4, 40, 6)):
+            out.append((f"{curve}_d{dim}_p1_op2_gauss{n}", curve, dim, md, 1, 2, ("gauss", n)))
+            out.append((f"{curve}_d{dim}_p2_op2_gauss{n}", curve, dim, md + 1, 2, 2, ("gauss_shift", n)))
+        out.append((f"{curve}_d3_p1_op1_gauss300", curve, 3, 8, 1, 1, ("gauss", 300)))
+        out.append((f"{curve}_d3_p1_op1_ex1L4", curve, 3, 6, 1, 1, ("ex1", 4)))
+    return out
+
+
+def main():
+    build_ref()
+    for name, curve, dim, md, order, op, (src, arg) in cases():
+        if src.startswith("gauss"):
+            gmd = md - 1 if src == "gauss_shift" else md
+            pts = trees.gaussian_points(arg, dim, gmd, seed=0)
+            if src == "gauss_shift":
+                # Same mesh one level finer in coordinates, so that Q2 node
+                # spacing never collapses at the deepest level.
+                tc, tl = None, None
+                r0 = run_ref(curve, dim, gmd, 1, 0, pts, None, 0, seed=1)
+                tc, tl = r0["tree_coords"] << np.uint32(1), r0["tree_levels"]
+                r = run_ref(curve, dim, md, order, op, tc, tl, 1, seed=1)
+                inputs = dict(in_kind=1, in_coords=tc, in_levels=tl)
+            else:
+                r = run_ref(curve, dim, md, order, op, pts, None, 0, seed=1)
+                inputs = dict(in_kind=0, in_coords=pts, in_levels=np.zeros(0, np.uint8))
+        else:
+            gen = getattr(trees, "example" + src[-1])
+            c, lv = gen(dim, arg, md)
+            r = run_ref(curve, dim, md, order, op, c, lv, 2, seed=1)
+            inputs = dict(in_kind=2, in_coords=c, in_levels=lv)
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            curve=curve, dim=dim, md=md, order=order, op=op, seed=1, **inputs,
+            tree_coords=r["tree_coords"], tree_levels=r["tree_levels"],
+            node_coords=r["node_coords"], node_levels=r["node_levels"], bdry=r["bdry"],
+            x=r["x"], y=r["y"], y_raw=r["y_raw"],
+            ip0=r["ip0"], ip1=r["ip1"], Q1d=r["Q1d"], Dg=r["Dg"], W=r["W"])
+        print(name, r["tree_levels"].size, r["node_levels"].size)
+
+
+if __name__ == "__main__":
+    main()
