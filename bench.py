@@ -1,0 +1,305 @@
+"""Benchmark of the GB300 k-tree matvec (feMatrix::matVec over the flattened
+fem::matvec traversal) on the spacetime moving-ball mesh.
+
+Workload (one "step" = one feMatrix::matVec over the whole mesh): dim 4
+(x,y,z,t), Q1 Laplacian + mass, FP64, every cell meeting the shell
+| |(x,y,z) - c(t)| - 0.2 | <= 2^-L with c(t) moving from (0.3,0.3,0.3) to
+(0.7,0.7,0.7) refined to level L, 2:1 balanced; nodal input uniform[-1,1]
+(seed 2).  Metric: element-matvecs per second (tree elements x steps / s).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--level L] [--order P]
+  python bench.py --impl reference ...   (the reference algorithm on the CPU)
+
+For N > 1 (torchrun) each rank runs an independent replica of the workload
+on its own GPU (the path has no exchange step on one mesh); value is the
+aggregate over ranks, timed as the maximum over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+METRIC = "elem-matvecs/s"
+MD = 10
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--level", type=int, default=7)
+    ap.add_argument("--order", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([f.strip() for f in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, nm in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def algorithmic_bytes(stats, n_nodes, npe):
+    """Bytes a leaf kernel must move per launch: x read + y write (8 B per node
+    each), per leaf visit nPe int32 node slots and one info word, per hanging
+    leaf nPe int32 parent slots, three fill-mask words and its index."""
+    nl, nh = stats["leaves"], stats["hanging_leaves"]
+    return 16 * n_nodes + (4 * npe + 4) * nl + (4 * npe + 12 + 4) * nh
+
+
+def moving_ball(dkt, level):
+    return dkt.moving_ball_tree(max_depth=MD, level=level, radius=0.2, halfwidth=2.0 ** -level)
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the reference algorithm (oracle port: a restatement of the
+# reference's recursive fem::matvec) on a bounded sample of the same mesh
+# family.
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    level, order, warmup, steps, seconds = args
+    import __graft_entry__ as ge
+    import oracle_port as orc
+    dkt = ge.load_package()
+    tc, tl = moving_ball(dkt, level)
+    orc.set_curve(4, MD)
+    sc, sl = orc.tree_sort(tc, tl, 4)
+    da = orc.DA(sc, sl, 4, order, 2)
+    x = dkt.uniform_pm1(2, da.n)
+    for _ in range(max(warmup, 1)):
+        da.matvec(x)
+    t0 = time.perf_counter()
+    calls = 0
+    while calls < steps or (time.perf_counter() - t0 < seconds and calls < 10 * steps):
+        da.matvec(x)
+        calls += 1
+        if time.perf_counter() - t0 >= seconds and calls >= 1:
+            break
+    dt = time.perf_counter() - t0
+    return sl.size * calls / dt, sl.size, calls
+
+
+def cpu_baseline(level, order, warmup, steps, seconds, procs=1):
+    """Throughput of the reference traversal restated on the CPU (oracle port),
+    `procs` independent single-threaded replicas (spawned processes)."""
+    if procs <= 1:
+        r, ne, calls = _cpu_worker((level, order, warmup, steps, seconds))
+        return r, ne, calls, 1
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_worker, [(level, order, warmup, steps, seconds)] * procs)
+    return sum(r for r, _, _ in res), res[0][1], res[0][2], procs
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    sample_level = min(a.level, 5)
+    t_start = time.perf_counter()
+    value, ne, calls, used = cpu_baseline(sample_level, a.order, a.warmup, a.steps, a.cpu_seconds, procs=cores)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "moving-ball spacetime matvec, dim 4, Q%d Laplacian+mass, FP64, level %d, "
+                               "max_depth %d" % (a.order, a.level, MD),
+                   "cpu_sample": "level %d, %d elements" % (sample_level, ne)},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": used, "kind": "port",
+                         "sample": "moving-ball level %d mesh (%d elements); %d independent single-threaded "
+                                   "replicas of the reference traversal restated (oracle port), each timing "
+                                   "%d whole fem::matvec calls" % (sample_level, ne, used, calls)},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_start,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_gpu(a, rank, world, local_rank):
+    import torch
+    import __graft_entry__ as ge
+    dkt = ge.load_package()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    t0 = time.perf_counter()
+    tc, tl = moving_ball(dkt, a.level)
+    t_mesh = time.perf_counter() - t0
+    da = dkt.DA(tc, tl, 4, order=a.order, max_depth=MD)
+    t_da = time.perf_counter() - t0 - t_mesh
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    t_plan = time.perf_counter() - t0 - t_mesh - t_da
+    n = da.n
+    ne = da.n_elem
+    st = A.stats()
+    npe = (a.order + 1) ** 4
+    x_host = torch.from_numpy(dkt.uniform_pm1(2, n)).pin_memory()
+    xd = x_host.to(dev)
+    yd = torch.empty_like(xd)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(a.warmup):
+        A.matvec(xd, yd, stream=stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    torch.cuda.synchronize(dev)
+    A.kernel_timing(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(local_rank) as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            A.matvec(xd, yd, stream=stream)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    k_ms, k_launches = A.kernel_timing(False)
+    t_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * ne * a.steps / (t_max / 1e3)
+    # end to end through the host-array entry point (pinned host in/out)
+    y_host = torch.empty(n, dtype=torch.float64).pin_memory()
+    xh = x_host.numpy()
+    for _ in range(2):
+        y_host.numpy()[:] = A.matvec_host(xh)
+    barrier()
+    e0 = time.perf_counter()
+    for _ in range(a.steps):
+        y_host.numpy()[:] = A.matvec_host(xh)
+    e_s = time.perf_counter() - e0
+    if world > 1:
+        t = torch.tensor([e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e_s = float(t.item())
+    e2e = world * ne * a.steps / e_s
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    B = algorithmic_bytes(st, n, npe)
+    k_avg_s = (k_ms / max(k_launches, 1)) / 1e3
+    achieved = B / k_avg_s / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": t_max / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "moving-ball spacetime matvec, dim 4, Q%d Laplacian+mass, FP64, level %d, "
+                               "max_depth %d" % (a.order, a.level, MD),
+                   "elements": ne, "nodes": n, "leaf_visits": st["leaves"], "hanging_leaves": st["hanging_leaves"],
+                   "stale_slots": st["stale_slots"], "parallelism": "replicas x%d" % world,
+                   "l2": "inputs larger than L2: %.2f GB of maps and vectors read per step" % (B / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_matvec_leaf",
+                     "kernel_ms": k_ms / max(k_launches, 1), "algorithmic_bytes": B},
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": 3 * a.steps,
+        "clocks": clk.summary(),
+        "setup_s": {"mesh": t_mesh, "da": t_da, "plan": t_plan},
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        sample_level = min(a.level, 5)
+        r, sne, calls, used = cpu_baseline(sample_level, a.order, 1, 3, a.cpu_seconds, procs=1)
+        out["cpu_baseline"] = {"value": r, "unit": METRIC, "cores": used, "kind": "port",
+                               "sample": "moving-ball level %d mesh (%d elements), %d fem::matvec calls of the "
+                                         "reference traversal restated (oracle port), 1 thread"
+                                         % (sample_level, sne, calls)}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    a = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        if a.impl == "gb300":
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+    else:
+        run_gpu(a, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,286 @@
+"""Python front end of the GB300 k-tree matvec library (ctypes over the C ABI).
+
+The product is the native library built from csrc/ (include/dkt_gb300.h is
+its contract); this module only loads it and wraps the calls for tests, the
+benchmark and Python users.  Device arrays are torch CUDA tensors, passed by
+address.  There is no CPU fallback: without the library or a GPU the calls
+raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+OK, E_ARG, E_CUDA, E_NOMEM, E_UNSUP, E_NOCONV, E_INTERNAL = 0, -1, -2, -3, -4, -5, -6
+CURVE_MORTON, CURVE_HILBERT = 0, 1
+OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM = 0, 1, 2, 3
+
+
+class DktError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("dkt error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib_path():
+    from . import build as _b  # noqa: F401  (package-relative when imported as a package)
+    return _b.LIB
+
+
+def load(build_if_missing=True):
+    """Load libdkt_gb300.so (building it in-tree first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_dkt_build", os.path.join(_PKG, "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    if build_if_missing and not b.up_to_date():
+        b.build()
+    if not os.path.exists(b.LIB):
+        raise RuntimeError("native library missing: %s (run __graft_entry__.build())" % b.LIB)
+    L = ctypes.CDLL(b.LIB)
+    P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    sig = {
+        "dkt_last_error": ([], ctypes.c_char_p),
+        "dkt_da_create": ([I, I, I, I, P, P, I64, I, P], I),
+        "dkt_da_local_nodal_size": ([P], I64),
+        "dkt_da_num_elements": ([P], I64),
+        "dkt_da_boundary_size": ([P], I64),
+        "dkt_da_get_nodes": ([P, P, P], I),
+        "dkt_da_get_boundary_ids": ([P, P], I),
+        "dkt_da_get_tree": ([P, P, P], I),
+        "dkt_da_destroy": ([P], None),
+        "dkt_plan_create": ([P, I, P, P], I),
+        "dkt_plan_create_from_nodes": ([I, I, I, I, P, P, I64, I, P, P], I),
+        "dkt_plan_num_nodes": ([P], I64),
+        "dkt_plan_stats": ([P, P], I),
+        "dkt_plan_export": ([P, P, P, P, P, P], I),
+        "dkt_matvec": ([P, P, P, ctypes.c_double, P], I),
+        "dkt_fematrix_matvec": ([P, P, P, ctypes.c_double, P], I),
+        "dkt_fematrix_matvec_host": ([P, P, P, ctypes.c_double], I),
+        "dkt_diagonal": ([P, P, P], I),
+        "dkt_cg_solve": ([P, P, P, I, ctypes.c_double, I, P, P, P], I),
+        "dkt_plan_kernel_timing": ([P, I, P, P], I),
+        "dkt_plan_destroy": ([P], None),
+        "dkt_mesh_gaussian_points": ([I64, I, I, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, P], I),
+        "dkt_mesh_tree_from_points": ([P, I64, I, I, I64, P, P, P], I),
+        "dkt_mesh_moving_ball": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
+        "dkt_free": ([P], None),
+        "dkt_probe_device": ([P], I),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if isinstance(a, np.ndarray) else ctypes.c_void_p(int(a.data_ptr()))
+
+
+def _check(rc):
+    if rc != OK:
+        raise DktError(rc, load().dkt_last_error().decode())
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return ctypes.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+
+
+class DA:
+    """ot::DA<dim> on one GB300: tree in SFC order, node list, boundary ids."""
+
+    def __init__(self, tree_coords, tree_levels, dim, order=1, max_depth=10, curve=CURVE_MORTON, sorted_tree=False):
+        L = load()
+        c = np.ascontiguousarray(tree_coords, dtype=np.uint32).reshape(-1, dim)
+        lv = np.ascontiguousarray(tree_levels, dtype=np.uint8)
+        h = ctypes.c_void_p()
+        _check(L.dkt_da_create(dim, order, curve, max_depth, _p(c), _p(lv), lv.size, int(bool(sorted_tree)),
+                               ctypes.byref(h)))
+        self._h, self.dim, self.order, self.max_depth = h, dim, order, max_depth
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def n(self):
+        return int(load().dkt_da_local_nodal_size(self._h))
+
+    @property
+    def n_elem(self):
+        return int(load().dkt_da_num_elements(self._h))
+
+    def nodes(self):
+        c = np.empty((self.n, self.dim), np.uint32)
+        lv = np.empty(self.n, np.uint8)
+        _check(load().dkt_da_get_nodes(self._h, _p(c), _p(lv)))
+        return c, lv
+
+    def boundary_ids(self):
+        nb = int(load().dkt_da_boundary_size(self._h))
+        ids = np.empty(max(nb, 1), np.uint32)
+        _check(load().dkt_da_get_boundary_ids(self._h, _p(ids)))
+        return ids[:nb]
+
+    def tree(self):
+        ne = self.n_elem
+        c = np.empty((ne, self.dim), np.uint32)
+        lv = np.empty(ne, np.uint8)
+        _check(load().dkt_da_get_tree(self._h, _p(c), _p(lv)))
+        return c, lv
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                load().dkt_da_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class Matrix:
+    """feMatrix<LeafT,dim> over a DA (or a bare node list) with a device plan."""
+
+    def __init__(self, da=None, op=OP_LAPMASS, tables=None, nodes=None, dim=None, order=1, max_depth=10,
+                 curve=CURVE_MORTON):
+        L = load()
+        h = ctypes.c_void_p()
+        t = None if tables is None else np.ascontiguousarray(tables, dtype=np.float64)
+        tp = None if t is None else _p(t)
+        if da is not None:
+            _check(L.dkt_plan_create(da.handle, op, tp, ctypes.byref(h)))
+        else:
+            c = np.ascontiguousarray(nodes[0], dtype=np.uint32).reshape(-1, dim)
+            lv = np.ascontiguousarray(nodes[1], dtype=np.uint8)
+            _check(L.dkt_plan_create_from_nodes(dim, order, curve, max_depth, _p(c), _p(lv), lv.size, op, tp,
+                                                ctypes.byref(h)))
+        self._h = h
+        self.n = int(L.dkt_plan_num_nodes(h))
+        self.dim = da.dim if da is not None else dim
+        self.order = da.order if da is not None else order
+        self.npe = (self.order + 1) ** self.dim
+
+    def stats(self):
+        s = np.zeros(4, np.int64)
+        _check(load().dkt_plan_stats(self._h, _p(s)))
+        return dict(zip(["leaves", "hanging_leaves", "stale_slots", "boundary_nodes"], s.tolist()))
+
+    def export(self):
+        """The flattened traversal as numpy arrays (e2n, info, hidx, p2n, fill)."""
+        st = self.stats()
+        nl, nh = st["leaves"], st["hanging_leaves"]
+        npe = self.npe
+        e2n = np.empty((npe, nl), np.int32)
+        info = np.empty(nl, np.uint32)
+        hidx = np.empty(nl, np.int32)
+        p2n = np.empty((npe, max(nh, 1)), np.int32)
+        fill = np.empty((3, max(nh, 1)), np.uint32)
+        _check(load().dkt_plan_export(self._h, _p(e2n), _p(info), _p(hidx), _p(p2n), _p(fill)))
+        return e2n, info, hidx, p2n[:, :nh], fill[:, :nh]
+
+    def matvec_raw(self, x_dev, y_dev, scale=1.0, stream=None):
+        """fem::matvec on device tensors (no boundary handling)."""
+        _check(load().dkt_matvec(self._h, _p(x_dev), _p(y_dev), scale, _stream(stream)))
+
+    def matvec(self, x_dev, y_dev, scale=1.0, stream=None):
+        """feMatrix::matVec on device tensors."""
+        _check(load().dkt_fematrix_matvec(self._h, _p(x_dev), _p(y_dev), scale, _stream(stream)))
+
+    def matvec_host(self, x, scale=1.0):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.n)
+        _check(load().dkt_fematrix_matvec_host(self._h, _p(x), _p(y), scale))
+        return y
+
+    def kernel_timing(self, enable):
+        """Close the current timing window; returns (total kernel ms, launches)."""
+        ms = ctypes.c_double(0.0)
+        n = ctypes.c_int64(0)
+        _check(load().dkt_plan_kernel_timing(self._h, int(bool(enable)), ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def diagonal(self, d_dev, stream=None):
+        _check(load().dkt_diagonal(self._h, _p(d_dev), _stream(stream)))
+
+    def cg(self, b_dev, x_dev, max_iter=10000, tol=1e-10, jacobi=True, stream=None):
+        it = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        rc = load().dkt_cg_solve(self._h, _p(b_dev), _p(x_dev), max_iter, tol, int(bool(jacobi)),
+                                 ctypes.byref(it), ctypes.byref(rr), _stream(stream))
+        if rc not in (OK, E_NOCONV):
+            _check(rc)
+        return it.value, rr.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                load().dkt_plan_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def probe_device():
+    """FP64 FMA / FP64 add / FP32 FMA / int64 add throughput of the current GPU."""
+    out = np.zeros(4)
+    _check(load().dkt_probe_device(_p(out)))
+    return dict(zip(["fp64_fma_tflops", "fp64_add_tops", "fp32_fma_tflops", "int64_add_tops"], out.tolist()))
+
+
+def gaussian_points(n, dim, max_depth, mean=0.5, sd=0.1, seed=0):
+    out = np.empty((n, dim), np.uint32)
+    _check(load().dkt_mesh_gaussian_points(n, dim, max_depth, mean, sd, seed, _p(out)))
+    return out
+
+
+def _take_cells(n, c, lv, dim):
+    L = load()
+    try:
+        coords = np.ctypeslib.as_array(ctypes.cast(c, ctypes.POINTER(ctypes.c_uint32)), shape=(n.value * dim,)).copy()
+        levels = np.ctypeslib.as_array(ctypes.cast(lv, ctypes.POINTER(ctypes.c_uint8)), shape=(n.value,)).copy()
+    finally:
+        L.dkt_free(c)
+        L.dkt_free(lv)
+    return coords.reshape(-1, dim), levels
+
+
+def tree_from_points(points, dim, max_depth, max_pts=1):
+    pts = np.ascontiguousarray(points, dtype=np.uint32).reshape(-1, dim)
+    n, c, lv = ctypes.c_int64(0), ctypes.c_void_p(), ctypes.c_void_p()
+    _check(load().dkt_mesh_tree_from_points(_p(pts), pts.shape[0], dim, max_depth, max_pts, ctypes.byref(n),
+                                            ctypes.byref(c), ctypes.byref(lv)))
+    return _take_cells(n, c, lv, dim)
+
+
+def moving_ball_tree(max_depth, level, radius=0.2, halfwidth=None, c0=(0.3, 0.3, 0.3), c1=(0.7, 0.7, 0.7)):
+    if halfwidth is None:
+        halfwidth = 2.0 ** -level
+    a0 = np.ascontiguousarray(c0, dtype=np.float64)
+    a1 = np.ascontiguousarray(c1, dtype=np.float64)
+    n, c, lv = ctypes.c_int64(0), ctypes.c_void_p(), ctypes.c_void_p()
+    _check(load().dkt_mesh_moving_ball(max_depth, level, radius, halfwidth, _p(a0), _p(a1), ctypes.byref(n),
+                                       ctypes.byref(c), ctypes.byref(lv)))
+    return _take_cells(n, c, lv, 4)
+
+
+def uniform_pm1(seed, n):
+    """Nodal vector x_i = 2u - 1 from the counter-based stream used everywhere
+    in this project (top 53 bits of splitmix64(seed * K + i))."""
+    def splitmix64(z):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+    with np.errstate(over="ignore"):
+        r = splitmix64(np.uint64(seed) * np.uint64(0xD1B54A32D192ED03) + np.arange(n, dtype=np.uint64))
+    return 2.0 * ((r >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)) - 1.0

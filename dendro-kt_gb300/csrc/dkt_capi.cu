@@ -1,0 +1,400 @@
+// C ABI (include/dkt_gb300.h): argument checking, error codes, object
+// lifetimes, host<->device movement.  All compute runs in the kernels of
+// dkt_da.cu, dkt_plan.cu and dkt_matvec.cu.
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "dkt_internal.cuh"
+#include "../../include/dkt_gb300.h"
+#include "../../include/dkt_gb300_mesh.h"
+#include "dkt_host.h"
+
+namespace dkt {
+void sort_tree(DA &da, cudaStream_t s);
+void build_da_nodes(DA &da, cudaStream_t s);
+void boundary_ids(const uint32_t *nx, int64_t n, int dim, int md, DBuf<uint32_t> &out, int64_t &nb, cudaStream_t s);
+void build_plan(Plan &pl, const uint32_t *node_x, const uint8_t *node_lev, int64_t n_nodes, const CurveHost &cv,
+                const double *ip_host, cudaStream_t s);
+void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
+void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
+void diagonal(const Plan &pl, double *diag, cudaStream_t s);
+int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,
+             cudaStream_t s);
+
+}  // namespace dkt
+
+struct dkt_da_s {
+  dkt::DA da;
+};
+struct dkt_plan_s {
+  dkt::Plan pl;
+};
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+  g_err = msg;
+  return code;
+}
+
+template <typename F>
+int guarded(F &&f)
+{
+  try {
+    return f();
+  } catch (const std::bad_alloc &e) {
+    return fail(DKT_E_NOMEM, std::string("host allocation failed: ") + e.what());
+  } catch (const std::invalid_argument &e) {
+    return fail(DKT_E_ARG, e.what());
+  } catch (const std::runtime_error &e) {
+    const std::string m = e.what();
+    if (m.find("out of memory") != std::string::npos) return fail(DKT_E_NOMEM, m);
+    if (m.find("CUDA") != std::string::npos || m.find("launch") != std::string::npos) return fail(DKT_E_CUDA, m);
+    return fail(DKT_E_INTERNAL, m);
+  } catch (...) {
+    return fail(DKT_E_INTERNAL, "unknown exception");
+  }
+}
+
+int check_cfg(int dim, int order, int curve, int md)
+{
+  if (dim < 2 || dim > 4) return fail(DKT_E_ARG, "dim must be 2, 3 or 4");
+  if (order < 1 || order > 2) return fail(DKT_E_UNSUP, "element order must be 1 or 2");
+  if (curve != DKT_CURVE_MORTON && curve != DKT_CURVE_HILBERT) return fail(DKT_E_ARG, "unknown curve");
+  if (curve == DKT_CURVE_HILBERT) return fail(DKT_E_UNSUP, "Hilbert ordering is not available in this build");
+  if (md < 1 || md > 30) return fail(DKT_E_ARG, "max_depth out of range");
+  if (dim * md + 6 > 64) return fail(DKT_E_UNSUP, "dim * max_depth too large (cell keys are 64-bit)");
+  return DKT_OK;
+}
+
+void setup_operator(dkt::Plan &pl, int op, const double *tables, cudaStream_t s)
+{
+  if (op < 0 || op > 3) throw std::invalid_argument("unknown operator");
+  pl.op.kind = op;
+  pl.op.npe = pl.npe;
+  pl.op.nlev = pl.md + 1;
+  if (op == DKT_OP_CUSTOM) {
+    if (!tables) throw std::invalid_argument("custom operator needs tables");
+    const size_t n = (size_t) (pl.md + 1) * pl.npe * pl.npe;
+    pl.op.table.assign(tables, tables + n);
+    pl.op.uses_scale = true;
+    pl.opTable.upload(pl.op.table.data(), n, s);
+    return;
+  }
+  dkt::builtin_operator(op, pl.dim, pl.order, pl.md, pl.op.A, pl.op.B, pl.op.alpha, pl.op.beta, pl.op.uses_scale);
+  pl.opA.upload(pl.op.A.data(), pl.op.A.size(), s);
+  pl.opB.upload(pl.op.B.data(), pl.op.B.size(), s);
+  pl.opAlpha.upload(pl.op.alpha.data(), pl.op.alpha.size(), s);
+  pl.opBeta.upload(pl.op.beta.data(), pl.op.beta.size(), s);
+}
+
+std::vector<double> interp_tables(int p)
+{
+  const dkt::RefEl1D re = dkt::refel_1d(p);
+  std::vector<double> ip(re.ip0);
+  ip.insert(ip.end(), re.ip1.begin(), re.ip1.end());
+  return ip;
+}
+}  // namespace
+
+extern "C" {
+
+const char *dkt_last_error(void) { return g_err.c_str(); }
+
+int dkt_da_create(int dim, int order, int curve, int max_depth, const uint32_t *tree_coords,
+                  const uint8_t *tree_levels, int64_t n_elem, int tree_is_sorted, dkt_da *out)
+{
+  if (!out || !tree_coords || !tree_levels || n_elem <= 0) return fail(DKT_E_ARG, "null or empty tree");
+  if (int rc = check_cfg(dim, order, curve, max_depth)) return rc;
+  return guarded([&]() {
+    for (int64_t i = 0; i < n_elem; i++) {
+      if ((int) tree_levels[i] > max_depth) throw std::invalid_argument("element level exceeds max_depth");
+      const uint32_t len = 1u << (max_depth - tree_levels[i]);
+      for (int d = 0; d < dim; d++) {
+        const uint32_t x = tree_coords[i * dim + d];
+        if (x >= (1u << max_depth) || (x & (len - 1u))) throw std::invalid_argument("element anchor not aligned or outside the domain");
+      }
+    }
+    dkt_da_s *h = new dkt_da_s();
+    dkt::DA &da = h->da;
+    da.dim = dim; da.order = order; da.md = max_depth; da.curve = curve; da.n_elem = n_elem;
+    da.cv.morton(dim);
+    da.cv.upload();
+    cudaStream_t s = 0;
+    try {
+      da.elem_x.upload(tree_coords, (size_t) n_elem * dim, s);
+      da.elem_lev.upload(tree_levels, (size_t) n_elem, s);
+      if (!tree_is_sorted) dkt::sort_tree(da, s);
+      dkt::build_da_nodes(da, s);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+    return DKT_OK;
+  });
+}
+
+int64_t dkt_da_local_nodal_size(dkt_da da) { return da ? da->da.n_nodes : -1; }
+int64_t dkt_da_num_elements(dkt_da da) { return da ? da->da.n_elem : -1; }
+int64_t dkt_da_boundary_size(dkt_da da) { return da ? da->da.n_bdry : -1; }
+
+int dkt_da_get_nodes(dkt_da da, uint32_t *coords, uint8_t *levels)
+{
+  if (!da || !coords || !levels) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    const dkt::DA &d = da->da;
+    DKT_CUDA(cudaMemcpy(coords, d.node_x.p, (size_t) d.n_nodes * d.dim * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    DKT_CUDA(cudaMemcpy(levels, d.node_lev.p, (size_t) d.n_nodes, cudaMemcpyDeviceToHost));
+    return DKT_OK;
+  });
+}
+
+int dkt_da_get_boundary_ids(dkt_da da, uint32_t *ids)
+{
+  if (!da || (!ids && da->da.n_bdry > 0)) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    if (da->da.n_bdry > 0)
+      DKT_CUDA(cudaMemcpy(ids, da->da.bdry.p, (size_t) da->da.n_bdry * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return DKT_OK;
+  });
+}
+
+int dkt_da_get_tree(dkt_da da, uint32_t *coords, uint8_t *levels)
+{
+  if (!da || !coords || !levels) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    const dkt::DA &d = da->da;
+    DKT_CUDA(cudaMemcpy(coords, d.elem_x.p, (size_t) d.n_elem * d.dim * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    DKT_CUDA(cudaMemcpy(levels, d.elem_lev.p, (size_t) d.n_elem, cudaMemcpyDeviceToHost));
+    return DKT_OK;
+  });
+}
+
+void dkt_da_destroy(dkt_da da) { delete da; }
+
+static int plan_common(int dim, int order, int curve, int md, const uint32_t *node_x_dev, const uint8_t *node_lev_dev,
+                       int64_t n, const uint32_t *bdry_dev, int64_t nb, int op, const double *tables, dkt_plan *out)
+{
+  dkt_plan_s *h = new dkt_plan_s();
+  try {
+    dkt::Plan &pl = h->pl;
+    pl.dim = dim; pl.order = order; pl.md = md;
+    cudaStream_t s = 0;
+    dkt::CurveHost cv;
+    cv.morton(dim);
+    cv.upload();
+    const std::vector<double> ip = interp_tables(order);
+    dkt::build_plan(pl, node_x_dev, node_lev_dev, n, cv, ip.data(), s);
+    setup_operator(pl, op, tables, s);
+    if (bdry_dev) {
+      pl.bdry.alloc(nb > 0 ? nb : 1);
+      if (nb > 0) DKT_CUDA(cudaMemcpyAsync(pl.bdry.p, bdry_dev, nb * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+      pl.n_bdry = nb;
+    } else {
+      dkt::boundary_ids(node_x_dev, n, dim, md, pl.bdry, pl.n_bdry, s);
+    }
+    DKT_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    delete h;
+    throw;
+  }
+  *out = h;
+  return DKT_OK;
+}
+
+int dkt_plan_create(dkt_da da, int op, const double *op_tables, dkt_plan *out)
+{
+  if (!da || !out) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    const dkt::DA &d = da->da;
+    return plan_common(d.dim, d.order, d.curve, d.md, d.node_x.p, d.node_lev.p, d.n_nodes, d.bdry.p, d.n_bdry, op,
+                       op_tables, out);
+  });
+}
+
+int dkt_plan_create_from_nodes(int dim, int order, int curve, int max_depth, const uint32_t *node_coords,
+                               const uint8_t *node_levels, int64_t sz, int op, const double *op_tables,
+                               dkt_plan *out)
+{
+  if (!out || !node_coords || !node_levels || sz <= 0) return fail(DKT_E_ARG, "null or empty node list");
+  if (int rc = check_cfg(dim, order, curve, max_depth)) return rc;
+  return guarded([&]() {
+    for (int64_t i = 0; i < sz; i++) {
+      if ((int) node_levels[i] > max_depth) throw std::invalid_argument("node level exceeds max_depth");
+      for (int d = 0; d < dim; d++)
+        if (node_coords[i * dim + d] > (1u << max_depth)) throw std::invalid_argument("node outside the domain");
+    }
+    dkt::DBuf<uint32_t> nx;
+    dkt::DBuf<uint8_t> nl;
+    nx.upload(node_coords, (size_t) sz * dim);
+    nl.upload(node_levels, (size_t) sz);
+    return plan_common(dim, order, curve, max_depth, nx.p, nl.p, sz, nullptr, 0, op, op_tables, out);
+  });
+}
+
+int64_t dkt_plan_num_nodes(dkt_plan plan) { return plan ? plan->pl.n_nodes : -1; }
+
+int dkt_plan_stats(dkt_plan plan, int64_t *out4)
+{
+  if (!plan || !out4) return fail(DKT_E_ARG, "null argument");
+  out4[0] = plan->pl.n_leaf;
+  out4[1] = plan->pl.n_hang;
+  out4[2] = plan->pl.stale_slots;
+  out4[3] = plan->pl.n_bdry;
+  return DKT_OK;
+}
+
+int dkt_plan_export(dkt_plan plan, int32_t *e2n, uint32_t *info, int32_t *hidx, int32_t *p2n, uint32_t *fill)
+{
+  if (!plan) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    const dkt::Plan &pl = plan->pl;
+    const size_t nl = (size_t) pl.n_leaf, nh = (size_t) pl.n_hang, npe = (size_t) pl.npe;
+    if (e2n) DKT_CUDA(cudaMemcpy(e2n, pl.e2n.p, npe * nl * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (info) DKT_CUDA(cudaMemcpy(info, pl.info.p, nl * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (hidx) DKT_CUDA(cudaMemcpy(hidx, pl.hidx.p, nl * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (p2n && nh) DKT_CUDA(cudaMemcpy(p2n, pl.p2n.p, npe * nh * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (fill && nh) DKT_CUDA(cudaMemcpy(fill, pl.fill.p, 3 * nh * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return DKT_OK;
+  });
+}
+
+int dkt_matvec(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream)
+{
+  if (!plan || !x_dev || !y_dev) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    dkt::matvec(plan->pl, x_dev, y_dev, scale, (cudaStream_t) stream);
+    return DKT_OK;
+  });
+}
+
+int dkt_fematrix_matvec(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream)
+{
+  if (!plan || !x_dev || !y_dev) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    dkt::fematrix_matvec(plan->pl, x_dev, y_dev, scale, (cudaStream_t) stream);
+    return DKT_OK;
+  });
+}
+
+int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host, double scale)
+{
+  if (!plan || !x_host || !y_host) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    dkt::Plan &pl = plan->pl;
+    const int64_t n = pl.n_nodes;
+    if (pl.xh.n < (size_t) n) pl.xh.alloc(n);
+    if (pl.yh.n < (size_t) n) pl.yh.alloc(n);
+    DKT_CUDA(cudaMemcpyAsync(pl.xh.p, x_host, n * sizeof(double), cudaMemcpyHostToDevice, 0));
+    dkt::fematrix_matvec(pl, pl.xh.p, pl.yh.p, scale, 0);
+    DKT_CUDA(cudaMemcpyAsync(y_host, pl.yh.p, n * sizeof(double), cudaMemcpyDeviceToHost, 0));
+    DKT_CUDA(cudaStreamSynchronize(0));
+    return DKT_OK;
+  });
+}
+
+int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream)
+{
+  if (!plan || !diag_dev) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    dkt::diagonal(plan->pl, diag_dev, (cudaStream_t) stream);
+    return DKT_OK;
+  });
+}
+
+int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int jacobi,
+                 int *iters, double *relres, void *stream)
+{
+  if (!plan || !b_dev || !x_dev || max_iter < 0 || !(tol > 0)) return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    return dkt::cg_solve(plan->pl, b_dev, x_dev, max_iter, tol, jacobi != 0, iters, relres, (cudaStream_t) stream);
+  });
+}
+
+int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t *launches)
+{
+  if (!plan) return fail(DKT_E_ARG, "null argument");
+  return guarded([&]() {
+    dkt::Plan &pl = plan->pl;
+    double tot = 0.0;
+    for (size_t k = 0; k + 1 < pl.ev.size(); k += 2) {
+      DKT_CUDA(cudaEventSynchronize(pl.ev[k + 1]));
+      float ms = 0.f;
+      DKT_CUDA(cudaEventElapsedTime(&ms, pl.ev[k], pl.ev[k + 1]));
+      tot += ms;
+    }
+    for (cudaEvent_t e : pl.ev) cudaEventDestroy(e);
+    pl.ev.clear();
+    if (total_ms) *total_ms = tot;
+    if (launches) *launches = pl.timed_launches;
+    pl.timed_launches = 0;
+    pl.timing = enable != 0;
+    return DKT_OK;
+  });
+}
+
+void dkt_plan_destroy(dkt_plan plan)
+{
+  if (!plan) return;
+  for (cudaEvent_t e : plan->pl.ev) cudaEventDestroy(e);
+  delete plan;
+}
+
+// ---- mesh generation (include/dkt_gb300_mesh.h) ----
+int dkt_mesh_gaussian_points(int64_t n, int dim, int max_depth, double mean, double sd, uint64_t seed,
+                             uint32_t *out)
+{
+  if (!out || n < 0 || dim < 2 || dim > 4 || max_depth < 1 || max_depth > 30) return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    dkt::gaussian_points(n, dim, max_depth, mean, sd, seed, out);
+    return DKT_OK;
+  });
+}
+
+static int export_cells(const std::vector<dkt::Cell> &cells, int dim, int64_t *n_out, uint32_t **coords,
+                        uint8_t **levels)
+{
+  const size_t n = cells.size();
+  uint32_t *c = (uint32_t *) std::malloc(n * dim * sizeof(uint32_t) + 1);
+  uint8_t *l = (uint8_t *) std::malloc(n + 1);
+  if (!c || !l) { std::free(c); std::free(l); return fail(DKT_E_NOMEM, "host allocation failed"); }
+  for (size_t i = 0; i < n; i++) {
+    for (int d = 0; d < dim; d++) c[i * dim + d] = cells[i].x[d];
+    l[i] = (uint8_t) cells[i].lev;
+  }
+  *n_out = (int64_t) n;
+  *coords = c;
+  *levels = l;
+  return DKT_OK;
+}
+
+int dkt_mesh_tree_from_points(const uint32_t *pts, int64_t n, int dim, int max_depth, int64_t max_pts,
+                              int64_t *n_out, uint32_t **coords, uint8_t **levels)
+{
+  if (!pts || !n_out || !coords || !levels || n <= 0 || dim < 2 || dim > 4 || max_pts < 1)
+    return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    const auto cells = dkt::tree_from_points(pts, n, dim, max_depth, max_pts);
+    return export_cells(cells, dim, n_out, coords, levels);
+  });
+}
+
+int dkt_mesh_moving_ball(int max_depth, int level, double radius, double halfwidth, const double *c0,
+                         const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels)
+{
+  if (!c0 || !c1 || !n_out || !coords || !levels || level < 1 || level > max_depth) return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    const auto cells = dkt::moving_ball_tree(max_depth, level, radius, halfwidth, c0, c1);
+    return export_cells(cells, 4, n_out, coords, levels);
+  });
+}
+
+void dkt_free(void *p) { std::free(p); }
+
+}  // extern "C"

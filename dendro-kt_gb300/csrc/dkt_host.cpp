@@ -1,0 +1,377 @@
+// Host-side pieces of the product: reference-element operators and the mesh
+// generators that produce the input trees (the callers of the matvec path).
+//
+//  * refel_1d: the 1D operators of RefElement (FEM/src/refel.cpp:75-220) from
+//    the mathematics -- Lagrange basis on equispaced nodes, Gauss-Legendre
+//    quadrature -- in the reference's storage convention A[k*M + j] = basis k
+//    evaluated at point j.
+//  * element matrices of the built-in operators, dense in lexicographic rank
+//    order (x fastest).
+//  * tree construction and 2:1 balancing with the semantics of
+//    SFC_Tree::locTreeConstruction / propagateNeighbours / locTreeBalancing
+//    (src/tsort.cpp:566-854), organised by level sets instead of recursive
+//    bucketing.
+//  * the moving-ball spacetime mesh (dim 4).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <unordered_set>
+#include <vector>
+
+#include "dkt_host.h"
+
+namespace dkt {
+
+static double lag(const std::vector<double> &u, int k, double x)
+{
+  double v = 1.0;
+  for (int m = 0; m < (int) u.size(); m++) if (m != k) v *= (x - u[m]) / (u[k] - u[m]);
+  return v;
+}
+static double lag_d(const std::vector<double> &u, int k, double x)
+{
+  double s = 0.0;
+  for (int i = 0; i < (int) u.size(); i++) {
+    if (i == k) continue;
+    double t = 1.0 / (u[k] - u[i]);
+    for (int m = 0; m < (int) u.size(); m++) if (m != k && m != i) t *= (x - u[m]) / (u[k] - u[m]);
+    s += t;
+  }
+  return s;
+}
+
+RefEl1D refel_1d(int p)
+{
+  RefEl1D r;
+  r.p = p;
+  r.M = p + 1;
+  const int M = r.M;
+  std::vector<double> u(M), g(M), w(M);
+  for (int k = 0; k < M; k++) u[k] = -1.0 + 2.0 * k / p;
+  for (int i = 0; i < M; i++) {
+    double x = -std::cos(M_PI * (i + 0.75) / (M + 0.5)), dp = 1.0;
+    for (int it = 0; it < 60; it++) {
+      double p0 = 1.0, p1 = x;
+      for (int n = 2; n <= M; n++) { double p2 = ((2.0 * n - 1) * x * p1 - (n - 1.0) * p0) / n; p0 = p1; p1 = p2; }
+      dp = M * (x * p1 - p0) / (x * x - 1.0);
+      const double dx = p1 / dp;
+      x -= dx;
+      if (std::fabs(dx) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = x;
+    for (int n = 2; n <= M; n++) { double p2 = ((2.0 * n - 1) * x * p1 - (n - 1.0) * p0) / n; p0 = p1; p1 = p2; }
+    dp = M * (x * p1 - p0) / (x * x - 1.0);
+    g[i] = x;
+    w[i] = 2.0 / ((1.0 - x * x) * dp * dp);
+  }
+  r.ip0.resize(M * M); r.ip1.resize(M * M); r.Q.resize(M * M); r.D.resize(M * M); r.W = w;
+  for (int k = 0; k < M; k++)
+    for (int j = 0; j < M; j++) {
+      r.ip0[k * M + j] = lag(u, k, 0.5 * (u[j] - 1.0));
+      r.ip1[k * M + j] = lag(u, k, 0.5 * (u[j] + 1.0));
+      r.Q[k * M + j] = lag(u, k, g[j]);
+      r.D[k * M + j] = lag_d(u, k, g[j]);
+    }
+  return r;
+}
+
+// Dense element matrix sum_g w_g * (prod_d B_d[c_d][g_d]) * (prod_d B_d[r_d][g_d])
+// over tensor Gauss points g, with B_d = D on axis `deriv` and Q elsewhere
+// (deriv < 0: mass).  Only axes < nax carry the quadrature; further axes (the
+// 3-axis HeatMat on more dimensions) are left out.
+static void tensor_matrix(const RefEl1D &re, int dim, int deriv, std::vector<double> &Kout)
+{
+  const int M = re.M;
+  int npe = 1;
+  for (int d = 0; d < dim; d++) npe *= M;
+  Kout.assign((size_t) npe * npe, 0.0);
+  for (int r = 0; r < npe; r++)
+    for (int c = 0; c < npe; c++) {
+      double v = 1.0;
+      int rr = r, cc = c;
+      for (int d = 0; d < dim; d++) {
+        const int rd = rr % M, cd = cc % M;
+        rr /= M; cc /= M;
+        const std::vector<double> &B = (d == deriv) ? re.D : re.Q;
+        double s = 0.0;
+        for (int g = 0; g < M; g++) s += re.W[g] * B[cd * M + g] * B[rd * M + g];
+        v *= s;
+      }
+      Kout[(size_t) r * npe + c] = v;
+    }
+}
+
+// Built-in operators: K_L = alpha[L] A + beta[L] B, L = 0..md, element side
+// h_L = 2^-L on the unit domain, J = h/2.
+void builtin_operator(int kind, int dim, int p, int md, std::vector<double> &A, std::vector<double> &B,
+                      std::vector<double> &alpha, std::vector<double> &beta, bool &uses_scale)
+{
+  const RefEl1D re = refel_1d(p);
+  int npe = 1;
+  for (int d = 0; d < dim; d++) npe *= re.M;
+  A.assign((size_t) npe * npe, 0.0);
+  B.assign((size_t) npe * npe, 0.0);
+  alpha.assign(md + 1, 0.0);
+  beta.assign(md + 1, 0.0);
+  uses_scale = true;
+  if (kind == 0) {   // identity
+    for (int r = 0; r < npe; r++) A[(size_t) r * npe + r] = 1.0;
+    for (int l = 0; l <= md; l++) alpha[l] = 1.0;
+    return;
+  }
+  std::vector<double> K;
+  for (int t = 0; t < dim; t++) {
+    tensor_matrix(re, dim, t, K);
+    for (size_t i = 0; i < K.size(); i++) A[i] += K[i];
+  }
+  if (kind == 1) {   // HeatMat<3>: sum_t (prod_{d!=t} J / J) = J
+    if (dim != 3) throw std::invalid_argument("the HeatMat operator is defined for dim 3");
+    uses_scale = false;
+    for (int l = 0; l <= md; l++) alpha[l] = 0.5 * std::ldexp(1.0, -l);
+    return;
+  }
+  tensor_matrix(re, dim, -1, B);   // mass
+  for (int l = 0; l <= md; l++) {
+    const double J = 0.5 * std::ldexp(1.0, -l);
+    alpha[l] = std::pow(J, dim - 2);
+    beta[l] = std::pow(J, dim);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mesh generation (input side).
+// ---------------------------------------------------------------------------
+static inline uint64_t splitmix64(uint64_t z)
+{
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static inline double u01(uint64_t seed, uint64_t i)
+{
+  return (double) (splitmix64(seed * 0xD1B54A32D192ED03ull + i) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// n points, each coordinate N(mean, sd) clipped to the unit cube (Box-Muller
+// on a counter-based uniform stream), quantised to level md.
+void gaussian_points(int64_t n, int dim, int md, double mean, double sd, uint64_t seed, uint32_t *out)
+{
+  const double top = (double) (1u << md);
+  for (int64_t i = 0; i < n; i++)
+    for (int d = 0; d < dim; d++) {
+      const uint64_t k = (uint64_t) (i * dim + d);
+      double a = u01(seed, 2 * k), b = u01(seed, 2 * k + 1);
+      if (a <= 0.0) a = 1e-300;
+      double z = std::sqrt(-2.0 * std::log(a)) * std::cos(2.0 * M_PI * b);
+      double v = mean + sd * z;
+      v = std::min(std::max(v, 0.0), 1.0 - std::ldexp(1.0, -md));
+      out[i * dim + d] = (uint32_t) std::floor(v * top);
+    }
+}
+
+static inline uint64_t ckey(const Cell &c, int dim, int md)
+{
+  uint64_t k = (uint64_t) c.lev;
+  for (int d = dim - 1; d >= 0; d--) k = (k << md) | c.x[d];
+  return k;
+}
+static inline Cell cdecode(uint64_t k, int dim, int md)
+{
+  Cell c;
+  const uint64_t m = (1ull << md) - 1;
+  for (int d = 0; d < dim; d++) { c.x[d] = (uint32_t) (k & m); k >>= md; }
+  c.lev = (int) k;
+  return c;
+}
+static inline Cell cparent(const Cell &c, int md)
+{
+  Cell p = c;
+  p.lev = c.lev - 1;
+  const uint32_t mask = ~((1u << (md - p.lev)) - 1u);
+  for (int d = 0; d < 4; d++) p.x[d] &= mask;
+  return p;
+}
+
+// Complete tree in which every leaf above level md holds at most max_pts
+// points (locTreeConstruction): recursive split of Morton-sorted points.
+static void construct(const std::vector<uint64_t> &pk, size_t b, size_t e, const Cell &c, int dim, int md,
+                      int64_t max_pts, std::vector<Cell> &leaves)
+{
+  const int nc = 1 << dim;
+  // points are sorted by interleaved Morton key of full resolution
+  for (int ch = 0; ch < nc; ch++) {
+    Cell k = c;
+    k.lev = c.lev + 1;
+    const uint32_t cl = 1u << (md - k.lev);
+    for (int d = 0; d < dim; d++) k.x[d] = c.x[d] | (((ch >> d) & 1) ? cl : 0u);
+    // key range of the child: interleaved prefix
+    uint64_t lo = 0;
+    for (int bit = md - 1; bit >= 0; bit--)
+      for (int d = dim - 1; d >= 0; d--) lo = (lo << 1) | ((k.x[d] >> bit) & 1u);
+    const int shift = dim * (md - k.lev);
+    const uint64_t hi = lo + (shift >= 64 ? ~0ull : ((1ull << shift) - 1ull));
+    const size_t cb = std::lower_bound(pk.begin() + b, pk.begin() + e, lo) - pk.begin();
+    const size_t ce = std::upper_bound(pk.begin() + cb, pk.begin() + e, hi) - pk.begin();
+    if ((int64_t) (ce - cb) > max_pts && k.lev < md) construct(pk, cb, ce, k, dim, md, max_pts, leaves);
+    else leaves.push_back(k);
+  }
+}
+
+// 2:1 balancing with the semantics of propagateNeighbours + reconstruction
+// (src/tsort.cpp:777-854): S = leaves closed under "parent and the parent's
+// in-domain neighbours"; the balanced tree's leaves are the children of the
+// parents of S-cells that are not themselves parents of S-cells.
+static std::vector<Cell> balance(const std::vector<Cell> &leaves, int dim, int md)
+{
+  std::vector<std::unordered_set<uint64_t>> S(md + 1);
+  for (const Cell &c : leaves) S[c.lev].insert(ckey(c, dim, md));
+  int n3 = 1;
+  for (int d = 0; d < dim; d++) n3 *= 3;
+  const uint64_t top = 1ull << md;
+  for (int l = md; l > 0; l--) {
+    std::vector<uint64_t> cur(S[l].begin(), S[l].end());
+    for (uint64_t k : cur) {
+      const Cell p = cparent(cdecode(k, dim, md), md);
+      const uint64_t len = 1ull << (md - p.lev);
+      for (int idx = 0; idx < n3; idx++) {
+        Cell nb = p;
+        bool ok = true;
+        int r = idx;
+        for (int d = 0; d < dim && ok; d++) {
+          const int delta = r % 3;
+          r /= 3;
+          if (delta == 1) { if (p.x[d] + len >= top) ok = false; else nb.x[d] = (uint32_t) (p.x[d] + len); }
+          else if (delta == 2) { if (p.x[d] < len) ok = false; else nb.x[d] = (uint32_t) (p.x[d] - len); }
+        }
+        if (ok) S[p.lev].insert(ckey(nb, dim, md));
+      }
+    }
+  }
+  std::unordered_set<uint64_t> I;
+  for (int l = 1; l <= md; l++)
+    for (uint64_t k : S[l]) I.insert(ckey(cparent(cdecode(k, dim, md), md), dim, md));
+  std::vector<Cell> out;
+  const int nc = 1 << dim;
+  for (uint64_t k : I) {
+    const Cell c = cdecode(k, dim, md);
+    const uint32_t cl = 1u << (md - c.lev - 1);
+    for (int ch = 0; ch < nc; ch++) {
+      Cell kc = c;
+      kc.lev = c.lev + 1;
+      for (int d = 0; d < dim; d++) kc.x[d] = c.x[d] | (((ch >> d) & 1) ? cl : 0u);
+      if (!I.count(ckey(kc, dim, md))) out.push_back(kc);
+    }
+  }
+  return out;
+}
+
+static uint64_t morton_full(const uint32_t *x, int dim, int md)
+{
+  uint64_t k = 0;
+  for (int bit = md - 1; bit >= 0; bit--)
+    for (int d = dim - 1; d >= 0; d--) k = (k << 1) | ((x[d] >> bit) & 1u);
+  return k;
+}
+
+// Points -> 2:1-balanced complete tree (unsorted cells; the DA sorts them).
+std::vector<Cell> tree_from_points(const uint32_t *pts, int64_t n, int dim, int md, int64_t max_pts)
+{
+  if (dim * md > 64) throw std::invalid_argument("dim*max_depth must be <= 64");
+  std::vector<uint64_t> pk(n);
+  for (int64_t i = 0; i < n; i++) pk[i] = morton_full(pts + i * dim, dim, md);
+  std::sort(pk.begin(), pk.end());
+  Cell root{};
+  root.lev = 0;
+  std::vector<Cell> leaves;
+  if ((int64_t) pk.size() > max_pts) construct(pk, 0, pk.size(), root, dim, md, max_pts, leaves);
+  else {
+    const int nc = 1 << dim;
+    for (int ch = 0; ch < nc; ch++) {
+      Cell k{};
+      k.lev = 1;
+      for (int d = 0; d < dim; d++) k.x[d] = ((ch >> d) & 1) ? (1u << (md - 1)) : 0u;
+      leaves.push_back(k);
+    }
+  }
+  return balance(leaves, dim, md);
+}
+
+// Spacetime moving ball (dim 4: x, y, z, t): refine every cell whose box meets
+// the shell | |(x,y,z) - c(t)| - R | <= w, c(t) = c0 + (c1 - c0) t, down to
+// `level`, then 2:1 balance.  For a cell [lo,hi]^3 x [t0,t1] the distance from
+// c(t) to the spatial box is convex in t (its square is a sum of squared
+// clamped linear functions), so its minimum over [t0,t1] is found by golden
+// section search; the largest distance to the box is convex too, so its
+// maximum sits at t0 or t1.  The cell meets the shell iff
+// min-distance <= R + w and max-distance >= R - w.
+static double box_dist(const double *lo, const double *hi, const double *c)
+{
+  double s = 0.0;
+  for (int d = 0; d < 3; d++) {
+    const double g = c[d] < lo[d] ? lo[d] - c[d] : (c[d] > hi[d] ? c[d] - hi[d] : 0.0);
+    s += g * g;
+  }
+  return std::sqrt(s);
+}
+static double box_far(const double *lo, const double *hi, const double *c)
+{
+  double s = 0.0;
+  for (int d = 0; d < 3; d++) {
+    const double f = std::max(std::fabs(c[d] - lo[d]), std::fabs(hi[d] - c[d]));
+    s += f * f;
+  }
+  return std::sqrt(s);
+}
+
+static void ball_refine(const Cell &c, int md, int level, double R, double w, const double *c0, const double *c1,
+                        std::vector<Cell> &leaves)
+{
+  const double s = std::ldexp(1.0, -md);
+  const double h = std::ldexp(1.0, -c.lev);
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; d++) { lo[d] = c.x[d] * s; hi[d] = lo[d] + h; }
+  const double t0 = c.x[3] * s, t1 = t0 + h;
+  auto centre = [&](double t, double *out) { for (int d = 0; d < 3; d++) out[d] = c0[d] + (c1[d] - c0[d]) * t; };
+  double ca[3], cb[3];
+  centre(t0, ca);
+  centre(t1, cb);
+  const double dmax = std::max(box_far(lo, hi, ca), box_far(lo, hi, cb));
+  double a = t0, b = t1;
+  const double gr = 0.5 * (std::sqrt(5.0) - 1.0);
+  for (int it = 0; it < 80; it++) {
+    const double m1 = b - gr * (b - a), m2 = a + gr * (b - a);
+    double p1[3], p2[3];
+    centre(m1, p1);
+    centre(m2, p2);
+    if (box_dist(lo, hi, p1) <= box_dist(lo, hi, p2)) b = m2; else a = m1;
+  }
+  double pm[3];
+  centre(0.5 * (a + b), pm);
+  const double dmin = std::min({box_dist(lo, hi, pm), box_dist(lo, hi, ca), box_dist(lo, hi, cb)});
+  const bool meets = (dmin <= R + w) && (dmax >= R - w);
+  if (meets && c.lev < level) {
+    for (int ch = 0; ch < 16; ch++) {
+      Cell k = c;
+      k.lev = c.lev + 1;
+      const uint32_t cl = 1u << (md - k.lev);
+      for (int d = 0; d < 4; d++) k.x[d] = c.x[d] | (((ch >> d) & 1) ? cl : 0u);
+      ball_refine(k, md, level, R, w, c0, c1, leaves);
+    }
+  } else {
+    leaves.push_back(c);
+  }
+}
+
+std::vector<Cell> moving_ball_tree(int md, int level, double R, double w, const double *c0, const double *c1)
+{
+  Cell root{};
+  root.lev = 0;
+  std::vector<Cell> leaves;
+  ball_refine(root, md, level, R, w, c0, c1, leaves);
+  return balance(leaves, 4, md);
+}
+
+}  // namespace dkt

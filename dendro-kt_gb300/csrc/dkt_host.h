@@ -1,0 +1,24 @@
+// Host-side declarations shared by the C ABI and dkt_host.cpp.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace dkt {
+
+struct RefEl1D {
+  int p = 1, M = 2;
+  std::vector<double> ip0, ip1, Q, D, W;
+};
+RefEl1D refel_1d(int p);
+void builtin_operator(int kind, int dim, int p, int md, std::vector<double> &A, std::vector<double> &B,
+                      std::vector<double> &alpha, std::vector<double> &beta, bool &uses_scale);
+
+struct Cell {
+  uint32_t x[4];
+  int lev;
+};
+void gaussian_points(int64_t n, int dim, int md, double mean, double sd, uint64_t seed, uint32_t *out);
+std::vector<Cell> tree_from_points(const uint32_t *pts, int64_t n, int dim, int md, int64_t max_pts);
+std::vector<Cell> moving_ball_tree(int md, int level, double R, double w, const double *c0, const double *c1);
+
+}  // namespace dkt

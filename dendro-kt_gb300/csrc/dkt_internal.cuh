@@ -1,0 +1,168 @@
+// Shared definitions of the GB300 implementation of the k-tree matvec path:
+// SFC digit arithmetic, device-resident DA and matvec-plan structures.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "dkt_prims.cuh"
+
+namespace dkt {
+
+constexpr int MAX_DIM = 4;
+constexpr int MAX_NPE = 81;   // (p+1)^dim for p <= 2, dim <= 4
+
+// Curve tables in the reference's layout (src/KDhcurvedata.cpp, hcurvedata.h):
+//   rot[r*2*nc + sfc]      = Morton child visited at SFC position sfc
+//   rot[r*2*nc + nc + m]   = SFC position of Morton child m
+//   ht[r*nc + m]           = orientation of Morton child m
+struct CurveDev {
+  const int8_t *rot = nullptr;
+  const int32_t *ht = nullptr;
+  int nrot = 1;
+};
+
+struct CurveHost {
+  std::vector<int8_t> rot;
+  std::vector<int32_t> ht;
+  int nrot = 1;
+  DBuf<int8_t> drot;
+  DBuf<int32_t> dht;
+  void morton(int dim)
+  {
+    const int nc = 1 << dim;
+    rot.assign(2 * nc, 0);
+    ht.assign(nc, 0);
+    for (int c = 0; c < nc; c++) { rot[c] = (int8_t) c; rot[nc + c] = (int8_t) c; }
+    nrot = 1;
+  }
+  void upload()
+  {
+    drot.upload(rot.data(), rot.size());
+    dht.upload(ht.data(), ht.size());
+  }
+  CurveDev dev() const { return CurveDev{drot.p, dht.p, nrot}; }
+};
+
+// Bits needed to store 0..nc (a child rank plus one sentinel).
+__host__ __device__ inline int slot_bits(int dim) { return dim == 2 ? 3 : dim == 3 ? 4 : 5; }
+
+// getMortonIndex(level) (include/treeNode.tcc:244-258) for coordinates < 2^(md+1).
+__host__ __device__ inline unsigned morton_at(const uint32_t *x, int dim, int md, int lev)
+{
+  unsigned c = 0;
+  const int sh = md - lev;
+  for (int d = 0; d < dim; d++) c |= ((x[d] >> sh) & 1u) << d;
+  return c;
+}
+
+// 128-bit builder: appends fields most-significant first.
+struct KeyBuilder {
+  uint64_t hi = 0, lo = 0;
+  int used = 0;
+  __host__ __device__ void push(uint64_t v, int bits)
+  {
+    if (bits == 0) return;
+    hi = (hi << bits) | (bits < 64 ? (lo >> (64 - bits)) : lo);
+    lo = (bits < 64) ? ((lo << bits) | v) : v;
+    used += bits;
+  }
+  // Left-align to a total width W so keys with different layouts compare on
+  // their first field.
+  __host__ __device__ Key128 finish(int W)
+  {
+    const int s = W - used;
+    if (s > 0) {
+      if (s >= 64) { hi = lo << (s - 64); lo = 0; }
+      else { hi = (hi << s) | (lo >> (64 - s)); lo <<= s; }
+    }
+    return Key128{lo, hi};
+  }
+};
+
+// SFC tree-sort key of a cell (SFC_Tree::locTreeSort, include/tsort.tcc:14-80):
+// for levels 1..md the SFC rank of the child taken at that level plus one, and
+// 0 below the cell's own level, so ancestors precede descendants.
+__host__ __device__ inline uint64_t tree_key(const uint32_t *x, int lev, int dim, int md, CurveDev cv)
+{
+  const int nc = 1 << dim, B = slot_bits(dim);
+  uint64_t k = 0;
+  int r = 0;
+  for (int l = 1; l <= md; l++) {
+    unsigned v = 0;
+    if (l <= lev) {
+      const unsigned m = morton_at(x, dim, md, l);
+      v = (unsigned) cv.rot[r * 2 * nc + nc + m] + 1u;
+      r = cv.ht[r * nc + m];
+    }
+    k = (k << B) | v;
+  }
+  return k;
+}
+
+// Node key used for exact coordinate lookups: coordinates concatenated with
+// md+1 bits per axis (coordinates may equal 2^md on the upper boundary).
+__host__ __device__ inline uint64_t coord_key(const uint32_t *x, int dim, int md)
+{
+  uint64_t k = 0;
+  for (int d = dim - 1; d >= 0; d--) k = (k << (md + 1)) | x[d];
+  return k;
+}
+
+// Cell key for set membership: level in the top bits, anchor below.
+__host__ __device__ inline uint64_t cell_key(const uint32_t *a, int lev, int dim, int md)
+{
+  uint64_t k = (uint64_t) lev;
+  for (int d = dim - 1; d >= 0; d--) k = (k << md) | a[d];
+  return k;
+}
+
+// Device-resident distributed array (ot::DA on one rank).
+struct DA {
+  int dim = 3, order = 1, md = 10, curve = 0;
+  int64_t n_elem = 0, n_nodes = 0, n_bdry = 0;
+  CurveHost cv;
+  DBuf<uint32_t> elem_x;     // [n_elem][dim], SFC order
+  DBuf<uint8_t> elem_lev;
+  DBuf<uint32_t> node_x;     // [n_nodes][dim], DA order
+  DBuf<uint8_t> node_lev;
+  DBuf<uint32_t> bdry;       // boundary node ids, ascending
+};
+
+// Elemental operator K_L = alpha[L] * A + beta[L] * B (dense nPe x nPe, the
+// reference's lexicographic node order, x fastest), or one dense table per
+// level when kind == custom.
+enum OpKind { OP_IDENTITY = 0, OP_HEAT = 1, OP_LAPMASS = 2, OP_CUSTOM = 3 };
+
+struct Operator {
+  int kind = OP_LAPMASS;
+  int npe = 8, nlev = 11;
+  bool uses_scale = true;            // HeatMat ignores the scale argument
+  std::vector<double> A, B;          // npe*npe each (row r = output, col c = input)
+  std::vector<double> alpha, beta;   // per level
+  std::vector<double> table;         // custom: nlev*npe*npe
+};
+
+// Flattened traversal: one record per leaf visit of fem::matvec.
+struct Plan {
+  int dim = 3, order = 1, md = 10, npe = 8;
+  int64_t n_nodes = 0, n_leaf = 0, n_hang = 0, n_bdry = 0;
+  int64_t stale_slots = 0;           // parent slots read unfilled with nonzero weight
+  DBuf<int32_t> e2n;                 // [npe][n_leaf]  node index or -1
+  DBuf<uint32_t> info;               // [n_leaf] level | child<<8 | hanging<<16
+  DBuf<int32_t> hidx;                // [n_leaf] index into hanging arrays or -1
+  DBuf<int32_t> p2n;                 // [npe][n_hang] parent node index (level L-1) or -1
+  DBuf<uint32_t> fill;               // [3][n_hang] filled-rank bitmask of the leaf
+  DBuf<uint32_t> bdry;               // boundary node ids
+  DBuf<double> opA, opB, opAlpha, opBeta, opTable;
+  DBuf<double> ip;                   // [2][M][M] child interpolation (ip_1D_0, ip_1D_1)
+  Operator op;
+  DBuf<double> xin;                  // scratch: boundary-zeroed input
+  DBuf<double> xh, yh;               // device copies for the host-array entry point
+  // Optional CUDA-event timing of the leaf kernel on its launching stream.
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;       // start/stop pairs of the current window
+  int64_t timed_launches = 0;
+};
+
+}  // namespace dkt

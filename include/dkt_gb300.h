@@ -1,0 +1,146 @@
+/*
+ * dkt_gb300.h -- C ABI of the GB300 (sm_103a) implementation of Dendro-KT's
+ * adaptive k-tree finite-element matvec, dim 2-4, element order 1-2.
+ *
+ * Plain pointers and sizes only.  Every function returns DKT_OK (0) on
+ * success or a negative DKT_E* code; dkt_last_error() describes the last
+ * failure of the calling thread.  No exception crosses the ABI.
+ *
+ * Coordinates follow the reference's integer convention: an orthant or node
+ * is a dim-vector of uint32 in [0, 2^max_depth] plus a level (the reference's
+ * TreeNode<unsigned,dim>, include/treeNode.h:36-253; m_uiMaxDepth is
+ * max_depth).  Arrays of coordinates are row-major [n][dim].
+ *
+ * Device pointers ("_dev") are CUDA global-memory addresses on the current
+ * device; "stream" is a cudaStream_t passed as void* (NULL = legacy stream).
+ */
+#ifndef DKT_GB300_H
+#define DKT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DKT_OK 0
+#define DKT_E_ARG (-1)      /* invalid argument */
+#define DKT_E_CUDA (-2)     /* CUDA runtime error */
+#define DKT_E_NOMEM (-3)    /* device allocation failed */
+#define DKT_E_UNSUP (-4)    /* configuration not supported */
+#define DKT_E_NOCONV (-5)   /* iterative solve did not converge */
+#define DKT_E_INTERNAL (-6)
+
+#define DKT_CURVE_MORTON 0
+#define DKT_CURVE_HILBERT 1
+
+/* Elemental operators.  IDENTITY is the test operator of
+ * test/testMatvec.cpp:187-198; HEAT is HeatEq::HeatMat<3>::elementalMatVec
+ * (FEM/examples/src/heatMat.cpp:45-117, scale ignored, Dirichlet zeroing in
+ * pre/postMatVec :119-139); LAPMASS is the Laplacian + mass operator
+ * K_e = J^(d-2) K_ref + J^d M_ref (J = h/2) with the same boundary zeroing;
+ * CUSTOM takes one dense nPe x nPe table per level, tabulated by the caller
+ * from its own feMatrix::elementalMatVec (an arbitrary host callback cannot
+ * run on the device). */
+#define DKT_OP_IDENTITY 0
+#define DKT_OP_HEAT 1
+#define DKT_OP_LAPMASS 2
+#define DKT_OP_CUSTOM 3
+
+typedef struct dkt_da_s *dkt_da;
+typedef struct dkt_plan_s *dkt_plan;
+
+/* ---- ot::DA<dim> --------------------------------------------------------
+ * dkt_da_create replaces ot::DA<dim>::DA(inTree, nEle, comm, order)
+ * (include/oda.h:150-167, src/oda.cpp:45-151) on one rank.  The tree must be
+ * complete and 2:1 balanced; unless tree_is_sorted, it is first put into SFC
+ * order exactly as SFC_Tree::locTreeSort does (include/tsort.tcc:14-80).  The
+ * node list, its order, the node levels and the boundary ids equal the
+ * reference's bit for bit (SFC_NodeSort::dist_countCGNodes,
+ * include/nsort.tcc:492-533).  Runs on the device. */
+int dkt_da_create(int dim, int order, int curve, int max_depth, const uint32_t *tree_coords,
+                  const uint8_t *tree_levels, int64_t n_elem, int tree_is_sorted, dkt_da *out);
+/* ot::DA::getLocalNodalSz (include/oda.h:180); equals getTotalNodalSz on one rank. */
+int64_t dkt_da_local_nodal_size(dkt_da da);
+int64_t dkt_da_num_elements(dkt_da da);
+/* Number of domain-boundary nodes (size of getBoundaryNodeIndices, oda.h:264). */
+int64_t dkt_da_boundary_size(dkt_da da);
+/* Host copies of getTNCoords (oda.h:252): coords [n][dim], levels [n]. */
+int dkt_da_get_nodes(dkt_da da, uint32_t *coords, uint8_t *levels);
+/* Host copy of getBoundaryNodeIndices (oda.h:264). */
+int dkt_da_get_boundary_ids(dkt_da da, uint32_t *ids);
+/* Host copy of the SFC-ordered tree the DA was built on. */
+int dkt_da_get_tree(dkt_da da, uint32_t *coords, uint8_t *levels);
+void dkt_da_destroy(dkt_da da);
+
+/* ---- fem::matvec -----------------------------------------------------------
+ * A plan is the flattened form of the recursive traversal
+ * fem::matvec(vecIn, vecOut, coords, sz, partFront, partBack, eleOp, scale,
+ * refElement) (FEM/include/matvec.h:37-38, 231-548): built once per node list,
+ * reused for every product.  op_tables is NULL except for DKT_OP_CUSTOM, where
+ * it holds (max_depth+1) tables of nPe*nPe doubles (row = output rank,
+ * column = input rank; rank = lexicographic element node index, x fastest).
+ */
+int dkt_plan_create(dkt_da da, int op, const double *op_tables, dkt_plan *out);
+/* Same, from a bare node list (the `coords, sz` arguments of fem::matvec). */
+int dkt_plan_create_from_nodes(int dim, int order, int curve, int max_depth, const uint32_t *node_coords,
+                               const uint8_t *node_levels, int64_t sz, int op, const double *op_tables,
+                               dkt_plan *out);
+int64_t dkt_plan_num_nodes(dkt_plan plan);
+/* Counters of the flattened traversal: [0] leaf visits, [1] hanging leaves,
+ * [2] parent-buffer slots that the reference would read without refilling
+ * (nonzero means its result depends on earlier leaves; the device path uses
+ * zero there), [3] boundary nodes. */
+int dkt_plan_stats(dkt_plan plan, int64_t *out4);
+
+/* Host copy of the flattened traversal (for inspection and tests):
+ * e2n [nPe][leaves] node of each lexicographic rank or -1; info [leaves]
+ * level | child<<8 | hanging<<16; hidx [leaves] hanging record or -1;
+ * p2n [nPe][hanging] parent node of level L-1 per rank or -1; fill
+ * [3][hanging] filled-rank bit masks.  Any pointer may be NULL. */
+int dkt_plan_export(dkt_plan plan, int32_t *e2n, uint32_t *info, int32_t *hidx, int32_t *p2n, uint32_t *fill);
+
+/* fem::matvec on device arrays: y = sum over leaves of the elemental products
+ * (no boundary handling).  y is overwritten (matvec.h:235). */
+int dkt_matvec(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream);
+
+/* feMatrix<LeafT,dim>::matVec(in, out, scale) (FEM/include/feMatrix.h:189-259)
+ * on device arrays: pre-matvec boundary zeroing of the input copy, fem::matvec,
+ * post-matvec boundary zeroing of the output (for HEAT and LAPMASS, the
+ * reference's HeatMat::preMatVec/postMatVec; IDENTITY and CUSTOM have no
+ * pre/post step).  x_dev is not modified. */
+int dkt_fematrix_matvec(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream);
+
+/* Same with host arrays: copies in, computes, copies out, synchronises. */
+int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host, double scale);
+
+/* Diagonal of the operator (for Jacobi preconditioning), on device. */
+int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream);
+
+/* CG on feMatrix::matVec in the form of HeatMat::cgSolve
+ * (FEM/examples/src/heatMat.cpp:164-325), optionally Jacobi-preconditioned,
+ * stopping when ||r||_2 <= tol * ||b||_2.  x_dev holds the initial guess and
+ * receives the solution.  iters/relres may be NULL. */
+int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int jacobi,
+                 int *iters, double *relres, void *stream);
+
+/* Measurement hook: with enable = 1 the leaf kernel of every later product
+ * is bracketed by CUDA events on its launching stream.  Each call first
+ * closes the current window, returning the summed kernel time (ms) and the
+ * number of timed launches since the previous call (synchronising on the
+ * last event), then sets the new state. */
+int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t *launches);
+
+void dkt_plan_destroy(dkt_plan plan);
+
+/* Throughput probes of the current device (no counterpart in the reference):
+ * out4 = {FP64 FMA TFLOP/s, FP64 add Tops/s, FP32 FMA TFLOP/s, int64 add Tops/s}. */
+int dkt_probe_device(double *out4);
+
+const char *dkt_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DKT_GB300_H */

@@ -1,0 +1,41 @@
+/*
+ * dkt_gb300_mesh.h -- C ABI of the host-side mesh generators that produce
+ * the input trees of the matvec path (the reference's ot::getPts,
+ * include/octUtils.h:29-65, and SFC_Tree::locTreeBalancing /
+ * distTreeBalancing on one rank, src/tsort.cpp:826-878).  Return codes as in
+ * dkt_gb300.h.  Arrays returned through pointer-to-pointer arguments are
+ * allocated with malloc and released with dkt_free.
+ */
+#ifndef DKT_GB300_MESH_H
+#define DKT_GB300_MESH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* n points, each coordinate N(mean, sd) on the unit cube (clipped), drawn from
+ * a counter-based stream of the given seed, quantised to level max_depth;
+ * out is [n][dim]. */
+int dkt_mesh_gaussian_points(int64_t n, int dim, int max_depth, double mean, double sd, uint64_t seed,
+                             uint32_t *out);
+
+/* Complete tree with at most max_pts points per leaf, then 2:1 balanced over
+ * all 3^dim - 1 neighbours; cells are returned unsorted (dkt_da_create sorts). */
+int dkt_mesh_tree_from_points(const uint32_t *pts, int64_t n, int dim, int max_depth, int64_t max_pts,
+                              int64_t *n_out, uint32_t **coords, uint8_t **levels);
+
+/* dim 4 (x,y,z,t): every cell whose box meets the shell
+ * | |(x,y,z) - c(t)| - radius | <= halfwidth, c(t) = c0 + (c1 - c0) t, is refined
+ * down to `level`; the result is 2:1 balanced. */
+int dkt_mesh_moving_ball(int max_depth, int level, double radius, double halfwidth, const double *c0,
+                         const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels);
+
+void dkt_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

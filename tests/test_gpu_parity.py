@@ -1,0 +1,190 @@
+"""Parity of the GB300 path with the reference, through the C ABI.
+
+Integer outputs (tree order, DA node list, node levels, boundary ids) must be
+bit-exact; matvec values within 1e-12 relative in the 2-norm against the
+reference's own outputs (golden fixtures) and against the CPU oracle on
+larger meshes."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+import oracle_port as orc
+import trees
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+GOLDEN = sorted(g for g in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "morton_*.npz")))
+
+
+@pytest.fixture(scope="module")
+def dkt():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return ge.load_package()
+
+
+def _rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def _gpu_mv(A, x, raw=False):
+    import torch
+    xd = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).cuda()
+    yd = torch.empty_like(xd)
+    (A.matvec_raw if raw else A.matvec)(xd, yd)
+    torch.cuda.synchronize()
+    return yd.cpu().numpy()
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_da_and_matvec(dkt, path):
+    g = np.load(path)
+    dim, md, order, op = int(g["dim"]), int(g["md"]), int(g["order"]), int(g["op"])
+    # shuffle the tree so the device sort is exercised
+    perm = np.random.default_rng(0).permutation(g["tree_levels"].size)
+    da = dkt.DA(g["tree_coords"][perm], g["tree_levels"][perm], dim, order=order, max_depth=md)
+    tc, tl = da.tree()
+    assert np.array_equal(tc, g["tree_coords"]) and np.array_equal(tl, g["tree_levels"])
+    nc, nl = da.nodes()
+    assert np.array_equal(nc, g["node_coords"]) and np.array_equal(nl, g["node_levels"])
+    assert np.array_equal(da.boundary_ids(), g["bdry"])
+    A = dkt.Matrix(da, op=op)
+    assert A.stats()["stale_slots"] == 0
+    assert _rel(_gpu_mv(A, g["x"]), g["y"]) <= TOL
+    assert _rel(_gpu_mv(A, g["x"], raw=True), g["y_raw"]) <= TOL
+
+
+def test_plan_from_nodes_matches_plan_from_da(dkt):
+    g = np.load(GOLDEN[0])
+    dim, md, order, op = int(g["dim"]), int(g["md"]), int(g["order"]), int(g["op"])
+    da = dkt.DA(g["tree_coords"], g["tree_levels"], dim, order=order, max_depth=md, sorted_tree=True)
+    A = dkt.Matrix(da, op=op)
+    B = dkt.Matrix(nodes=(g["node_coords"], g["node_levels"]), dim=dim, order=order, max_depth=md, op=op)
+    assert A.stats() == B.stats()
+    assert _rel(_gpu_mv(B, g["x"]), _gpu_mv(A, g["x"])) <= 1e-15
+
+
+@pytest.mark.parametrize("dim,n,md,order,op", [
+    (3, 32768, 10, 1, 1),     # adaptive 3D Q1 HeatMat on a 32768-point Gaussian cloud
+    (3, 4000, 10, 2, 2),      # 3D Q2 Laplacian+mass
+    (2, 3000, 12, 1, 2),
+    (2, 2000, 12, 2, 2),
+])
+def test_gaussian_meshes_vs_oracle(dkt, dim, n, md, order, op):
+    gmd = md - 1 if order == 2 else md
+    pts = dkt.gaussian_points(n, dim, gmd, seed=0)
+    tc, tl = dkt.tree_from_points(pts, dim, gmd)
+    if order == 2:
+        tc = tc << np.uint32(1)   # same mesh, one level finer in coordinates
+    da = dkt.DA(tc, tl, dim, order=order, max_depth=md)
+    orc.set_curve(dim, md)
+    sc, sl = da.tree()
+    ora = orc.DA(sc, sl, dim, order, op)
+    nc, nl = da.nodes()
+    assert np.array_equal(nc, ora.node_coords) and np.array_equal(nl, ora.node_levels)
+    assert np.array_equal(da.boundary_ids(), ora.bdry)
+    A = dkt.Matrix(da, op=op)
+    x = dkt.uniform_pm1(1, da.n)
+    y = _gpu_mv(A, x)
+    yr = ora.matvec(x)
+    assert _rel(y, yr) <= TOL
+    st, ost = A.stats(), ora.stats()
+    assert st["leaves"] == ost["leaves"] and st["hanging_leaves"] == ost["hanging_leaves"]
+    assert st["stale_slots"] == 0 and ost["stale_reads"] == 0
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_moving_ball_4d_vs_oracle(dkt, order):
+    md, level = 7, 4
+    tc, tl = dkt.moving_ball_tree(max_depth=md, level=level)
+    da = dkt.DA(tc, tl, 4, order=order, max_depth=md)
+    orc.set_curve(4, md)
+    sc, sl = da.tree()
+    ora = orc.DA(sc, sl, 4, order, 2)
+    nc, nl = da.nodes()
+    assert np.array_equal(nc, ora.node_coords) and np.array_equal(nl, ora.node_levels)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    x = dkt.uniform_pm1(2, da.n)
+    assert _rel(_gpu_mv(A, x), ora.matvec(x)) <= TOL
+    assert A.stats()["leaves"] == ora.stats()["leaves"]
+
+
+@pytest.mark.parametrize("dim,L", [(2, 4), (3, 3), (4, 2)])
+def test_identity_uniform_known_answer(dkt, dim, L):
+    """all-ones input, identity eleOp, uniform grid: 2^k at each node
+    (test/testMatvec.cpp:254-264)."""
+    md = 6
+    c, lv = trees.example2(dim, L, md)
+    da = dkt.DA(c, lv, dim, order=1, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_IDENTITY)
+    y = _gpu_mv(A, np.ones(da.n))
+    nc, _ = da.nodes()
+    k = np.sum((nc != 0) & (nc != (1 << md)), axis=1)
+    assert np.array_equal(y, 2.0 ** k)
+
+
+def test_host_entry_point_matches_device(dkt):
+    g = np.load(GOLDEN[-1])
+    dim, md, order, op = int(g["dim"]), int(g["md"]), int(g["order"]), int(g["op"])
+    da = dkt.DA(g["tree_coords"], g["tree_levels"], dim, order=order, max_depth=md)
+    A = dkt.Matrix(da, op=op)
+    # same arithmetic; atomics may add in a different order
+    assert _rel(A.matvec_host(g["x"]), _gpu_mv(A, g["x"])) <= 1e-15
+
+
+def test_custom_tables_reproduce_builtin(dkt):
+    """A per-level table operator (the drop-in for an arbitrary feMatrix
+    subclass, tabulated from its elementalMatVec) reproduces the built-in one."""
+    dim, md, order = 3, 8, 1
+    pts = dkt.gaussian_points(500, dim, md, seed=5)
+    tc, tl = dkt.tree_from_points(pts, dim, md)
+    da = dkt.DA(tc, tl, dim, order=order, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    # tabulate the built-in operator column by column through a one-element mesh
+    npe = 8
+    tables = np.zeros((md + 1, npe, npe))
+    for lev in range(md + 1):
+        J = 0.5 * 2.0 ** -lev
+        K, M = _lapmass_ref(dim, order)
+        tables[lev] = J ** (dim - 2) * K + J ** dim * M
+    B = dkt.Matrix(da, op=dkt.OP_CUSTOM, tables=tables)
+    x = dkt.uniform_pm1(4, da.n)
+    assert _rel(_gpu_mv(B, x, raw=True), _gpu_mv(A, x, raw=True)) <= 1e-13
+
+
+def _lapmass_ref(dim, order):
+    """Q1 1D stiffness/mass on [-1,1] and their tensor products (numpy)."""
+    assert order == 1
+    k1 = 0.5 * np.array([[1.0, -1.0], [-1.0, 1.0]])
+    m1 = np.array([[2.0, 1.0], [1.0, 2.0]]) / 3.0
+    K = np.zeros((2 ** dim, 2 ** dim))
+    for a in range(dim):
+        T = np.ones((1, 1))
+        for d in range(dim):
+            T = np.kron(k1 if d == a else m1, T)
+        K += T
+    M = np.ones((1, 1))
+    for d in range(dim):
+        M = np.kron(m1, M)
+    return K, M
+
+
+def test_cg_solves_lapmass(dkt):
+    import torch
+    dim, md = 3, 9
+    pts = dkt.gaussian_points(3000, dim, md, seed=1)
+    tc, tl = dkt.tree_from_points(pts, dim, md)
+    da = dkt.DA(tc, tl, dim, order=1, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    b = dkt.uniform_pm1(3, da.n)
+    b[da.boundary_ids()] = 0.0
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros_like(bd)
+    it, rr = A.cg(bd, xd, max_iter=5000, tol=1e-10, jacobi=True)
+    r = b - _gpu_mv(A, xd.cpu().numpy())
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-10, (it, rr)
