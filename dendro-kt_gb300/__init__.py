@@ -17,6 +17,7 @@ _lib = None
 OK, E_ARG, E_CUDA, E_NOMEM, E_UNSUP, E_NOCONV, E_INTERNAL = 0, -1, -2, -3, -4, -5, -6
 CURVE_MORTON, CURVE_HILBERT = 0, 1
 OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM = 0, 1, 2, 3
+ARITH_AUTO, ARITH_FP64, ARITH_FIXED = 0, 1, 2
 
 
 class DktError(RuntimeError):
@@ -66,6 +67,7 @@ def load(build_if_missing=True):
         "dkt_diagonal": ([P, P, P], I),
         "dkt_cg_solve": ([P, P, P, I, ctypes.c_double, I, P, P, P], I),
         "dkt_plan_kernel_timing": ([P, I, P, P], I),
+        "dkt_plan_set_arithmetic": ([P, I], I),
         "dkt_plan_destroy": ([P], None),
         "dkt_mesh_gaussian_points": ([I64, I, I, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, P], I),
         "dkt_mesh_tree_from_points": ([P, I64, I, I, I64, P, P, P], I),
@@ -201,6 +203,10 @@ class Matrix:
         y = np.empty(self.n)
         _check(load().dkt_fematrix_matvec_host(self._h, _p(x), _p(y), scale))
         return y
+
+    def set_arithmetic(self, mode):
+        """ARITH_AUTO (fixed point where it applies), ARITH_FP64 or ARITH_FIXED."""
+        _check(load().dkt_plan_set_arithmetic(self._h, mode))
 
     def kernel_timing(self, enable):
         """Close the current timing window; returns (total kernel ms, launches)."""

@@ -21,6 +21,7 @@ void build_plan(Plan &pl, const uint32_t *node_x, const uint8_t *node_lev, int64
 void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void diagonal(const Plan &pl, double *diag, cudaStream_t s);
+bool q1fx_setup(Plan &pl, cudaStream_t s);
 int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,
              cudaStream_t s);
 
@@ -192,6 +193,7 @@ static int plan_common(int dim, int order, int curve, int md, const uint32_t *no
     const std::vector<double> ip = interp_tables(order);
     dkt::build_plan(pl, node_x_dev, node_lev_dev, n, cv, ip.data(), s);
     setup_operator(pl, op, tables, s);
+    dkt::q1fx_setup(pl, s);
     if (bdry_dev) {
       pl.bdry.alloc(nb > 0 ? nb : 1);
       if (nb > 0) DKT_CUDA(cudaMemcpyAsync(pl.bdry.p, bdry_dev, nb * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
@@ -315,6 +317,14 @@ int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter
   return guarded([&]() {
     return dkt::cg_solve(plan->pl, b_dev, x_dev, max_iter, tol, jacobi != 0, iters, relres, (cudaStream_t) stream);
   });
+}
+
+int dkt_plan_set_arithmetic(dkt_plan plan, int mode)
+{
+  if (!plan || mode < 0 || mode > 2) return fail(DKT_E_ARG, "bad argument");
+  if (mode == 2 && !plan->pl.fx_ready) return fail(DKT_E_UNSUP, "fixed-point arithmetic needs a Q1 built-in operator");
+  plan->pl.arith = mode;
+  return DKT_OK;
 }
 
 int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t *launches)

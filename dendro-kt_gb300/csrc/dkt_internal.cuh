@@ -159,6 +159,13 @@ struct Plan {
   Operator op;
   DBuf<double> xin;                  // scratch: boundary-zeroed input
   DBuf<double> xh, yh;               // device copies for the host-array entry point
+  // Exact fixed-point path of the Q1 built-in operators (dkt_q1fx.cu).
+  int arith = 0;                     // 0 auto, 1 native FP64, 2 fixed point
+  bool fx_ready = false;
+  int fx_c = 0;
+  DBuf<long long> fx_fm, xq, yq;
+  DBuf<int> fx_fe, fx_sx;
+  DBuf<unsigned long long> fx_amax;
   // Optional CUDA-event timing of the leaf kernel on its launching stream.
   bool timing = false;
   std::vector<cudaEvent_t> ev;       // start/stop pairs of the current window

@@ -24,7 +24,7 @@ struct Pow<0, M> {
 // forward:   y_j = sum_k ip[k*M + j] x_k   (parent -> child)
 // transpose: y_j = sum_k ip[j*M + k] x_k   (child -> parent)
 template <int DIM, int M, bool TRANSPOSE>
-__device__ __forceinline__ void interp(double *v, const double *__restrict__ ip, unsigned child)
+__host__ __device__ __forceinline__ void interp(double *v, const double *__restrict__ ip, unsigned child)
 {
   constexpr int NPE = Pow<DIM, M>::v;
   constexpr int UR = NPE <= 16 ? NPE : 1;
@@ -49,27 +49,28 @@ __device__ __forceinline__ void interp(double *v, const double *__restrict__ ip,
   }
 }
 
+__host__ __device__ __forceinline__ void accum(double *p, double v)
+{
+#ifdef __CUDA_ARCH__
+  atomicAdd(p, v);
+#else
+  *p += v;
+#endif
+}
+
+// One leaf visit: gather, parent interpolation, elemental operator, scatter
+// and the hanging transpose.  sA/sB/sip point at the staged operator and
+// interpolation tables.
 template <int DIM, int P, bool CUSTOM>
-__global__ void __launch_bounds__(128) k_matvec_leaf(
-    const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+__host__ __device__ __forceinline__ void leaf_body(
+    int64_t i, const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
-    const double *__restrict__ gA, const double *__restrict__ gB, const double *__restrict__ alpha,
-    const double *__restrict__ beta, const double *__restrict__ table, const double *__restrict__ gip,
-    const double *__restrict__ x, double *__restrict__ y, double scale)
+    const double *sA, const double *sB, const double *__restrict__ alpha, const double *__restrict__ beta,
+    const double *__restrict__ table, const double *sip, const double *__restrict__ x, double *__restrict__ y,
+    double scale)
 {
   constexpr int M = P + 1, NPE = Pow<DIM, M>::v;
   constexpr int UR = NPE <= 16 ? NPE : 1;
-  extern __shared__ double sm[];
-  // custom operators keep no A/B in shared memory: the interpolation tables
-  // then start at the beginning of the dynamic allocation
-  double *sA = sm, *sB = sm + NPE * NPE, *sip = CUSTOM ? sm : sm + 2 * NPE * NPE;
-  if (!CUSTOM) {
-    for (int t = threadIdx.x; t < NPE * NPE; t += blockDim.x) { sA[t] = gA[t]; sB[t] = gB[t]; }
-  }
-  for (int t = threadIdx.x; t < 2 * M * M; t += blockDim.x) sip[t] = gip[t];
-  __syncthreads();
-  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_leaf) return;
   const uint32_t inf = info[i];
   const int L = inf & 0xFFu;
   const unsigned child = (inf >> 8) & 0xFFu;
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(128) k_matvec_leaf(
   }
 #pragma unroll UR
   for (int r = 0; r < NPE; r++)
-    if (nd[r] >= 0) atomicAdd(&y[nd[r]], out[r]);
+    if (nd[r] >= 0) accum(&y[nd[r]], out[r]);
   if (hang) {
 #pragma unroll UR
     for (int r = 0; r < NPE; r++)
@@ -128,9 +129,34 @@ __global__ void __launch_bounds__(128) k_matvec_leaf(
 #pragma unroll UR
     for (int q = 0; q < NPE; q++) {
       const int32_t pn = p2n[(int64_t) q * n_hang + h];
-      if (pn >= 0 && !((fm[q >> 5] >> (q & 31)) & 1u)) atomicAdd(&y[pn], out[q]);
+      if (pn >= 0 && !((fm[q >> 5] >> (q & 31)) & 1u)) accum(&y[pn], out[q]);
     }
   }
+}
+
+template <int DIM, int P, bool CUSTOM>
+__global__ void __launch_bounds__(128) k_matvec_leaf(
+    const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+    const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
+    const double *__restrict__ gA, const double *__restrict__ gB, const double *__restrict__ alpha,
+    const double *__restrict__ beta, const double *__restrict__ table, const double *__restrict__ gip,
+    const double *__restrict__ x, double *__restrict__ y, double scale)
+{
+  constexpr int M = P + 1, NPE = Pow<DIM, M>::v;
+  constexpr int UR = NPE <= 16 ? NPE : 1;
+  extern __shared__ double sm[];
+  // custom operators keep no A/B in shared memory: the interpolation tables
+  // then start at the beginning of the dynamic allocation
+  double *sA = sm, *sB = sm + NPE * NPE, *sip = CUSTOM ? sm : sm + 2 * NPE * NPE;
+  if (!CUSTOM) {
+    for (int t = threadIdx.x; t < NPE * NPE; t += blockDim.x) { sA[t] = gA[t]; sB[t] = gB[t]; }
+  }
+  for (int t = threadIdx.x; t < 2 * M * M; t += blockDim.x) sip[t] = gip[t];
+  __syncthreads();
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_leaf) return;
+  leaf_body<DIM, P, CUSTOM>(i, e2n, info, hidx, p2n, fill, n_leaf, n_hang, sA, sB, alpha, beta, table, sip, x, y,
+                            scale);
 }
 
 __global__ void k_zero_at(double *__restrict__ v, const uint32_t *__restrict__ ids, int64_t nb)
@@ -173,9 +199,12 @@ static void launch_leaf(Plan &pl, const double *x, double *y, double scale, cuda
   }
 }
 
+void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cudaStream_t s);
+
 // fem::matvec: y = 0, then the leaf kernel.
 void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
 {
+  if (pl.fx_ready && pl.arith != 1) { q1fx_matvec(pl, x, y, scale, false, s); return; }
   DKT_CUDA(cudaMemsetAsync(y, 0, pl.n_nodes * sizeof(double), s));
   if (pl.n_leaf == 0) return;
   switch (pl.dim * 10 + pl.order) {
@@ -194,6 +223,7 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
 {
   const bool bc = (pl.op.kind == OP_HEAT || pl.op.kind == OP_LAPMASS);
+  if (pl.fx_ready && pl.arith != 1) { q1fx_matvec(pl, x, y, scale, bc, s); return; }
   if (!bc) { matvec(pl, x, y, scale, s); return; }
   if (pl.xin.n < (size_t) pl.n_nodes) pl.xin.alloc(pl.n_nodes);
   DKT_CUDA(cudaMemcpyAsync(pl.xin.p, x, pl.n_nodes * sizeof(double), cudaMemcpyDeviceToDevice, s));

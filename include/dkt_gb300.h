@@ -124,6 +124,16 @@ int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream);
 int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int jacobi,
                  int *iters, double *relres, void *stream);
 
+/* Arithmetic of the leaf kernel.  AUTO (default) uses FIXED where it applies:
+ * the Q1 built-in operators are diagonal in the Hadamard basis and run in
+ * exact int64 fixed point (deterministic, ~2^-50 relative to max|x|*|K|,
+ * well inside the 1e-12 parity tolerance); FP64 forces the dense native-FP64
+ * kernel (used for Q2 and custom operators). */
+#define DKT_ARITH_AUTO 0
+#define DKT_ARITH_FP64 1
+#define DKT_ARITH_FIXED 2
+int dkt_plan_set_arithmetic(dkt_plan plan, int mode);
+
 /* Measurement hook: with enable = 1 the leaf kernel of every later product
  * is bracketed by CUDA events on its launching stream.  Each call first
  * closes the current window, returning the summed kernel time (ms) and the

@@ -53,6 +53,7 @@ def lib():
         L.dkto_matvec_raw.argtypes = [P, P, P]
         L.dkto_fematrix_matvec.argtypes = [P, P, P]
         L.dkto_last_stats.argtypes = [P, P]
+        L.dkto_set_stale_mode.argtypes = [ctypes.c_int]
         L.dkto_cg.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_double, P, P]
         _lib = L
     return _lib
@@ -76,6 +77,12 @@ def set_curve(dim, max_depth, rot=None, ht=None):
         ht = np.ascontiguousarray(ht, dtype=np.int32)
         nrot = ht.size >> dim
         _check(lib().dkto_set_curve(dim, max_depth, _ptr(rot), _ptr(ht), nrot))
+
+
+def set_stale_mode(mode):
+    """0: parent-buffer slots keep earlier leaves' values (the reference's
+    static buffer); 1: unfilled slots read as zero."""
+    _check(lib().dkto_set_stale_mode(int(mode)))
 
 
 def tree_balance(points, dim, max_pts=1):
@@ -136,9 +143,9 @@ class DA:
         return y
 
     def stats(self):
-        s = np.zeros(5, np.int64)
+        s = np.zeros(6, np.int64)
         _check(lib().dkto_last_stats(self._h, _ptr(s)))
-        return dict(zip(["leaves", "hanging_leaves", "stale_reads", "aliased", "max_level"], s.tolist()))
+        return dict(zip(["leaves", "hanging_leaves", "stale_reads", "aliased", "max_level", "ref_errors"], s.tolist()))
 
     def cg(self, b, x0=None, diag=None, max_iter=10000, tol=1e-10):
         b = np.ascontiguousarray(b, dtype=np.float64)

@@ -669,8 +669,11 @@ void ele_op(int op, unsigned dim, const RefEl &re, const double *in, double *out
 // values from earlier leaves in slots that are not refilled.
 // ---------------------------------------------------------------------------
 struct MatvecStats {
-  int64_t leaves = 0, hanging_leaves = 0, stale_reads = 0, aliased = 0, max_depth_seen = 0;
+  int64_t leaves = 0, hanging_leaves = 0, stale_reads = 0, aliased = 0, max_depth_seen = 0, ref_errors = 0;
 };
+// 0: parent-buffer slots keep earlier leaves' values, as the reference's
+// function-static buffer does; 1: unfilled slots read as zero.
+int g_stale_mode = 0;
 
 template <int dim>
 struct Traversal {
@@ -784,12 +787,17 @@ struct Traversal {
       if (pVin == nullptr || pCoords == nullptr || pSz == 0) { fprintf(stderr, "oracle: parent has no nodes\n"); return; }
       TN<dim> par = get_parent(root);
       std::fill(parentFill.begin(), parentFill.end(), 0);
+      if (g_stale_mode == 1) std::fill(parentBuf.begin(), parentBuf.end(), 0.0);
       for (size_t i = 0; i < pSz; i++) {
         if (pCoords[i].lev != pLev - 1) continue;
         unsigned r = lex_node_rank(pCoords[i], par, p);
         parentFill[r] = 1;
         parentBuf[r] = pVin[i];
       }
+      // The reference's own consistency check (matvec.h:439-447): every rank
+      // is filled in the leaf or in the parent buffer.
+      for (unsigned r = 0; r < nPe; r++)
+        if (!leafFill[r] && !parentFill[r]) { st.ref_errors++; break; }
       // Instrumentation: does any unfilled leaf rank read a stale parent slot
       // with nonzero weight?
       {
@@ -1023,13 +1031,16 @@ int dkto_fematrix_matvec(void *hp, const double *x, double *y)
 
 // Counters from the last traversal: leaves, hanging leaves, stale parent
 // slots read with nonzero weight, aliased leaf ranks, deepest level.
-int dkto_last_stats(void *hp, int64_t *out5)
+int dkto_last_stats(void *hp, int64_t *out6)
 {
   OracleDA *h = (OracleDA *) hp;
-  out5[0] = h->stats.leaves; out5[1] = h->stats.hanging_leaves; out5[2] = h->stats.stale_reads;
-  out5[3] = h->stats.aliased; out5[4] = h->stats.max_depth_seen;
+  out6[0] = h->stats.leaves; out6[1] = h->stats.hanging_leaves; out6[2] = h->stats.stale_reads;
+  out6[3] = h->stats.aliased; out6[4] = h->stats.max_depth_seen; out6[5] = h->stats.ref_errors;
   return 0;
 }
+
+// Select how unfilled parent-buffer slots are read (see g_stale_mode).
+int dkto_set_stale_mode(int mode) { g_stale_mode = mode; return 0; }
 
 // Unpreconditioned or Jacobi-preconditioned CG in the form of
 // HeatMat::cgSolve (FEM/examples/src/heatMat.cpp:164-325), stopping on

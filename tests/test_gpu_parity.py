@@ -55,8 +55,11 @@ def test_golden_da_and_matvec(dkt, path):
     assert np.array_equal(da.boundary_ids(), g["bdry"])
     A = dkt.Matrix(da, op=op)
     assert A.stats()["stale_slots"] == 0
-    assert _rel(_gpu_mv(A, g["x"]), g["y"]) <= TOL
-    assert _rel(_gpu_mv(A, g["x"], raw=True), g["y_raw"]) <= TOL
+    modes = [dkt.ARITH_FP64, dkt.ARITH_AUTO] if order == 1 else [dkt.ARITH_AUTO]
+    for mode in modes:   # native FP64 kernel and, for Q1, the exact fixed-point kernel
+        A.set_arithmetic(mode)
+        assert _rel(_gpu_mv(A, g["x"]), g["y"]) <= TOL, mode
+        assert _rel(_gpu_mv(A, g["x"], raw=True), g["y_raw"]) <= TOL, mode
 
 
 def test_plan_from_nodes_matches_plan_from_da(dkt):
@@ -90,9 +93,11 @@ def test_gaussian_meshes_vs_oracle(dkt, dim, n, md, order, op):
     assert np.array_equal(da.boundary_ids(), ora.bdry)
     A = dkt.Matrix(da, op=op)
     x = dkt.uniform_pm1(1, da.n)
-    y = _gpu_mv(A, x)
     yr = ora.matvec(x)
-    assert _rel(y, yr) <= TOL
+    assert _rel(_gpu_mv(A, x), yr) <= TOL
+    if order == 1:
+        A.set_arithmetic(dkt.ARITH_FP64)
+        assert _rel(_gpu_mv(A, x), yr) <= TOL
     st, ost = A.stats(), ora.stats()
     assert st["leaves"] == ost["leaves"] and st["hanging_leaves"] == ost["hanging_leaves"]
     assert st["stale_slots"] == 0 and ost["stale_reads"] == 0
@@ -172,6 +177,32 @@ def _lapmass_ref(dim, order):
     for d in range(dim):
         M = np.kron(m1, M)
     return K, M
+
+
+@pytest.mark.parametrize("dim,order", [(2, 1), (3, 1), (4, 1), (3, 2), (4, 2)])
+def test_single_element_equals_dense_operator(dkt, dim, order):
+    """A one-element mesh (the root cell): fem::matvec is the dense element
+    matrix of the built-in Laplacian+mass at level 0 applied to x."""
+    md = 6
+    c = np.zeros((1, dim), np.uint32)
+    lv = np.zeros(1, np.uint8)
+    da = dkt.DA(c, lv, dim, order=order, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    orc.set_curve(dim, md)
+    ora = orc.DA(c, lv, dim, order, 2)
+    x = dkt.uniform_pm1(7, da.n)
+    assert _rel(_gpu_mv(A, x, raw=True), ora.matvec_raw(x)) <= TOL
+
+
+def test_fixed_point_is_deterministic(dkt):
+    dim, md = 3, 9
+    pts = dkt.gaussian_points(2000, dim, md, seed=2)
+    tc, tl = dkt.tree_from_points(pts, dim, md)
+    da = dkt.DA(tc, tl, dim, order=1, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_HEAT)
+    x = dkt.uniform_pm1(5, da.n)
+    ys = [_gpu_mv(A, x) for _ in range(3)]
+    assert all(np.array_equal(ys[0], y) for y in ys[1:])
 
 
 def test_cg_solves_lapmass(dkt):
