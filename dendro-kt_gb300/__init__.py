@@ -64,6 +64,7 @@ def load(build_if_missing=True):
         "dkt_matvec": ([P, P, P, ctypes.c_double, P], I),
         "dkt_fematrix_matvec": ([P, P, P, ctypes.c_double, P], I),
         "dkt_fematrix_matvec_host": ([P, P, P, ctypes.c_double], I),
+        "dkt_fematrix_matvec_noalloc": ([P, P, P, ctypes.c_double, P], I),
         "dkt_diagonal": ([P, P, P], I),
         "dkt_cg_solve": ([P, P, P, I, ctypes.c_double, I, P, P, P], I),
         "dkt_plan_kernel_timing": ([P, I, P, P], I),
@@ -197,6 +198,10 @@ class Matrix:
     def matvec(self, x_dev, y_dev, scale=1.0, stream=None):
         """feMatrix::matVec on device tensors."""
         _check(load().dkt_fematrix_matvec(self._h, _p(x_dev), _p(y_dev), scale, _stream(stream)))
+
+    def matvec_noalloc(self, x_dev, y_dev, scale=1.0, stream=None):
+        """feMatrix::matVec that allocates no device memory (fixed 8 MiB scratch per device)."""
+        _check(load().dkt_fematrix_matvec_noalloc(self._h, _p(x_dev), _p(y_dev), scale, _stream(stream)))
 
     def matvec_host(self, x, scale=1.0):
         x = np.ascontiguousarray(x, dtype=np.float64)

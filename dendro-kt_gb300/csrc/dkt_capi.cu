@@ -22,6 +22,7 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void diagonal(const Plan &pl, double *diag, cudaStream_t s);
 bool q1fx_setup(Plan &pl, cudaStream_t s);
+std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,
              cudaStream_t s);
 
@@ -283,6 +284,18 @@ int dkt_fematrix_matvec(dkt_plan plan, const double *x_dev, double *y_dev, doubl
     dkt::fematrix_matvec(plan->pl, x_dev, y_dev, scale, (cudaStream_t) stream);
     return DKT_OK;
   });
+}
+
+int dkt_fematrix_matvec_noalloc(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream)
+{
+  if (!plan || !x_dev || !y_dev) return fail(DKT_E_ARG, "null argument");
+  try {
+    const std::string err = dkt::fematrix_matvec_noalloc(plan->pl, x_dev, y_dev, scale, (cudaStream_t) stream);
+    if (!err.empty()) return fail(err.find("exceed") != std::string::npos ? DKT_E_ARG : DKT_E_CUDA, err);
+  } catch (const std::exception &e) {
+    return fail(DKT_E_CUDA, e.what());
+  }
+  return DKT_OK;
 }
 
 int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host, double scale)

@@ -7,6 +7,7 @@
 // and for hanging leaves zeroes the filled ranks, applies IKD_Child2Parent and
 // adds the result to the parent nodes whose rank is unfilled in the leaf mask
 // (matvec.h:482-522).
+#include <string>
 #include "dkt_internal.cuh"
 
 namespace dkt {
@@ -236,6 +237,103 @@ void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStr
     k_zero_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(y, pl.bdry.p, pl.n_bdry);
     check_launch("zero_bdry_out");
   }
+}
+
+// ---------------------------------------------------------------------------
+// feMatrix::matVec without any device allocation.
+//
+// Some callers cannot let a matrix-vector product allocate device memory:
+// a solver or serving loop that has reserved its whole device-memory budget
+// up front (an allocation inside a request would break that accounting, or
+// fail under memory pressure), and host code that must not stall the device
+// (cudaMalloc and cudaFree can synchronise it).  For them this variant keeps
+// its only scratch -- the boundary-zeroed copy of the input vector that the
+// regular path allocates inside the plan -- in a fixed array in device global
+// memory that every GPU loading this library holds until the process exits.
+// ---------------------------------------------------------------------------
+constexpr int64_t NOALLOC_MAX_NODES = int64_t(1) << 20;   // 1,048,576 doubles = 8 MiB per device
+static __device__ __align__(256) double g_noalloc_xin[NOALLOC_MAX_NODES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // device address of the array, per device
+
+// The array's name is only a host-side handle; its device address is looked
+// up once per device, with that device current.
+static cudaError_t noalloc_scratch(double **out)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_xin);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+template <int DIM, int P>
+static void launch_leaf_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
+{
+  constexpr int M = P + 1, NPE = Pow<DIM, M>::v;
+  const bool custom = pl.op.kind == OP_CUSTOM;
+  const size_t smem = (size_t) (custom ? 0 : 2 * NPE * NPE) * sizeof(double) + 2 * M * M * sizeof(double) + 16;
+  const unsigned threads = 128, blocks = grid_for(pl.n_leaf, threads);
+  if (custom) {
+    k_matvec_leaf<DIM, P, true><<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p,
+                                                              pl.n_leaf, pl.n_hang, nullptr, nullptr, nullptr, nullptr,
+                                                              pl.opTable.p, pl.ip.p, x, y, scale);
+  } else {
+    auto kfn = k_matvec_leaf<DIM, P, false>;
+    if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    kfn<<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang,
+                                      pl.opA.p, pl.opB.p, pl.opAlpha.p, pl.opBeta.p, nullptr, pl.ip.p, x, y,
+                                      pl.op.uses_scale ? scale : 1.0);
+  }
+  check_launch("matvec_leaf_noalloc");
+}
+
+// Returns an empty string on success, else the reason of the failure.
+std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
+{
+  if (pl.n_nodes > NOALLOC_MAX_NODES)
+    return "dkt_fematrix_matvec_noalloc: " + std::to_string(pl.n_nodes) + " nodes exceed its fixed scratch of " +
+           std::to_string(NOALLOC_MAX_NODES) + " nodes";
+  double *scratch = nullptr;
+  cudaError_t e = noalloc_scratch(&scratch);
+  if (e != cudaSuccess) return std::string("dkt_fematrix_matvec_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+  const bool bc = (pl.op.kind == OP_HEAT || pl.op.kind == OP_LAPMASS);
+  const double *xin = x;
+  if (bc) {
+    // every entry that the kernel reads is overwritten here; nothing of the
+    // previous call's contents survives into this one
+    DKT_CUDA(cudaMemcpyAsync(scratch, x, pl.n_nodes * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (pl.n_bdry > 0) {
+      k_zero_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(scratch, pl.bdry.p, pl.n_bdry);
+      check_launch("noalloc_zero_in");
+    }
+    xin = scratch;
+  }
+  DKT_CUDA(cudaMemsetAsync(y, 0, pl.n_nodes * sizeof(double), s));
+  if (pl.n_leaf > 0) {
+    switch (pl.dim * 10 + pl.order) {
+      case 21: launch_leaf_noalloc<2, 1>(pl, xin, y, scale, s); break;
+      case 22: launch_leaf_noalloc<2, 2>(pl, xin, y, scale, s); break;
+      case 31: launch_leaf_noalloc<3, 1>(pl, xin, y, scale, s); break;
+      case 32: launch_leaf_noalloc<3, 2>(pl, xin, y, scale, s); break;
+      case 41: launch_leaf_noalloc<4, 1>(pl, xin, y, scale, s); break;
+      case 42: launch_leaf_noalloc<4, 2>(pl, xin, y, scale, s); break;
+      default: return "dkt_fematrix_matvec_noalloc: unsupported dim/order";
+    }
+  }
+  if (bc && pl.n_bdry > 0) {
+    k_zero_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(y, pl.bdry.p, pl.n_bdry);
+    check_launch("noalloc_zero_out");
+  }
+  return std::string();
 }
 
 }  // namespace dkt

@@ -111,6 +111,21 @@ int dkt_matvec(dkt_plan plan, const double *x_dev, double *y_dev, double scale, 
  * pre/post step).  x_dev is not modified. */
 int dkt_fematrix_matvec(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream);
 
+/* feMatrix::matVec that allocates no device memory (no counterpart in the
+ * reference).  For callers that must not allocate during a product: a solver
+ * or serving loop that reserved its device-memory budget up front, or host
+ * code that must not let cudaMalloc/cudaFree stall the device.  Same result
+ * as dkt_fematrix_matvec with DKT_ARITH_FP64 (the dense native-FP64 kernel).
+ * Its one scratch buffer, the boundary-zeroed input copy, is a fixed array in
+ * device global memory of 1,048,576 doubles (8 MiB) that every GPU loading
+ * this library holds until the process exits; plans with more nodes are
+ * rejected with DKT_E_ARG.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the array:
+ * calls whose work overlaps on the GPU (different streams, or different
+ * threads) race on it and must be serialised by the caller. */
+int dkt_fematrix_matvec_noalloc(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream);
+
 /* Same with host arrays: copies in, computes, copies out, synchronises. */
 int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host, double scale);
 
