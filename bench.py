@@ -113,8 +113,8 @@ def algorithmic_bytes(stats, n_nodes, npe):
     return 16 * n_nodes + (4 * npe + 4) * nl + (4 * npe + 12 + 4) * nh
 
 
-def moving_ball(dkt, level):
-    return dkt.moving_ball_tree(max_depth=MD, level=level, radius=0.2, halfwidth=2.0 ** -level)
+def moving_ball(dkt, level, device=False):
+    return dkt.moving_ball_tree(max_depth=MD, level=level, radius=0.2, halfwidth=2.0 ** -level, device=device)
 
 
 # ---------------------------------------------------------------------------
@@ -189,7 +189,7 @@ def run_gpu(a, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     t0 = time.perf_counter()
-    tc, tl = moving_ball(dkt, a.level)
+    tc, tl = moving_ball(dkt, a.level, device=True)
     t_mesh = time.perf_counter() - t0
     da = dkt.DA(tc, tl, 4, order=a.order, max_depth=MD)
     t_da = time.perf_counter() - t0 - t_mesh

@@ -16,8 +16,9 @@ _lib = None
 
 OK, E_ARG, E_CUDA, E_NOMEM, E_UNSUP, E_NOCONV, E_INTERNAL = 0, -1, -2, -3, -4, -5, -6
 CURVE_MORTON, CURVE_HILBERT = 0, 1
-OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM = 0, 1, 2, 3
+OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM, OP_LAPLACE, OP_MASS = 0, 1, 2, 3, 4, 5
 ARITH_AUTO, ARITH_FP64, ARITH_FIXED = 0, 1, 2
+TRAVERSAL_REFERENCE, TRAVERSAL_CONFORMING = 0, 1
 
 
 class DktError(RuntimeError):
@@ -57,6 +58,7 @@ def load(build_if_missing=True):
         "dkt_da_get_tree": ([P, P, P], I),
         "dkt_da_destroy": ([P], None),
         "dkt_plan_create": ([P, I, P, P], I),
+        "dkt_plan_create_ex": ([P, I, P, I, P], I),
         "dkt_plan_create_from_nodes": ([I, I, I, I, P, P, I64, I, P, P], I),
         "dkt_plan_num_nodes": ([P], I64),
         "dkt_plan_stats": ([P, P], I),
@@ -74,6 +76,7 @@ def load(build_if_missing=True):
         "dkt_mesh_tree_from_points": ([P, I64, I, I, I64, P, P, P], I),
         "dkt_mesh_moving_ball": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
         "dkt_free": ([P], None),
+        "dkt_mesh_moving_ball_device": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
         "dkt_probe_device": ([P], I),
     }
     for name, (args, res) in sig.items():
@@ -155,13 +158,13 @@ class Matrix:
     """feMatrix<LeafT,dim> over a DA (or a bare node list) with a device plan."""
 
     def __init__(self, da=None, op=OP_LAPMASS, tables=None, nodes=None, dim=None, order=1, max_depth=10,
-                 curve=CURVE_MORTON):
+                 curve=CURVE_MORTON, traversal=TRAVERSAL_REFERENCE):
         L = load()
         h = ctypes.c_void_p()
         t = None if tables is None else np.ascontiguousarray(tables, dtype=np.float64)
         tp = None if t is None else _p(t)
         if da is not None:
-            _check(L.dkt_plan_create(da.handle, op, tp, ctypes.byref(h)))
+            _check(L.dkt_plan_create_ex(da.handle, op, tp, traversal, ctypes.byref(h)))
         else:
             c = np.ascontiguousarray(nodes[0], dtype=np.uint32).reshape(-1, dim)
             lv = np.ascontiguousarray(nodes[1], dtype=np.uint8)
@@ -183,13 +186,13 @@ class Matrix:
         st = self.stats()
         nl, nh = st["leaves"], st["hanging_leaves"]
         npe = self.npe
-        e2n = np.empty((npe, nl), np.int32)
+        e2n = np.empty((nl, npe), np.int32)
         info = np.empty(nl, np.uint32)
         hidx = np.empty(nl, np.int32)
-        p2n = np.empty((npe, max(nh, 1)), np.int32)
-        fill = np.empty((3, max(nh, 1)), np.uint32)
+        p2n = np.empty((max(nh, 1), npe), np.int32)
+        fill = np.empty((max(nh, 1), 3), np.uint32)
         _check(load().dkt_plan_export(self._h, _p(e2n), _p(info), _p(hidx), _p(p2n), _p(fill)))
-        return e2n, info, hidx, p2n[:, :nh], fill[:, :nh]
+        return e2n, info, hidx, p2n[:nh], fill[:nh]
 
     def matvec_raw(self, x_dev, y_dev, scale=1.0, stream=None):
         """fem::matvec on device tensors (no boundary handling)."""
@@ -273,14 +276,17 @@ def tree_from_points(points, dim, max_depth, max_pts=1):
     return _take_cells(n, c, lv, dim)
 
 
-def moving_ball_tree(max_depth, level, radius=0.2, halfwidth=None, c0=(0.3, 0.3, 0.3), c1=(0.7, 0.7, 0.7)):
+def moving_ball_tree(max_depth, level, radius=0.2, halfwidth=None, c0=(0.3, 0.3, 0.3), c1=(0.7, 0.7, 0.7),
+                     device=False):
+    """Spacetime moving-ball tree (dim 4); device=True builds it on the GPU."""
     if halfwidth is None:
         halfwidth = 2.0 ** -level
     a0 = np.ascontiguousarray(c0, dtype=np.float64)
     a1 = np.ascontiguousarray(c1, dtype=np.float64)
     n, c, lv = ctypes.c_int64(0), ctypes.c_void_p(), ctypes.c_void_p()
-    _check(load().dkt_mesh_moving_ball(max_depth, level, radius, halfwidth, _p(a0), _p(a1), ctypes.byref(n),
-                                       ctypes.byref(c), ctypes.byref(lv)))
+    fn = load().dkt_mesh_moving_ball_device if device else load().dkt_mesh_moving_ball
+    _check(fn(max_depth, level, radius, halfwidth, _p(a0), _p(a1), ctypes.byref(n), ctypes.byref(c),
+              ctypes.byref(lv)))
     return _take_cells(n, c, lv, 4)
 
 

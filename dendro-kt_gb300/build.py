@@ -16,7 +16,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libdkt_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["dkt_da.cu", "dkt_plan.cu", "dkt_matvec.cu", "dkt_cg.cu", "dkt_capi.cu", "dkt_probe.cu", "dkt_q1fx.cu"]
+CU = ["dkt_da.cu", "dkt_plan.cu", "dkt_matvec.cu", "dkt_cg.cu", "dkt_capi.cu", "dkt_probe.cu", "dkt_q1fx.cu", "dkt_stale.cu", "dkt_tree.cu"]
 CPP = ["dkt_host.cpp"]
 
 
@@ -52,7 +52,7 @@ def _compile(src, verbose_ptxas=False):
         if verbose_ptxas:
             cmd.insert(1, "-Xptxas=-v")
     else:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-c", src, "-o", obj]
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("compile failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))

@@ -22,6 +22,11 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void diagonal(const Plan &pl, double *diag, cudaStream_t s);
 bool q1fx_setup(Plan &pl, cudaStream_t s);
+void moving_ball_device(int md, int level, double R, double w, const double *c0, const double *c1,
+                        DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s);
+void unpack_cells_to_host(const DBuf<uint64_t> &keys, int64_t n, int dim, int md, uint32_t *coords, uint8_t *levels,
+                          cudaStream_t s);
+void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s);
 std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,
              cudaStream_t s);
@@ -76,7 +81,7 @@ int check_cfg(int dim, int order, int curve, int md)
 
 void setup_operator(dkt::Plan &pl, int op, const double *tables, cudaStream_t s)
 {
-  if (op < 0 || op > 3) throw std::invalid_argument("unknown operator");
+  if (op < 0 || op > 5) throw std::invalid_argument("unknown operator");
   pl.op.kind = op;
   pl.op.npe = pl.npe;
   pl.op.nlev = pl.md + 1;
@@ -181,12 +186,14 @@ int dkt_da_get_tree(dkt_da da, uint32_t *coords, uint8_t *levels)
 void dkt_da_destroy(dkt_da da) { delete da; }
 
 static int plan_common(int dim, int order, int curve, int md, const uint32_t *node_x_dev, const uint8_t *node_lev_dev,
-                       int64_t n, const uint32_t *bdry_dev, int64_t nb, int op, const double *tables, dkt_plan *out)
+                       int64_t n, const uint32_t *bdry_dev, int64_t nb, int op, const double *tables, dkt_plan *out,
+                       int traversal = DKT_TRAVERSAL_REFERENCE)
 {
   dkt_plan_s *h = new dkt_plan_s();
   try {
     dkt::Plan &pl = h->pl;
     pl.dim = dim; pl.order = order; pl.md = md;
+    pl.conforming = (traversal == DKT_TRAVERSAL_CONFORMING);
     cudaStream_t s = 0;
     dkt::CurveHost cv;
     cv.morton(dim);
@@ -194,6 +201,7 @@ static int plan_common(int dim, int order, int curve, int md, const uint32_t *no
     const std::vector<double> ip = interp_tables(order);
     dkt::build_plan(pl, node_x_dev, node_lev_dev, n, cv, ip.data(), s);
     setup_operator(pl, op, tables, s);
+    dkt::stale_setup(pl, ip, s);
     dkt::q1fx_setup(pl, s);
     if (bdry_dev) {
       pl.bdry.alloc(nb > 0 ? nb : 1);
@@ -218,6 +226,17 @@ int dkt_plan_create(dkt_da da, int op, const double *op_tables, dkt_plan *out)
     const dkt::DA &d = da->da;
     return plan_common(d.dim, d.order, d.curve, d.md, d.node_x.p, d.node_lev.p, d.n_nodes, d.bdry.p, d.n_bdry, op,
                        op_tables, out);
+  });
+}
+
+int dkt_plan_create_ex(dkt_da da, int op, const double *op_tables, int traversal, dkt_plan *out)
+{
+  if (!da || !out) return fail(DKT_E_ARG, "null argument");
+  if (traversal != DKT_TRAVERSAL_REFERENCE && traversal != DKT_TRAVERSAL_CONFORMING) return fail(DKT_E_ARG, "bad traversal");
+  return guarded([&]() {
+    const dkt::DA &d = da->da;
+    return plan_common(d.dim, d.order, d.curve, d.md, d.node_x.p, d.node_lev.p, d.n_nodes, d.bdry.p, d.n_bdry, op,
+                       op_tables, out, traversal);
   });
 }
 
@@ -415,6 +434,26 @@ int dkt_mesh_moving_ball(int max_depth, int level, double radius, double halfwid
   return guarded([&]() {
     const auto cells = dkt::moving_ball_tree(max_depth, level, radius, halfwidth, c0, c1);
     return export_cells(cells, 4, n_out, coords, levels);
+  });
+}
+
+int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double halfwidth, const double *c0,
+                                const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels)
+{
+  if (!c0 || !c1 || !n_out || !coords || !levels || level < 1 || level > max_depth || 4 * max_depth + 6 > 64)
+    return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    dkt::DBuf<uint64_t> keys;
+    int64_t n = 0;
+    dkt::moving_ball_device(max_depth, level, radius, halfwidth, c0, c1, keys, n, 0);
+    uint32_t *c = (uint32_t *) std::malloc((size_t) n * 4 * sizeof(uint32_t) + 1);
+    uint8_t *l = (uint8_t *) std::malloc((size_t) n + 1);
+    if (!c || !l) { std::free(c); std::free(l); return fail(DKT_E_NOMEM, "host allocation failed"); }
+    dkt::unpack_cells_to_host(keys, n, 4, max_depth, c, l, 0);
+    *n_out = n;
+    *coords = c;
+    *levels = l;
+    return DKT_OK;
   });
 }
 

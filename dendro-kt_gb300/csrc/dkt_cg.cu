@@ -86,7 +86,7 @@ __global__ void k_diag(const int32_t *__restrict__ e2n, const uint32_t *__restri
   if (i >= n_leaf) return;
   const int L = info[i] & 0xFFu;
   for (int r = 0; r < npe; r++) {
-    const int32_t n = e2n[(int64_t) r * n_leaf + i];
+    const int32_t n = e2n[(int64_t) i * npe + r];
     if (n < 0) continue;
     const double v = table ? table[((int64_t) L * npe + r) * npe + r]
                            : alpha[L] * A[r * npe + r] + beta[L] * B[r * npe + r];
@@ -111,7 +111,7 @@ void diagonal(const Plan &pl, double *diag, cudaStream_t s)
   k_diag<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.e2n.p, pl.info.p, pl.n_leaf, pl.npe, pl.opA.p, pl.opB.p,
                                              pl.opAlpha.p, pl.opBeta.p, custom ? pl.opTable.p : nullptr, diag);
   check_launch("diag");
-  if ((pl.op.kind == OP_HEAT || pl.op.kind == OP_LAPMASS) && pl.n_bdry > 0) {
+  if (op_has_bc(pl.op.kind) && pl.n_bdry > 0) {
     k_set_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(diag, pl.bdry.p, pl.n_bdry, 1.0);
     check_launch("diag_bdry");
   }

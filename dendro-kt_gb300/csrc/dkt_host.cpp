@@ -135,8 +135,8 @@ void builtin_operator(int kind, int dim, int p, int md, std::vector<double> &A, 
   tensor_matrix(re, dim, -1, B);   // mass
   for (int l = 0; l <= md; l++) {
     const double J = 0.5 * std::ldexp(1.0, -l);
-    alpha[l] = std::pow(J, dim - 2);
-    beta[l] = std::pow(J, dim);
+    alpha[l] = (kind == 5) ? 0.0 : std::pow(J, dim - 2);   // 5: mass only
+    beta[l] = (kind == 4) ? 0.0 : std::pow(J, dim);         // 4: Laplacian only
   }
 }
 

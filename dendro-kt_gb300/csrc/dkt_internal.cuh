@@ -132,7 +132,9 @@ struct DA {
 // Elemental operator K_L = alpha[L] * A + beta[L] * B (dense nPe x nPe, the
 // reference's lexicographic node order, x fastest), or one dense table per
 // level when kind == custom.
-enum OpKind { OP_IDENTITY = 0, OP_HEAT = 1, OP_LAPMASS = 2, OP_CUSTOM = 3 };
+enum OpKind { OP_IDENTITY = 0, OP_HEAT = 1, OP_LAPMASS = 2, OP_CUSTOM = 3, OP_LAPLACE = 4, OP_MASS = 5 };
+// operators whose feMatrix pre/post steps zero the domain-boundary entries
+__host__ __device__ inline bool op_has_bc(int k) { return k == OP_HEAT || k == OP_LAPMASS || k == OP_LAPLACE; }
 
 struct Operator {
   int kind = OP_LAPMASS;
@@ -146,19 +148,28 @@ struct Operator {
 // Flattened traversal: one record per leaf visit of fem::matvec.
 struct Plan {
   int dim = 3, order = 1, md = 10, npe = 8;
+  // false: the reference traversal (parent values only from level L-1 nodes,
+  // transpose masked by the leaf fill mask); true: the conforming P^T K P
+  bool conforming = false;
   int64_t n_nodes = 0, n_leaf = 0, n_hang = 0, n_bdry = 0;
   int64_t stale_slots = 0;           // parent slots read unfilled with nonzero weight
-  DBuf<int32_t> e2n;                 // [npe][n_leaf]  node index or -1
+  DBuf<int32_t> e2n;                 // [n_leaf][npe]  node index or -1
   DBuf<uint32_t> info;               // [n_leaf] level | child<<8 | hanging<<16
   DBuf<int32_t> hidx;                // [n_leaf] index into hanging arrays or -1
-  DBuf<int32_t> p2n;                 // [npe][n_hang] parent node index (level L-1) or -1
-  DBuf<uint32_t> fill;               // [3][n_hang] filled-rank bitmask of the leaf
+  DBuf<int32_t> p2n;                 // [n_hang][npe] parent node index (level L-1) or -1
+  DBuf<uint32_t> fill;               // [n_hang][3] filled-rank bitmask of the leaf
   DBuf<uint32_t> bdry;               // boundary node ids
   DBuf<double> opA, opB, opAlpha, opBeta, opTable;
   DBuf<double> ip;                   // [2][M][M] child interpolation (ip_1D_0, ip_1D_1)
   Operator op;
   DBuf<double> xin;                  // scratch: boundary-zeroed input
   DBuf<double> xh, yh;               // device copies for the host-array entry point
+  // Emulation of the reference's static parent buffer (dkt_stale.cu).
+  bool st_ready = false;
+  int64_t st_start = 0, st_n_ent = 0, st_n_runs = 0;
+  DBuf<int32_t> st_row, st_idx, st_runs, st_hzoff, st_hztab, st_srow, st_sidx, st_gstart;
+  DBuf<double> st_w, st_v, st_sw, st_f;
+  DBuf<long long> st_vq;
   // Exact fixed-point path of the Q1 built-in operators (dkt_q1fx.cu).
   int arith = 0;                     // 0 auto, 1 native FP64, 2 fixed point
   bool fx_ready = false;

@@ -68,7 +68,8 @@ __host__ __device__ __forceinline__ void leaf_body(
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
     const double *sA, const double *sB, const double *__restrict__ alpha, const double *__restrict__ beta,
     const double *__restrict__ table, const double *sip, const double *__restrict__ x, double *__restrict__ y,
-    double scale)
+    double scale, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
+    const double *__restrict__ stv, int conforming)
 {
   constexpr int M = P + 1, NPE = Pow<DIM, M>::v;
   constexpr int UR = NPE <= 16 ? NPE : 1;
@@ -80,19 +81,26 @@ __host__ __device__ __forceinline__ void leaf_body(
   int32_t nd[NPE];
 #pragma unroll UR
   for (int r = 0; r < NPE; r++) {
-    nd[r] = e2n[(int64_t) r * n_leaf + i];
+    nd[r] = e2n[(int64_t) i * NPE + r];
     u[r] = nd[r] >= 0 ? x[nd[r]] : 0.0;
   }
   int64_t h = 0;
   uint32_t fm[3] = {0, 0, 0};
   if (hang) {
     h = hidx[i];
-    for (int w = 0; w < 3; w++) fm[w] = fill[(int64_t) w * n_hang + h];
+    for (int w = 0; w < 3; w++) fm[w] = fill[(int64_t) h * 3 + w];
     double xp[NPE];
+    const int32_t hz = hzoff ? hzoff[h] : -1;   // slots this leaf reads from the static buffer
 #pragma unroll UR
     for (int q = 0; q < NPE; q++) {
-      const int32_t pn = p2n[(int64_t) q * n_hang + h];
-      xp[q] = pn >= 0 ? x[pn] : 0.0;
+      const int32_t pn = p2n[(int64_t) h * NPE + q];
+      double v = 0.0;
+      if (pn >= 0) v = x[pn];
+      else if (hz >= 0) {
+        const int32_t id = hztab[(int64_t) hz * NPE + q];
+        if (id >= 0) v = stv[id];
+      }
+      xp[q] = v;
     }
     interp<DIM, M, false>(xp, sip, child);
 #pragma unroll UR
@@ -129,8 +137,8 @@ __host__ __device__ __forceinline__ void leaf_body(
     interp<DIM, M, true>(out, sip, child);
 #pragma unroll UR
     for (int q = 0; q < NPE; q++) {
-      const int32_t pn = p2n[(int64_t) q * n_hang + h];
-      if (pn >= 0 && !((fm[q >> 5] >> (q & 31)) & 1u)) accum(&y[pn], out[q]);
+      const int32_t pn = p2n[(int64_t) h * NPE + q];
+      if (pn >= 0 && (conforming || !((fm[q >> 5] >> (q & 31)) & 1u))) accum(&y[pn], out[q]);
     }
   }
 }
@@ -141,7 +149,8 @@ __global__ void __launch_bounds__(128) k_matvec_leaf(
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
     const double *__restrict__ gA, const double *__restrict__ gB, const double *__restrict__ alpha,
     const double *__restrict__ beta, const double *__restrict__ table, const double *__restrict__ gip,
-    const double *__restrict__ x, double *__restrict__ y, double scale)
+    const double *__restrict__ x, double *__restrict__ y, double scale, const int32_t *__restrict__ hzoff,
+    const int32_t *__restrict__ hztab, const double *__restrict__ stv, int conforming)
 {
   constexpr int M = P + 1, NPE = Pow<DIM, M>::v;
   constexpr int UR = NPE <= 16 ? NPE : 1;
@@ -157,7 +166,7 @@ __global__ void __launch_bounds__(128) k_matvec_leaf(
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_leaf) return;
   leaf_body<DIM, P, CUSTOM>(i, e2n, info, hidx, p2n, fill, n_leaf, n_hang, sA, sB, alpha, beta, table, sip, x, y,
-                            scale);
+                            scale, hzoff, hztab, stv, conforming);
 }
 
 __global__ void k_zero_at(double *__restrict__ v, const uint32_t *__restrict__ ids, int64_t nb)
@@ -165,6 +174,10 @@ __global__ void k_zero_at(double *__restrict__ v, const uint32_t *__restrict__ i
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nb) v[ids[i]] = 0.0;
 }
+
+#define ST_ARGS (pl.st_ready ? pl.st_hzoff.p : nullptr), pl.st_hztab.p, pl.st_v.p, (pl.conforming ? 1 : 0)
+
+void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s);
 
 template <int DIM, int P>
 static void launch_leaf(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
@@ -183,13 +196,13 @@ static void launch_leaf(Plan &pl, const double *x, double *y, double scale, cuda
   if (custom) {
     auto kfn = k_matvec_leaf<DIM, P, true>;
     kfn<<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang,
-                                      nullptr, nullptr, nullptr, nullptr, pl.opTable.p, pl.ip.p, x, y, scale);
+                                      nullptr, nullptr, nullptr, nullptr, pl.opTable.p, pl.ip.p, x, y, scale, ST_ARGS);
   } else {
     auto kfn = k_matvec_leaf<DIM, P, false>;
     if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
     kfn<<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang,
                                       pl.opA.p, pl.opB.p, pl.opAlpha.p, pl.opBeta.p, nullptr, pl.ip.p, x, y,
-                                      pl.op.uses_scale ? scale : 1.0);
+                                      pl.op.uses_scale ? scale : 1.0, ST_ARGS);
   }
   check_launch("matvec_leaf");
   if (pl.timing) {
@@ -208,6 +221,7 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
   if (pl.fx_ready && pl.arith != 1) { q1fx_matvec(pl, x, y, scale, false, s); return; }
   DKT_CUDA(cudaMemsetAsync(y, 0, pl.n_nodes * sizeof(double), s));
   if (pl.n_leaf == 0) return;
+  stale_eval(pl, x, nullptr, s);
   switch (pl.dim * 10 + pl.order) {
     case 21: launch_leaf<2, 1>(pl, x, y, scale, s); break;
     case 22: launch_leaf<2, 2>(pl, x, y, scale, s); break;
@@ -223,7 +237,7 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
 // (HeatMat::preMatVec/postMatVec) for the operators that have them.
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
 {
-  const bool bc = (pl.op.kind == OP_HEAT || pl.op.kind == OP_LAPMASS);
+  const bool bc = op_has_bc(pl.op.kind);
   if (pl.fx_ready && pl.arith != 1) { q1fx_matvec(pl, x, y, scale, bc, s); return; }
   if (!bc) { matvec(pl, x, y, scale, s); return; }
   if (pl.xin.n < (size_t) pl.n_nodes) pl.xin.alloc(pl.n_nodes);
@@ -285,13 +299,13 @@ static void launch_leaf_noalloc(const Plan &pl, const double *x, double *y, doub
   if (custom) {
     k_matvec_leaf<DIM, P, true><<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p,
                                                               pl.n_leaf, pl.n_hang, nullptr, nullptr, nullptr, nullptr,
-                                                              pl.opTable.p, pl.ip.p, x, y, scale);
+                                                              pl.opTable.p, pl.ip.p, x, y, scale, ST_ARGS);
   } else {
     auto kfn = k_matvec_leaf<DIM, P, false>;
     if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
     kfn<<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang,
                                       pl.opA.p, pl.opB.p, pl.opAlpha.p, pl.opBeta.p, nullptr, pl.ip.p, x, y,
-                                      pl.op.uses_scale ? scale : 1.0);
+                                      pl.op.uses_scale ? scale : 1.0, ST_ARGS);
   }
   check_launch("matvec_leaf_noalloc");
 }
@@ -305,7 +319,7 @@ std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, 
   double *scratch = nullptr;
   cudaError_t e = noalloc_scratch(&scratch);
   if (e != cudaSuccess) return std::string("dkt_fematrix_matvec_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
-  const bool bc = (pl.op.kind == OP_HEAT || pl.op.kind == OP_LAPMASS);
+  const bool bc = op_has_bc(pl.op.kind);
   const double *xin = x;
   if (bc) {
     // every entry that the kernel reads is overwritten here; nothing of the
@@ -319,6 +333,7 @@ std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, 
   }
   DKT_CUDA(cudaMemsetAsync(y, 0, pl.n_nodes * sizeof(double), s));
   if (pl.n_leaf > 0) {
+    stale_eval(const_cast<Plan &>(pl), xin, nullptr, s);
     switch (pl.dim * 10 + pl.order) {
       case 21: launch_leaf_noalloc<2, 1>(pl, xin, y, scale, s); break;
       case 22: launch_leaf_noalloc<2, 2>(pl, xin, y, scale, s); break;

@@ -142,7 +142,7 @@ __global__ void k_build_leaves(const uint64_t *__restrict__ cand, int64_t n_cand
                                int dim, int md, int p, int npe, const double *__restrict__ ip,
                                int32_t *__restrict__ e2n, int32_t *__restrict__ p2n, uint32_t *__restrict__ fill,
                                uint32_t *__restrict__ info, uint32_t *__restrict__ valid, uint32_t *__restrict__ hang,
-                               unsigned long long *__restrict__ stale)
+                               unsigned long long *__restrict__ stale, int conforming)
 {
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_cand) return;
@@ -176,7 +176,7 @@ __global__ void k_build_leaves(const uint64_t *__restrict__ cand, int64_t n_cand
     int qq = q;
     for (int d = 0; d < dim; d++) { const int id = qq % M; qq /= M; x[d] = pa[d] + (uint32_t) (plen * id / p); }
     int32_t nd = find_node(lk, li, n_nodes, x, dim, md);
-    if (nd >= 0 && (int) nlev[nd] != L - 1) nd = -1;
+    if (nd >= 0 && !conforming && (int) nlev[nd] != L - 1) nd = -1;
     p2n[i * npe + q] = nd;
     if (nd < 0) {
       // Weight of parent slot q on leaf rank r: prod_d ip_{bit_d}[q_d][r_d].
@@ -222,12 +222,12 @@ __global__ void k_layout(const uint32_t *__restrict__ order, const uint32_t *__r
   const int64_t c = vidx[order[i]];   // candidate index
   const uint32_t inf = info_t[c];
   info[i] = inf;
-  for (int r = 0; r < npe; r++) e2n[(int64_t) r * n_leaf + i] = e2n_t[c * npe + r];
+  for (int r = 0; r < npe; r++) e2n[(int64_t) i * npe + r] = e2n_t[c * npe + r];
   if ((inf >> 16) & 1u) {
     const int64_t h = hpos[i];
     hidx[i] = (int32_t) h;
-    for (int q = 0; q < npe; q++) p2n[(int64_t) q * n_hang + h] = p2n_t[c * npe + q];
-    for (int w = 0; w < 3; w++) fill[(int64_t) w * n_hang + h] = fill_t[c * 3 + w];
+    for (int q = 0; q < npe; q++) p2n[(int64_t) h * npe + q] = p2n_t[c * npe + q];
+    for (int w = 0; w < 3; w++) fill[(int64_t) h * 3 + w] = fill_t[c * 3 + w];
   } else {
     hidx[i] = -1;
   }
@@ -328,7 +328,7 @@ void build_plan(Plan &pl, const uint32_t *node_x, const uint8_t *node_lev, int64
   DKT_CUDA(cudaMemsetAsync(stale.p, 0, sizeof(unsigned long long), s));
   k_build_leaves<<<grid_for(n_cand, 128), 128, 0, s>>>(cand.p, n_cand, lk.p, li.p, node_lev, n_nodes, dim, md, p, npe,
                                                   ipd.p, e2n_t.p, p2n_t.p, fill_t.p, info_t.p, valid.p, hang.p,
-                                                  stale.p);
+                                                  stale.p, pl.conforming ? 1 : 0);
   check_launch("build_leaves");
   unsigned long long st = 0;
   DKT_CUDA(cudaMemcpyAsync(&st, stale.p, sizeof(st), cudaMemcpyDeviceToHost, s));

@@ -31,58 +31,21 @@ __device__ __forceinline__ long long mulshift(long long v, long long m, int e)
   return (long long) ((lo >> e) | ((unsigned long long) hi << (64 - e)));
 }
 
-// In-place Walsh-Hadamard transform over DIM axes (rank bit d = axis d).
+// One thread per four lexicographic ranks of a leaf (2^dim / 4 lanes per
+// leaf): butterflies along axes 0 and 1 stay in registers, along the higher
+// axes they are warp shuffles between the lanes of the leaf.  Each lane reads
+// its four node indices with one 16-byte load.  The integer steps are the
+// same as evaluating the leaf sequentially, so results are bit-identical.
 template <int DIM>
-__device__ __forceinline__ void wht(long long *u)
+__device__ __forceinline__ void bfly_reg(long long *v, int d)
 {
-  constexpr int NPE = 1 << DIM;
+  // axis d in {0, 1} inside the thread's four ranks
 #pragma unroll
-  for (int d = 0; d < DIM; d++) {
-#pragma unroll
-    for (int r = 0; r < NPE; r++) {
-      if (r & (1 << d)) continue;
-      const long long a = u[r], b = u[r | (1 << d)];
-      u[r] = a + b;
-      u[r | (1 << d)] = a - b;
-    }
-  }
-}
-
-// Parent -> child interpolation of Q1 (IKD_Parent2Child with ip_1D_{0,1}):
-// along an axis where the child bit is 0, child node 0 takes parent node 0
-// and child node 1 the mean; mirrored when the bit is 1.
-template <int DIM>
-__device__ __forceinline__ void p2c(long long *v, unsigned child)
-{
-  constexpr int NPE = 1 << DIM;
-#pragma unroll
-  for (int d = 0; d < DIM; d++) {
-    const bool hi = (child >> d) & 1u;
-#pragma unroll
-    for (int r = 0; r < NPE; r++) {
-      if (r & (1 << d)) continue;
-      const long long a = v[r], b = v[r | (1 << d)];
-      const long long m = (a + b) >> 1;
-      if (hi) v[r] = m; else v[r | (1 << d)] = m;
-    }
-  }
-}
-
-// Transpose (IKD_Child2Parent with ipT_1D_{0,1}).
-template <int DIM>
-__device__ __forceinline__ void c2p(long long *v, unsigned child)
-{
-  constexpr int NPE = 1 << DIM;
-#pragma unroll
-  for (int d = 0; d < DIM; d++) {
-    const bool hi = (child >> d) & 1u;
-#pragma unroll
-    for (int r = 0; r < NPE; r++) {
-      if (r & (1 << d)) continue;
-      const long long a = v[r], b = v[r | (1 << d)];
-      if (hi) { v[r] = a >> 1; v[r | (1 << d)] = b + (a >> 1); }
-      else { v[r] = a + (b >> 1); v[r | (1 << d)] = b >> 1; }
-    }
+  for (int k = 0; k < 4; k++) {
+    if (k & (1 << d)) continue;
+    const long long a = v[k], b = v[k | (1 << d)];
+    v[k] = a + b;
+    v[k | (1 << d)] = a - b;
   }
 }
 
@@ -91,54 +54,134 @@ __global__ void __launch_bounds__(256) k_matvec_q1fx(
     const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
     const long long *__restrict__ fm, const int *__restrict__ fe, const long long *__restrict__ xq,
-    unsigned long long *__restrict__ yq)
+    unsigned long long *__restrict__ yq, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
+    const long long *__restrict__ stvq, int conforming)
 {
-  constexpr int NPE = 1 << DIM;
-  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_leaf) return;
-  const uint32_t inf = info[i];
+  constexpr int NPE = 1 << DIM, LPL = NPE / 4;
+  const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = tid / LPL;
+  const int sub = (int) (tid % LPL);
+  const int rb = sub * 4;                      // first rank of this lane
+  const bool valid = i < n_leaf;
+  const uint32_t inf = valid ? __ldg(info + i) : 0u;
   const int L = inf & 0xFFu;
   const unsigned child = (inf >> 8) & 0xFFu;
   const bool hang = (inf >> 16) & 1u;
-  long long u[NPE];
-  int32_t nd[NPE];
+  int4 e = make_int4(-1, -1, -1, -1);
+  if (valid) e = __ldg(reinterpret_cast<const int4 *>(e2n + i * NPE + rb));
+  const int nd[4] = {e.x, e.y, e.z, e.w};
+  long long v[4];
 #pragma unroll
-  for (int r = 0; r < NPE; r++) {
-    nd[r] = e2n[(int64_t) r * n_leaf + i];
-    u[r] = nd[r] >= 0 ? __ldg(xq + nd[r]) : 0ll;
-  }
+  for (int k = 0; k < 4; k++) v[k] = nd[k] >= 0 ? __ldg(xq + nd[k]) : 0ll;
   int64_t h = 0;
-  uint32_t fmask = 0;
-  if (hang) {
-    h = hidx[i];
-    fmask = fill[h];
-    long long xp[NPE];
+  uint32_t fmask = 0xFFFFu;
+  int pn[4] = {-1, -1, -1, -1};
+  const bool grp_hang = (LPL > 1) ? (bool) __any_sync(0xffffffffu, hang) : hang;
+  if (grp_hang) {
+    long long xp[4] = {0, 0, 0, 0};
+    if (hang) {
+      h = __ldg(hidx + i);
+      fmask = __ldg(fill + h * 3);
+      const int4 pq = __ldg(reinterpret_cast<const int4 *>(p2n + h * NPE + rb));
+      pn[0] = pq.x; pn[1] = pq.y; pn[2] = pq.z; pn[3] = pq.w;
+      const int32_t hz = hzoff ? __ldg(hzoff + h) : -1;
 #pragma unroll
-    for (int q = 0; q < NPE; q++) {
-      const int32_t pn = p2n[(int64_t) q * n_hang + h];
-      xp[q] = pn >= 0 ? __ldg(xq + pn) : 0ll;
+      for (int k = 0; k < 4; k++) {
+        if (pn[k] >= 0) xp[k] = __ldg(xq + pn[k]);
+        else if (hz >= 0) {
+          const int32_t id = __ldg(hztab + (int64_t) hz * NPE + rb + k);
+          if (id >= 0) xp[k] = __ldg(stvq + id);
+        }
+      }
     }
-    p2c<DIM>(xp, child);
+    // parent -> child interpolation
 #pragma unroll
-    for (int r = 0; r < NPE; r++)
-      if (!((fmask >> r) & 1u)) u[r] = xp[r];
+    for (int d = 0; d < 2; d++) {
+      const bool cb = (child >> d) & 1u;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (k & (1 << d)) continue;
+        const long long m = (xp[k] + xp[k | (1 << d)]) >> 1;
+        if (cb) xp[k] = m; else xp[k | (1 << d)] = m;
+      }
+    }
+#pragma unroll
+    for (int d = 2; d < DIM; d++) {
+      const bool cb = (child >> d) & 1u;
+      const bool mine = (sub >> (d - 2)) & 1;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const long long o = __shfl_xor_sync(0xffffffffu, xp[k], 1 << (d - 2));
+        if (mine != cb) xp[k] = (xp[k] + o) >> 1;
+      }
+    }
+    if (hang) {
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (!((fmask >> (rb + k)) & 1u)) v[k] = xp[k];
+    }
   }
-  wht<DIM>(u);
+  // Walsh-Hadamard transform, per-mode scaling, transform back
+  bfly_reg<DIM>(v, 0);
+  bfly_reg<DIM>(v, 1);
 #pragma unroll
-  for (int s = 0; s < NPE; s++) u[s] = mulshift(u[s], fm[L * NPE + s], fe[L * NPE + s]);
-  wht<DIM>(u);
+  for (int d = 2; d < DIM; d++) {
+    const bool mine = (sub >> (d - 2)) & 1;
 #pragma unroll
-  for (int r = 0; r < NPE; r++)
-    if (nd[r] >= 0) atomicAdd(yq + nd[r], (unsigned long long) u[r]);
-  if (hang) {
+    for (int k = 0; k < 4; k++) {
+      const long long o = __shfl_xor_sync(0xffffffffu, v[k], 1 << (d - 2));
+      v[k] = mine ? (o - v[k]) : (v[k] + o);
+    }
+  }
+  if (valid) {
 #pragma unroll
-    for (int r = 0; r < NPE; r++)
-      if ((fmask >> r) & 1u) u[r] = 0;
-    c2p<DIM>(u, child);
+    for (int k = 0; k < 4; k++) v[k] = mulshift(v[k], __ldg(fm + L * NPE + rb + k), __ldg(fe + L * NPE + rb + k));
+  }
+  bfly_reg<DIM>(v, 0);
+  bfly_reg<DIM>(v, 1);
 #pragma unroll
-    for (int q = 0; q < NPE; q++) {
-      const int32_t pn = p2n[(int64_t) q * n_hang + h];
-      if (pn >= 0 && !((fmask >> q) & 1u)) atomicAdd(yq + pn, (unsigned long long) u[q]);
+  for (int d = 2; d < DIM; d++) {
+    const bool mine = (sub >> (d - 2)) & 1;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long o = __shfl_xor_sync(0xffffffffu, v[k], 1 << (d - 2));
+      v[k] = mine ? (o - v[k]) : (v[k] + o);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (nd[k] >= 0) atomicAdd(yq + nd[k], (unsigned long long) v[k]);
+  if (grp_hang) {
+    // transpose of the interpolation on the unfilled ranks, into the parent nodes
+    long long z[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) z[k] = (hang && !((fmask >> (rb + k)) & 1u)) ? v[k] : 0ll;
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+      const bool cb = (child >> d) & 1u;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (k & (1 << d)) continue;
+        const long long a = z[k], b = z[k | (1 << d)];
+        if (cb) { z[k] = a >> 1; z[k | (1 << d)] = b + (a >> 1); }
+        else { z[k] = a + (b >> 1); z[k | (1 << d)] = b >> 1; }
+      }
+    }
+#pragma unroll
+    for (int d = 2; d < DIM; d++) {
+      const bool cb = (child >> d) & 1u;
+      const bool mine = (sub >> (d - 2)) & 1;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const long long o = __shfl_xor_sync(0xffffffffu, z[k], 1 << (d - 2));
+        z[k] = (mine == cb) ? z[k] + (o >> 1) : (z[k] >> 1);
+      }
+    }
+    if (hang) {
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (pn[k] >= 0 && (conforming || !((fmask >> (rb + k)) & 1u)))
+          atomicAdd(yq + pn[k], (unsigned long long) z[k]);
     }
   }
 }
@@ -192,6 +235,8 @@ __global__ void k_min_level(const uint32_t *__restrict__ info, int64_t n, int *_
     m = min(m, (int) (info[i] & 0xFFu));
   atomicMin(out, m);
 }
+
+void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s);
 
 // Host setup of the per-(level, mode) factors.  Returns false when the
 // operator is not one of the diagonalisable Q1 built-ins.
@@ -263,9 +308,10 @@ static void launch_q1fx(Plan &pl, cudaStream_t s)
     DKT_CUDA(cudaEventCreate(&e1));
     DKT_CUDA(cudaEventRecord(e0, s));
   }
-  k_matvec_q1fx<DIM><<<grid_for(pl.n_leaf, threads), threads, 0, s>>>(
+  k_matvec_q1fx<DIM><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.fx_fe.p,
-      (const long long *) pl.xq.p, (unsigned long long *) pl.yq.p);
+      (const long long *) pl.xq.p, (unsigned long long *) pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr,
+      pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0);
   check_launch("matvec_q1fx");
   if (pl.timing) {
     DKT_CUDA(cudaEventRecord(e1, s));
@@ -301,6 +347,7 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
     check_launch("zero_in");
   }
   DKT_CUDA(cudaMemsetAsync(pl.yq.p, 0, n * sizeof(long long), s));
+  stale_eval(pl, nullptr, pl.xq.p, s);
   switch (pl.dim) {
     case 2: launch_q1fx<2>(pl, s); break;
     case 3: launch_q1fx<3>(pl, s); break;

@@ -1,0 +1,235 @@
+// Emulation of the reference's function-static parent buffer.
+//
+// fem::matvec interpolates a hanging leaf's missing values from a parent
+// buffer that is function-static (FEM/include/matvec.h:283): it refills only
+// the slots that hold a parent node of level L-1 (matvec.h:415-431), applies
+// IKD_Parent2Child in place to all slots (matvec.h:450), and reads the result
+// at the leaf's unfilled ranks (matvec.h:454-456).  A slot it does not refill
+// keeps the value the previous hanging leaf left there, so for some meshes
+// (the reference then reports "parent is missing needed nodes",
+// matvec.h:443-447) a leaf reads values of earlier leaves.  The buffer state
+// after hanging leaf g is S_g = IP_g * merge(fresh_g, S_{g-1}), linear in the
+// input vector.  Only the slots that reach an unfilled rank with nonzero
+// weight matter; this file finds that dependency closure once per plan (host,
+// backward sweep over the hanging leaves in traversal order), splits it into
+// independent runs of consecutive hanging leaves, and evaluates each run per
+// product with one thread walking it in order.  The leaf kernels then read
+// the run results in place of the unrefilled slots.
+#include <array>
+#include <cmath>
+#include <vector>
+#include "dkt_internal.cuh"
+
+namespace dkt {
+
+// Host analysis.  ip: [2][M][M] child interpolation (A[k*M+j]: parent k -> child j).
+void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s)
+{
+  pl.st_ready = false;
+  pl.stale_slots = 0;
+  pl.st_start = 0;
+  const int64_t H = pl.n_hang, NL = pl.n_leaf;
+  if (H == 0 || pl.conforming) return;
+  const int npe = pl.npe, M = pl.order + 1, dim = pl.dim, nc = 1 << dim;
+  std::vector<uint32_t> info(NL);
+  std::vector<int32_t> hidx(NL), p2n((size_t) npe * H);
+  std::vector<uint32_t> fill((size_t) 3 * H);
+  DKT_CUDA(cudaMemcpyAsync(info.data(), pl.info.p, NL * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  DKT_CUDA(cudaMemcpyAsync(hidx.data(), pl.hidx.p, NL * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  DKT_CUDA(cudaMemcpyAsync(p2n.data(), pl.p2n.p, (size_t) npe * H * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  DKT_CUDA(cudaMemcpyAsync(fill.data(), pl.fill.p, (size_t) 3 * H * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  DKT_CUDA(cudaStreamSynchronize(s));
+  std::vector<uint8_t> child(H);
+  for (int64_t i = 0; i < NL; i++)
+    if (hidx[i] >= 0) child[hidx[i]] = (uint8_t) ((info[i] >> 8) & 0xFFu);
+  // W[c][r][q]: weight of parent slot q on child rank r
+  std::vector<double> W((size_t) nc * npe * npe);
+  for (int c = 0; c < nc; c++)
+    for (int r = 0; r < npe; r++)
+      for (int q = 0; q < npe; q++) {
+        double w = 1.0;
+        int rr = r, qq = q;
+        for (int d = 0; d < dim; d++) {
+          const int rd = rr % M, qd = qq % M;
+          rr /= M;
+          qq /= M;
+          w *= ip[(size_t) ((c >> d) & 1) * M * M + qd * M + rd];
+        }
+        W[((size_t) c * npe + r) * npe + q] = w;
+      }
+  auto Wv = [&](int c, int r, int q) { return W[((size_t) c * npe + r) * npe + q]; };
+  auto filled = [&](int64_t h, int r) { return (fill[(size_t) h * 3 + (r >> 5)] >> (r & 31)) & 1u; };
+  auto stale = [&](int64_t h, int q) { return p2n[(size_t) h * npe + q] < 0; };
+  // need[g]: slots of S_g that later leaves read (bit set per slot)
+  std::vector<std::array<uint32_t, 3>> need(H, {0u, 0u, 0u});
+  std::vector<std::array<uint32_t, 3>> hazard(H, {0u, 0u, 0u});
+  int64_t n_hazard_slots = 0;
+  for (int64_t h = 0; h < H; h++) {
+    for (int q = 0; q < npe; q++) {
+      if (!stale(h, q)) continue;
+      bool hz = false;
+      for (int r = 0; r < npe && !hz; r++)
+        if (!filled(h, r) && Wv(child[h], r, q) != 0.0) hz = true;
+      if (hz) {
+        hazard[h][q >> 5] |= 1u << (q & 31);
+        n_hazard_slots++;
+        if (h > 0) need[h - 1][q >> 5] |= 1u << (q & 31);
+        else pl.st_start++;
+      }
+    }
+  }
+  pl.stale_slots = n_hazard_slots;
+  if (n_hazard_slots == 0) return;
+  // backward closure: an entry (g, q) needs (g-1, q') for stale q' with weight
+  for (int64_t g = H - 1; g >= 0; g--) {
+    for (int q = 0; q < npe; q++) {
+      if (!((need[g][q >> 5] >> (q & 31)) & 1u)) continue;
+      for (int q2 = 0; q2 < npe; q2++) {
+        if (!stale(g, q2) || Wv(child[g], q, q2) == 0.0) continue;
+        if (g > 0) need[g - 1][q2 >> 5] |= 1u << (q2 & 31);
+        else pl.st_start++;
+      }
+    }
+  }
+  // Entries in increasing g, grouped by g; groups of consecutive g form runs
+  // (independent of each other).  Terms are split into fresh ones (a node's
+  // input value) and stale ones (an entry of the previous group).
+  std::vector<int32_t> ent_base(H, -1);
+  std::vector<int32_t> frow(1, 0), fidx, srow(1, 0), sidx;
+  std::vector<double> fw, sw;
+  std::vector<int32_t> gstart;     // entry offset of every group, plus the end
+  std::vector<int32_t> runs;       // pairs [first group, end group)
+  int32_t n_ent = 0;
+  int64_t prev_g = -2;
+  for (int64_t g = 0; g < H; g++) {
+    const bool any = need[g][0] | need[g][1] | need[g][2];
+    if (!any) continue;
+    if (g != prev_g + 1) {
+      if (!runs.empty()) runs.push_back((int32_t) gstart.size());
+      runs.push_back((int32_t) gstart.size());
+    }
+    prev_g = g;
+    gstart.push_back(n_ent);
+    ent_base[g] = n_ent;
+    for (int q = 0; q < npe; q++) {
+      if (!((need[g][q >> 5] >> (q & 31)) & 1u)) continue;
+      n_ent++;
+      for (int q2 = 0; q2 < npe; q2++) {
+        const double w = Wv(child[g], q, q2);
+        if (w == 0.0) continue;
+        if (!stale(g, q2)) {
+          fidx.push_back(p2n[(size_t) g * npe + q2]);
+          fw.push_back(w);
+        } else if (g > 0 && ent_base[g - 1] >= 0) {
+          int32_t id = ent_base[g - 1];
+          for (int k = 0; k < q2; k++) id += (need[g - 1][k >> 5] >> (k & 31)) & 1u;
+          sidx.push_back(id);
+          sw.push_back(w);
+        }
+        // g == 0: the slot holds the buffer's initial contents (zero)
+      }
+      frow.push_back((int32_t) fidx.size());
+      srow.push_back((int32_t) sidx.size());
+    }
+  }
+  if (!runs.empty()) runs.push_back((int32_t) gstart.size());
+  gstart.push_back(n_ent);
+  // per hazard leaf: entry id of (h-1, q) for each slot it reads stale
+  std::vector<int32_t> hz_off(H, -1), hz_tab;
+  for (int64_t h = 0; h < H; h++) {
+    if (!(hazard[h][0] | hazard[h][1] | hazard[h][2]) || h == 0) continue;
+    hz_off[h] = (int32_t) (hz_tab.size() / npe);
+    for (int q = 0; q < npe; q++) {
+      int32_t id = -1;
+      if (stale(h, q) && ((need[h - 1][q >> 5] >> (q & 31)) & 1u)) {
+        id = ent_base[h - 1];
+        for (int k = 0; k < q; k++) id += (need[h - 1][k >> 5] >> (k & 31)) & 1u;
+      }
+      hz_tab.push_back(id);
+    }
+  }
+  pl.st_n_ent = n_ent;
+  pl.st_n_runs = (int64_t) runs.size() / 2;
+  // keep every upload non-empty
+  if (fidx.empty()) { fidx.push_back(0); fw.push_back(0.0); }
+  if (sidx.empty()) { sidx.push_back(0); sw.push_back(0.0); }
+  if (runs.empty()) runs.push_back(0);
+  if (hz_tab.empty()) hz_tab.push_back(-1);
+  pl.st_row.upload(frow.data(), frow.size(), s);
+  pl.st_idx.upload(fidx.data(), fidx.size(), s);
+  pl.st_w.upload(fw.data(), fw.size(), s);
+  pl.st_srow.upload(srow.data(), srow.size(), s);
+  pl.st_sidx.upload(sidx.data(), sidx.size(), s);
+  pl.st_sw.upload(sw.data(), sw.size(), s);
+  pl.st_gstart.upload(gstart.data(), gstart.size(), s);
+  pl.st_runs.upload(runs.data(), runs.size(), s);
+  pl.st_f.alloc(std::max<int64_t>(n_ent, 1));
+  pl.st_hzoff.upload(hz_off.data(), hz_off.size(), s);
+  pl.st_hztab.upload(hz_tab.data(), hz_tab.size(), s);
+  pl.st_v.alloc(std::max<int64_t>(n_ent, 1));
+  pl.st_vq.alloc(std::max<int64_t>(n_ent, 1));
+  DKT_CUDA(cudaStreamSynchronize(s));
+  pl.st_ready = true;
+}
+
+// Fresh part of every entry: independent, one thread each.
+template <bool FIXED>
+__global__ void k_stale_fresh(int64_t n_ent, const int32_t *__restrict__ row, const int32_t *__restrict__ idx,
+                              const double *__restrict__ w, const double *__restrict__ x,
+                              const long long *__restrict__ xq, double *__restrict__ f)
+{
+  const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_ent) return;
+  double acc = 0.0;
+  for (int32_t k = row[e]; k < row[e + 1]; k++) {
+    const int32_t j = idx[k];
+    acc += w[k] * (FIXED ? (double) xq[j] : x[j]);
+  }
+  f[e] = acc;
+}
+
+// The chained part: one warp per run walks its groups in order; lanes split
+// the entries of a group.  Values of the previous group were written by the
+// same warp before the __syncwarp.
+template <bool FIXED>
+__global__ void k_stale_chain(const int32_t *__restrict__ runs, int64_t n_runs, const int32_t *__restrict__ gstart,
+                              const int32_t *__restrict__ srow, const int32_t *__restrict__ sidx,
+                              const double *__restrict__ sw, const double *__restrict__ f, double *__restrict__ v,
+                              long long *__restrict__ vq)
+{
+  const int64_t wid = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= n_runs) return;
+  for (int32_t grp = runs[2 * wid]; grp < runs[2 * wid + 1]; grp++) {
+    for (int32_t e = gstart[grp] + lane; e < gstart[grp + 1]; e += 32) {
+      double acc = f[e];
+      for (int32_t k = srow[e]; k < srow[e + 1]; k++) acc += sw[k] * __ldcg(v + sidx[k]);
+      __stcg(v + e, acc);
+      if (FIXED) vq[e] = __double2ll_rn(acc);
+    }
+    __syncwarp();
+    __threadfence_block();
+  }
+}
+
+void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
+{
+  if (!pl.st_ready || pl.st_n_runs == 0) return;
+  const int64_t ne = pl.st_n_ent;
+  if (xq) {
+    k_stale_fresh<true><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, nullptr, xq,
+                                                           pl.st_f.p);
+    k_stale_chain<true><<<grid_for(pl.st_n_runs * 32, 128), 128, 0, s>>>(
+        pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p, pl.st_sw.p, pl.st_f.p, pl.st_v.p,
+        pl.st_vq.p);
+  } else {
+    k_stale_fresh<false><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, x, nullptr,
+                                                            pl.st_f.p);
+    k_stale_chain<false><<<grid_for(pl.st_n_runs * 32, 128), 128, 0, s>>>(
+        pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p, pl.st_sw.p, pl.st_f.p, pl.st_v.p,
+        nullptr);
+  }
+  check_launch("stale_eval");
+}
+
+}  // namespace dkt

@@ -46,6 +46,11 @@ extern "C" {
 #define DKT_OP_HEAT 1
 #define DKT_OP_LAPMASS 2
 #define DKT_OP_CUSTOM 3
+/* Laplacian alone (J^(d-2) K_ref, Dirichlet zeroing as HeatMat) and mass
+ * alone (J^d M_ref, no boundary step: the right-hand side b = M f of the
+ * Poisson problems, the role of feVector::computeVec, FEM/include/feVector.h:122-168). */
+#define DKT_OP_LAPLACE 4
+#define DKT_OP_MASS 5
 
 typedef struct dkt_da_s *dkt_da;
 typedef struct dkt_plan_s *dkt_plan;
@@ -82,6 +87,15 @@ void dkt_da_destroy(dkt_da da);
  * column = input rank; rank = lexicographic element node index, x fastest).
  */
 int dkt_plan_create(dkt_da da, int op, const double *op_tables, dkt_plan *out);
+/* Traversal variants.  REFERENCE reproduces fem::matvec exactly, including
+ * its parent-buffer reads (matvec.h:411-456) and its transpose mask
+ * (matvec.h:497-521), which make the operator non-symmetric.  CONFORMING
+ * takes the parent values from every node on the parent lattice and adds the
+ * transpose to all of them: the symmetric P^T K P, for Krylov solvers (no
+ * counterpart in the reference). */
+#define DKT_TRAVERSAL_REFERENCE 0
+#define DKT_TRAVERSAL_CONFORMING 1
+int dkt_plan_create_ex(dkt_da da, int op, const double *op_tables, int traversal, dkt_plan *out);
 /* Same, from a bare node list (the `coords, sz` arguments of fem::matvec). */
 int dkt_plan_create_from_nodes(int dim, int order, int curve, int max_depth, const uint32_t *node_coords,
                                const uint8_t *node_levels, int64_t sz, int op, const double *op_tables,
@@ -94,10 +108,10 @@ int64_t dkt_plan_num_nodes(dkt_plan plan);
 int dkt_plan_stats(dkt_plan plan, int64_t *out4);
 
 /* Host copy of the flattened traversal (for inspection and tests):
- * e2n [nPe][leaves] node of each lexicographic rank or -1; info [leaves]
+ * e2n [leaves][nPe] node of each lexicographic rank or -1; info [leaves]
  * level | child<<8 | hanging<<16; hidx [leaves] hanging record or -1;
- * p2n [nPe][hanging] parent node of level L-1 per rank or -1; fill
- * [3][hanging] filled-rank bit masks.  Any pointer may be NULL. */
+ * p2n [hanging][nPe] parent node of level L-1 per rank or -1; fill
+ * [hanging][3] filled-rank bit masks.  Any pointer may be NULL. */
 int dkt_plan_export(dkt_plan plan, int32_t *e2n, uint32_t *info, int32_t *hidx, int32_t *p2n, uint32_t *fill);
 
 /* fem::matvec on device arrays: y = sum over leaves of the elemental products

@@ -32,6 +32,11 @@ int dkt_mesh_tree_from_points(const uint32_t *pts, int64_t n, int dim, int max_d
 int dkt_mesh_moving_ball(int max_depth, int level, double radius, double halfwidth, const double *c0,
                          const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels);
 
+/* Same mesh, built on the current device (refinement frontier level by level,
+ * balancing by sorted cell-key sets); cells returned sorted by level. */
+int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double halfwidth, const double *c0,
+                                const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels);
+
 void dkt_free(void *p);
 
 #ifdef __cplusplus

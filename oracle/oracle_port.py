@@ -54,6 +54,7 @@ def lib():
         L.dkto_fematrix_matvec.argtypes = [P, P, P]
         L.dkto_last_stats.argtypes = [P, P]
         L.dkto_set_stale_mode.argtypes = [ctypes.c_int]
+        L.dkto_set_conforming.argtypes = [ctypes.c_int]
         L.dkto_cg.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_double, P, P]
         _lib = L
     return _lib
@@ -83,6 +84,12 @@ def set_stale_mode(mode):
     """0: parent-buffer slots keep earlier leaves' values (the reference's
     static buffer); 1: unfilled slots read as zero."""
     _check(lib().dkto_set_stale_mode(int(mode)))
+
+
+def set_conforming(on):
+    """0: the reference's traversal; 1: its conforming variant (parent values
+    from every node on the parent lattice, unmasked transpose: P^T K P)."""
+    _check(lib().dkto_set_conforming(int(on)))
 
 
 def tree_balance(points, dim, max_pts=1):

@@ -657,7 +657,9 @@ void ele_op(int op, unsigned dim, const RefEl &re, const double *in, double *out
     for (unsigned d = 0; d < dim; d++) { apply_axis(dim, M, (int) d == term ? re.D.data() : re.Q.data(), false, a.data(), b.data(), d); std::swap(a, b); }
     for (unsigned idx = 0; idx < n; idx++) a[idx] *= wq[idx];
     for (unsigned d = 0; d < dim; d++) { apply_axis(dim, M, (int) d == term ? re.D.data() : re.Q.data(), true, a.data(), b.data(), d); std::swap(a, b); }
-    const double f = term < 0 ? Jd : Jdm2;
+    double f = term < 0 ? Jd : Jdm2;
+    if (op == 4 && term < 0) f = 0.0;   // Laplacian only
+    if (op == 5 && term >= 0) f = 0.0;  // mass only
     for (unsigned idx = 0; idx < n; idx++) acc[idx] += f * a[idx];
   }
   for (unsigned i = 0; i < n; i++) out[i] = scale * acc[i];
@@ -674,6 +676,22 @@ struct MatvecStats {
 // 0: parent-buffer slots keep earlier leaves' values, as the reference's
 // function-static buffer does; 1: unfilled slots read as zero.
 int g_stale_mode = 0;
+// Conforming variant (not the reference's behaviour): the parent values are
+// taken from every node on the parent's lattice whatever its level, and the
+// transpose adds to every such parent node, which makes the operator the
+// symmetric P^T K P.  Used as the oracle of the conforming device mode.
+int g_conforming = 0;
+
+template <int dim>
+inline bool on_lattice(const TN<dim> &pt, const TN<dim> &host, unsigned p)
+{
+  const uint64_t len = cell_len(host.lev);
+  for (int d = 0; d < dim; d++) {
+    const uint64_t off = (uint64_t) pt.x[d] - host.x[d];
+    if ((off * p) % len) return false;
+  }
+  return true;
+}
 
 template <int dim>
 struct Traversal {
@@ -789,7 +807,7 @@ struct Traversal {
       std::fill(parentFill.begin(), parentFill.end(), 0);
       if (g_stale_mode == 1) std::fill(parentBuf.begin(), parentBuf.end(), 0.0);
       for (size_t i = 0; i < pSz; i++) {
-        if (pCoords[i].lev != pLev - 1) continue;
+        if (g_conforming ? !on_lattice(pCoords[i], par, p) : pCoords[i].lev != pLev - 1) continue;
         unsigned r = lex_node_rank(pCoords[i], par, p);
         parentFill[r] = 1;
         parentBuf[r] = pVin[i];
@@ -821,9 +839,9 @@ struct Traversal {
       ikd_interp(dim, *re, leafOut.data(), leafOut.data(), morton_index(root, root.lev), true);
       TN<dim> par = get_parent(root);
       for (size_t i = 0; i < pSz; i++) {
-        if (pCoords[i].lev != pLev - 1) continue;
+        if (g_conforming ? !on_lattice(pCoords[i], par, p) : pCoords[i].lev != pLev - 1) continue;
         unsigned r = lex_node_rank(pCoords[i], par, p);
-        if (!leafFill[r]) pVout[i] += leafOut[r];
+        if (g_conforming || !leafFill[r]) pVout[i] += leafOut[r];
       }
     }
   }
@@ -1023,9 +1041,10 @@ int dkto_fematrix_matvec(void *hp, const double *x, double *y)
   OracleDA *h = (OracleDA *) hp;
   const size_t n = h->nodeL.size();
   std::vector<double> xin(x, x + n);
-  if (h->op != 0) for (uint32_t b : h->bdry) xin[b] = 0.0;
+  const bool bc = (h->op == 1 || h->op == 2 || h->op == 4);
+  if (bc) for (uint32_t b : h->bdry) xin[b] = 0.0;
   dkto_matvec_raw(hp, xin.data(), y);
-  if (h->op != 0) for (uint32_t b : h->bdry) y[b] = 0.0;
+  if (bc) for (uint32_t b : h->bdry) y[b] = 0.0;
   return 0;
 }
 
@@ -1041,6 +1060,9 @@ int dkto_last_stats(void *hp, int64_t *out6)
 
 // Select how unfilled parent-buffer slots are read (see g_stale_mode).
 int dkto_set_stale_mode(int mode) { g_stale_mode = mode; return 0; }
+
+// Select the reference traversal (0) or its conforming variant (1).
+int dkto_set_conforming(int on) { g_conforming = on; return 0; }
 
 // Unpreconditioned or Jacobi-preconditioned CG in the form of
 // HeatMat::cgSolve (FEM/examples/src/heatMat.cpp:164-325), stopping on

@@ -119,6 +119,37 @@ def test_moving_ball_4d_vs_oracle(dkt, order):
     assert A.stats()["leaves"] == ora.stats()["leaves"]
 
 
+def test_device_moving_ball_equals_host(dkt):
+    for level in (3, 5):
+        hc, hl = dkt.moving_ball_tree(max_depth=8, level=level)
+        dc, dl = dkt.moving_ball_tree(max_depth=8, level=level, device=True)
+        key = lambda c, l: sorted(map(tuple, np.concatenate([c.astype(np.int64), l[:, None].astype(np.int64)], 1)))
+        assert len(hl) == len(dl) and key(hc, hl) == key(dc, dl)
+
+
+def test_moving_ball_static_buffer_emulation(dkt):
+    """Level-5 moving ball: the reference reads its static parent buffer in
+    slots it did not refill (4,680 slot reads per product).  The device path
+    reproduces those values; compared with the oracle port, which keeps the
+    buffer exactly as the reference does, on a first and a second product."""
+    md, level = 10, 5
+    tc, tl = dkt.moving_ball_tree(max_depth=md, level=level)
+    da = dkt.DA(tc, tl, 4, order=1, max_depth=md)
+    orc.set_curve(4, md)
+    orc.set_stale_mode(0)
+    sc, sl = da.tree()
+    ora = orc.DA(sc, sl, 4, 1, 2)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    assert A.stats()["stale_slots"] > 0
+    for seed in (2, 3):
+        x = dkt.uniform_pm1(seed, da.n)
+        yr = ora.matvec(x)
+        assert ora.stats()["stale_reads"] == A.stats()["stale_slots"]
+        for mode in (dkt.ARITH_FP64, dkt.ARITH_AUTO):
+            A.set_arithmetic(mode)
+            assert _rel(_gpu_mv(A, x), yr) <= TOL, (seed, mode)
+
+
 @pytest.mark.parametrize("dim,L", [(2, 4), (3, 3), (4, 2)])
 def test_identity_uniform_known_answer(dkt, dim, L):
     """all-ones input, identity eleOp, uniform grid: 2^k at each node
@@ -219,3 +250,52 @@ def test_cg_solves_lapmass(dkt):
     it, rr = A.cg(bd, xd, max_iter=5000, tol=1e-10, jacobi=True)
     r = b - _gpu_mv(A, xd.cpu().numpy())
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-10, (it, rr)
+
+
+@pytest.mark.parametrize("op", ["OP_LAPLACE", "OP_MASS"])
+def test_laplace_and_mass_operators_vs_oracle(dkt, op):
+    dim, md = 3, 9
+    pts = dkt.gaussian_points(3000, dim, md, seed=4)
+    tc, tl = dkt.tree_from_points(pts, dim, md)
+    da = dkt.DA(tc, tl, dim, order=1, max_depth=md)
+    orc.set_curve(dim, md)
+    sc, sl = da.tree()
+    ora = orc.DA(sc, sl, dim, 1, getattr(dkt, op))
+    A = dkt.Matrix(da, op=getattr(dkt, op))
+    x = dkt.uniform_pm1(6, da.n)
+    yr = ora.matvec(x)
+    for mode in (dkt.ARITH_FP64, dkt.ARITH_AUTO):
+        A.set_arithmetic(mode)
+        assert _rel(_gpu_mv(A, x), yr) <= TOL, mode
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_conforming_traversal_vs_oracle(dkt, order):
+    """Conforming traversal (parent nodes of any level on the parent lattice,
+    unmasked transpose, parent slots with no node read as zero) on the
+    level-5 moving ball: equal to the oracle run in the same mode, and
+    symmetric."""
+    md, level = 10, 5 if order == 1 else 4
+    tc, tl = dkt.moving_ball_tree(max_depth=md, level=level)
+    da = dkt.DA(tc, tl, 4, order=order, max_depth=md)
+    orc.set_curve(4, md)
+    orc.set_conforming(1)
+    orc.set_stale_mode(1)
+    try:
+        sc, sl = da.tree()
+        ora = orc.DA(sc, sl, 4, order, 2)
+        A = dkt.Matrix(da, op=dkt.OP_LAPMASS, traversal=dkt.TRAVERSAL_CONFORMING)
+        x = dkt.uniform_pm1(7, da.n)
+        z = dkt.uniform_pm1(8, da.n)
+        yr = ora.matvec_raw(x)
+        assert A.stats()["stale_slots"] == 0
+        modes = (dkt.ARITH_FP64, dkt.ARITH_AUTO) if order == 1 else (dkt.ARITH_FP64,)
+        for mode in modes:
+            A.set_arithmetic(mode)
+            y = _gpu_mv(A, x, raw=True)
+            assert _rel(y, yr) <= TOL, mode
+            az = _gpu_mv(A, z, raw=True)
+            assert abs(z @ y - x @ az) <= 1e-12 * np.linalg.norm(y) * np.linalg.norm(z)
+    finally:
+        orc.set_conforming(0)
+        orc.set_stale_mode(0)
