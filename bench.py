@@ -37,13 +37,15 @@ MD = 10
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--level", type=int, default=7)
+    ap.add_argument("--level", type=int, default=8)
     ap.add_argument("--order", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--solve-level", type=int, default=7,
+                    help="moving-ball level of the Poisson solves (FP64 vs mixed PCG); 0 skips them")
     return ap.parse_args()
 
 
@@ -103,6 +105,19 @@ class Clocks:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def traffic(kernel, leaf_visits):
+    """DRAM bytes (read + write) of one launch of `kernel`, from the committed
+    ncu summary of that kernel: the summary's per-leaf-visit traffic of its
+    captured launch times this workload's leaf visits, or None without one."""
+    import glob
+    import re
+    for f in sorted(glob.glob(os.path.join(REPO, "profiles", kernel + "_*.md"))):
+        m = re.search(r"dram_bytes_per_leaf_visit:\s*([0-9.eE+]+)", open(f).read())
+        if m:
+            return float(m.group(1)) * leaf_visits
+    return None
 
 
 def algorithmic_bytes(stats, n_nodes, npe):
@@ -182,6 +197,45 @@ def run_reference(a, rank, world):
     print(json.dumps(out), flush=True)
 
 
+def run_solves(a, dkt, dev):
+    """4D Q1 Poisson -Laplace(u) = f on the moving-ball mesh (conforming
+    traversal, homogeneous Dirichlet), f = prod sin(pi x_d) + N(0, 0.1^2)
+    noise (seed 3), b = M f: plain FP64 Jacobi-PCG against mixed-precision
+    refinement, both to ||b - A x||_2 <= 1e-10 ||b||_2 (FP64 residual)."""
+    import torch
+    tc, tl = moving_ball(dkt, a.solve_level, device=True)
+    da = dkt.DA(tc, tl, 4, order=1, max_depth=MD)
+    A = dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
+    M = dkt.Matrix(da, op=dkt.OP_MASS, traversal=dkt.TRAVERSAL_CONFORMING)
+    f = torch.from_numpy(dkt.sine_load(da, noise_sd=0.1, seed=3)).to(dev)
+    b = torch.empty_like(f)
+    M.matvec(f, b)
+    b[torch.from_numpy(da.boundary_ids().astype(np.int64)).to(dev)] = 0.0
+    nb = float(torch.linalg.norm(b))
+    out = {"workload": "4D Q1 Poisson, moving-ball level %d (%d elements, %d nodes), conforming traversal, "
+                       "Jacobi-PCG to 1e-10 relative 2-norm residual" % (a.solve_level, da.n_elem, da.n)}
+    stream = torch.cuda.current_stream(dev)
+    for name, prec in (("fp64", dkt.PREC_FP64), ("mixed", dkt.PREC_MIXED)):
+        x = torch.zeros_like(b)
+        A.pcg(b, x, precision=prec, tol=1e-10, max_iter=64)      # warm-up: graphs, buffers
+        x.zero_()
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        it, ref, rr, ok = A.pcg(b, x, precision=prec, tol=1e-10)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        ax = torch.empty_like(b)
+        A.matvec(x, ax)
+        true_rel = float(torch.linalg.norm(b - ax)) / nb
+        out[name] = {"solves_per_s": 1e3 / ms, "ms": ms, "iterations": it, "refinements": ref,
+                     "relres": rr, "true_relres": true_rel, "converged": bool(ok)}
+    out["mixed_over_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    return out
+
+
 def run_gpu(a, rank, world, local_rank):
     import torch
     import __graft_entry__ as ge
@@ -214,6 +268,7 @@ def run_gpu(a, rank, world, local_rank):
     barrier()
     torch.cuda.synchronize(dev)
     A.kernel_timing(True)
+    launches0 = A.launch_count()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with Clocks(local_rank) as clk:
@@ -225,6 +280,7 @@ def run_gpu(a, rank, world, local_rank):
     barrier()
     ms = ev0.elapsed_time(ev1)
     k_ms, k_launches = A.kernel_timing(False)
+    launches = A.launch_count() - launches0
     t_max = ms
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -249,26 +305,31 @@ def run_gpu(a, rank, world, local_rank):
     if rank != 0:
         return
     peak, peak_kind = peaks()
+    fixed = a.order == 1
+    kname = "k_matvec_q1fx" if fixed else "k_matvec_leaf"
+    dtype = "i64 (exact fixed point, f64 in/out)" if fixed else "f64"
     B = algorithmic_bytes(st, n, npe)
     k_avg_s = (k_ms / max(k_launches, 1)) / 1e3
     achieved = B / k_avg_s / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": t_max / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": dtype, "data": "synthetic",
         "config": {"workload": "moving-ball spacetime matvec, dim 4, Q%d Laplacian+mass, FP64, level %d, "
                                "max_depth %d" % (a.order, a.level, MD),
                    "elements": ne, "nodes": n, "leaf_visits": st["leaves"], "hanging_leaves": st["hanging_leaves"],
                    "stale_slots": st["stale_slots"], "parallelism": "replicas x%d" % world,
                    "l2": "inputs larger than L2: %.2f GB of maps and vectors read per step" % (B / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_matvec_leaf",
+                     "traffic": traffic(kname, st["leaves"]), "peak_kind": peak_kind, "kernel": kname,
                      "kernel_ms": k_ms / max(k_launches, 1), "algorithmic_bytes": B},
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
-        "gpu_launches": 3 * a.steps,
+        "gpu_launches": launches,
         "clocks": clk.summary(),
         "setup_s": {"mesh": t_mesh, "da": t_da, "plan": t_plan},
     }
+    if a.solve_level > 0:
+        out["solve"] = run_solves(a, dkt, dev)
     if world == 1 and not a.no_cpu_baseline:
         sample_level = min(a.level, 5)
         r, sne, calls, used = cpu_baseline(sample_level, a.order, 1, 3, a.cpu_seconds, procs=1)

@@ -19,6 +19,7 @@ CURVE_MORTON, CURVE_HILBERT = 0, 1
 OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM, OP_LAPLACE, OP_MASS = 0, 1, 2, 3, 4, 5
 ARITH_AUTO, ARITH_FP64, ARITH_FIXED = 0, 1, 2
 TRAVERSAL_REFERENCE, TRAVERSAL_CONFORMING = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
 
 
 class DktError(RuntimeError):
@@ -69,7 +70,16 @@ def load(build_if_missing=True):
         "dkt_fematrix_matvec_noalloc": ([P, P, P, ctypes.c_double, P], I),
         "dkt_diagonal": ([P, P, P], I),
         "dkt_cg_solve": ([P, P, P, I, ctypes.c_double, I, P, P, P], I),
+        "dkt_pcg_solve": ([P, P, P, I, I, ctypes.c_double, I, P, P, P, P], I),
+        "dkt_matvec_f32": ([P, P, P, P], I),
         "dkt_plan_kernel_timing": ([P, I, P, P], I),
+        "dkt_plan_launch_count": ([P, P], I),
+        "dkt_plan_set_tile": ([P, I], I),
+        "dkt_batch_create": ([P, I, P], I),
+        "dkt_plan_num_meshes": ([P, P], I),
+        "dkt_plan_mesh_offsets": ([P, P], I),
+        "dkt_plan_autotune": ([P, P, P], I),
+        "dkt_plan_stats_ex": ([P, P, I], I),
         "dkt_plan_set_arithmetic": ([P, I], I),
         "dkt_plan_destroy": ([P], None),
         "dkt_mesh_gaussian_points": ([I64, I, I, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, P], I),
@@ -77,6 +87,14 @@ def load(build_if_missing=True):
         "dkt_mesh_moving_ball": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
         "dkt_free": ([P], None),
         "dkt_mesh_moving_ball_device": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
+        "dkt_mesh_sphere_shell_device": ([I, I, I, ctypes.c_double, ctypes.c_double, P, P, P, P], I),
+        "dkt_mesh_sphere_shell": ([I, I, I, ctypes.c_double, ctypes.c_double, P, P, P, P], I),
+        "dkt_server_create": ([I, ctypes.c_double, I, ctypes.c_double, P], I),
+        "dkt_server_submit": ([P, I, I, P, P, I64, ctypes.c_uint64, P], I),
+        "dkt_server_wait": ([P, I64, P], I),
+        "dkt_server_solution": ([P, I64, P, I64], I),
+        "dkt_server_release": ([P, I64], I),
+        "dkt_server_destroy": ([P], None),
         "dkt_probe_device": ([P], I),
     }
     for name, (args, res) in sig.items():
@@ -176,10 +194,25 @@ class Matrix:
         self.order = da.order if da is not None else order
         self.npe = (self.order + 1) ** self.dim
 
+    @classmethod
+    def batch(cls, mats):
+        """One block-diagonal plan over several matrices (same dim, order,
+        max_depth, operator, traversal, tile size); vectors are concatenated."""
+        L = load()
+        arr = (ctypes.c_void_p * len(mats))(*[m._h.value for m in mats])
+        h = ctypes.c_void_p()
+        _check(L.dkt_batch_create(arr, len(mats), ctypes.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        self.n = int(L.dkt_plan_num_nodes(h))
+        self.dim, self.order, self.npe = mats[0].dim, mats[0].order, mats[0].npe
+        return self
+
     def stats(self):
-        s = np.zeros(4, np.int64)
-        _check(load().dkt_plan_stats(self._h, _p(s)))
-        return dict(zip(["leaves", "hanging_leaves", "stale_slots", "boundary_nodes"], s.tolist()))
+        s = np.zeros(8, np.int64)
+        _check(load().dkt_plan_stats_ex(self._h, _p(s), 8))
+        return dict(zip(["leaves", "hanging_leaves", "stale_slots", "boundary_nodes", "stale_entries",
+                         "stale_runs", "stale_longest_run", "stale_longest_run_entries"], s.tolist()))
 
     def export(self):
         """The flattened traversal as numpy arrays (e2n, info, hidx, p2n, fill)."""
@@ -216,6 +249,16 @@ class Matrix:
         """ARITH_AUTO (fixed point where it applies), ARITH_FP64 or ARITH_FIXED."""
         _check(load().dkt_plan_set_arithmetic(self._h, mode))
 
+    def set_tile(self, tile_leaves):
+        """Leaves per tile of the Q1 kernels (0: untiled kernel)."""
+        _check(load().dkt_plan_set_tile(self._h, int(tile_leaves)))
+
+    def launch_count(self):
+        """Kernels launched so far by this matrix's products and solves."""
+        n = ctypes.c_int64()
+        _check(load().dkt_plan_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
     def kernel_timing(self, enable):
         """Close the current timing window; returns (total kernel ms, launches)."""
         ms = ctypes.c_double(0.0)
@@ -234,6 +277,41 @@ class Matrix:
         if rc not in (OK, E_NOCONV):
             _check(rc)
         return it.value, rr.value
+
+    def pcg(self, b_dev, x_dev, precision=0, max_iter=100000, tol=1e-10, jacobi=True, stream=None):
+        """Device-resident Jacobi-PCG (precision PREC_FP64) or mixed-precision
+        refinement (PREC_MIXED).  Returns (iterations, refinements, relres,
+        converged); for a batch the first three are per-mesh arrays."""
+        m = self.num_meshes()
+        it, ref, rr = np.zeros(m, np.int32), np.zeros(m, np.int32), np.zeros(m)
+        rc = load().dkt_pcg_solve(self._h, _p(b_dev), _p(x_dev), int(precision), int(max_iter), float(tol),
+                                  int(bool(jacobi)), _p(it), _p(ref), _p(rr), _stream(stream))
+        if rc not in (OK, E_NOCONV):
+            _check(rc)
+        if m == 1:
+            return int(it[0]), int(ref[0]), float(rr[0]), rc == OK
+        return it, ref, rr, rc == OK
+
+    def num_meshes(self):
+        n = ctypes.c_int(0)
+        _check(load().dkt_plan_num_meshes(self._h, ctypes.byref(n)))
+        return n.value
+
+    def mesh_offsets(self):
+        m = self.num_meshes()
+        o = np.zeros(m + 1, np.int64)
+        _check(load().dkt_plan_mesh_offsets(self._h, _p(o)))
+        return o
+
+    def autotune(self):
+        """Keeps the fastest tile size; returns (tile, ms per product)."""
+        t, ms = ctypes.c_int(0), ctypes.c_double(0.0)
+        _check(load().dkt_plan_autotune(self._h, ctypes.byref(t), ctypes.byref(ms)))
+        return t.value, ms.value
+
+    def matvec_f32(self, x_dev, y_dev, stream=None):
+        """Binary32 feMatrix product (Q1 built-in operators)."""
+        _check(load().dkt_matvec_f32(self._h, _p(x_dev), _p(y_dev), _stream(stream)))
 
     def __del__(self):
         try:
@@ -276,6 +354,19 @@ def tree_from_points(points, dim, max_depth, max_pts=1):
     return _take_cells(n, c, lv, dim)
 
 
+def sphere_shell_tree(dim, max_depth, level, centre, radius, halfwidth=None, device=True):
+    """2:1-balanced tree refined to `level` on a sphere shell (device=True
+    builds it on the GPU, False on the host; the trees are equal)."""
+    if halfwidth is None:
+        halfwidth = 2.0 ** -level
+    c = np.ascontiguousarray(centre, dtype=np.float64)
+    n, cp, lv = ctypes.c_int64(0), ctypes.c_void_p(), ctypes.c_void_p()
+    fn = load().dkt_mesh_sphere_shell_device if device else load().dkt_mesh_sphere_shell
+    _check(fn(dim, max_depth, level, float(radius), float(halfwidth), _p(c),
+                                               ctypes.byref(n), ctypes.byref(cp), ctypes.byref(lv)))
+    return _take_cells(n, cp, lv, dim)
+
+
 def moving_ball_tree(max_depth, level, radius=0.2, halfwidth=None, c0=(0.3, 0.3, 0.3), c1=(0.7, 0.7, 0.7),
                      device=False):
     """Spacetime moving-ball tree (dim 4); device=True builds it on the GPU."""
@@ -288,6 +379,77 @@ def moving_ball_tree(max_depth, level, radius=0.2, halfwidth=None, c0=(0.3, 0.3,
     _check(fn(max_depth, level, radius, halfwidth, _p(a0), _p(a1), ctypes.byref(n), ctypes.byref(c),
               ctypes.byref(lv)))
     return _take_cells(n, c, lv, 4)
+
+
+class _SolveReport(ctypes.Structure):
+    _fields_ = [("rc", ctypes.c_int), ("dim", ctypes.c_int), ("n_elem", ctypes.c_int64), ("n_nodes", ctypes.c_int64),
+                ("iterations", ctypes.c_int), ("refinements", ctypes.c_int), ("relres", ctypes.c_double),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_start", ctypes.c_double),
+                ("t_done", ctypes.c_double), ("device_bytes", ctypes.c_int64), ("est_bytes", ctypes.c_double)]
+
+
+class Server:
+    """Request loop for Q1 Poisson solves (native worker threads, admission
+    against a device-memory budget, concurrent requests on separate streams)."""
+
+    def __init__(self, workers=4, budget_bytes=150e9, precision=PREC_MIXED, tol=1e-10):
+        h = ctypes.c_void_p()
+        _check(load().dkt_server_create(int(workers), float(budget_bytes), int(precision), float(tol),
+                                        ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, tree_coords, tree_levels, dim, max_depth, seed=0):
+        c = np.ascontiguousarray(tree_coords, dtype=np.uint32).reshape(-1, dim)
+        lv = np.ascontiguousarray(tree_levels, dtype=np.uint8)
+        t = ctypes.c_int64(0)
+        _check(load().dkt_server_submit(self._h, dim, max_depth, _p(c), _p(lv), lv.size, ctypes.c_uint64(seed),
+                                         ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket, solution=True):
+        rep = _SolveReport()
+        _check(load().dkt_server_wait(self._h, ctypes.c_int64(ticket), ctypes.byref(rep)))
+        out = {k: getattr(rep, k) for k, _ in _SolveReport._fields_}
+        if solution and rep.n_nodes > 0:
+            x = np.empty(rep.n_nodes)
+            _check(load().dkt_server_solution(self._h, ctypes.c_int64(ticket), _p(x), ctypes.c_int64(x.size)))
+            out["x"] = x
+        load().dkt_server_release(self._h, ctypes.c_int64(ticket))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().dkt_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cluster_points(n, dim, max_depth, seed, sd=0.05):
+    """n points around 1-4 Gaussian clusters (centres uniform in
+    [0.2, 0.8]^dim, standard deviation sd, numpy PCG64 stream of `seed`),
+    clipped to the unit cube, as integer coordinates at max_depth."""
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(1, 5))
+    centres = rng.uniform(0.2, 0.8, size=(k, dim))
+    which = rng.integers(0, k, size=n)
+    p = np.clip(centres[which] + rng.normal(0.0, sd, size=(n, dim)), 0.0, 1.0 - 2.0 ** -max_depth)
+    return np.floor(p * (1 << max_depth)).astype(np.uint32)
+
+
+def sine_load(da, noise_sd=0.1, seed=3):
+    """Nodal load f = prod_d sin(pi x_d) + N(0, noise_sd^2) noise (numpy
+    PCG64 stream of `seed`) at the DA's nodes, in DA node order."""
+    c, _ = da.nodes()
+    x = c.astype(np.float64) * (0.5 ** da.max_depth)
+    f = np.prod(np.sin(np.pi * x), axis=1)
+    if noise_sd:
+        f = f + np.random.default_rng(seed).normal(0.0, noise_sd, size=len(f))
+    return f
 
 
 def uniform_pm1(seed, n):

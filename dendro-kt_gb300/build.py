@@ -16,7 +16,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libdkt_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["dkt_da.cu", "dkt_plan.cu", "dkt_matvec.cu", "dkt_cg.cu", "dkt_capi.cu", "dkt_probe.cu", "dkt_q1fx.cu", "dkt_stale.cu", "dkt_tree.cu"]
+CU = ["dkt_da.cu", "dkt_plan.cu", "dkt_matvec.cu", "dkt_cg.cu", "dkt_capi.cu", "dkt_probe.cu", "dkt_q1fx.cu", "dkt_stale.cu", "dkt_tree.cu", "dkt_solve.cu", "dkt_tile.cu", "dkt_batch.cu", "dkt_serve.cu"]
 CPP = ["dkt_host.cpp"]
 
 
@@ -48,7 +48,10 @@ def up_to_date():
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
     if src.endswith(".cu"):
-        cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
+        # per-thread default streams: the work a host thread issues on stream 0
+        # does not serialise with other threads' (concurrent served requests)
+        cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--default-stream", "per-thread", "-Xcompiler",
+               "-fPIC", "-c", src, "-o", obj]
         if verbose_ptxas:
             cmd.insert(1, "-Xptxas=-v")
     else:

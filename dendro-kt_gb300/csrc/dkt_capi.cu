@@ -22,23 +22,28 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void diagonal(const Plan &pl, double *diag, cudaStream_t s);
 bool q1fx_setup(Plan &pl, cudaStream_t s);
+void tile_setup(Plan &pl, int T, cudaStream_t s);
+bool tile_size_supported(int dim, int T);
+inline int default_tile(int dim) { return dim == 4 ? 128 : 256; }
+void sphere_shell_device(int dim, int md, int level, double R, double w, const double *c, DBuf<uint64_t> &out,
+                         int64_t &n_out, cudaStream_t s);
 void moving_ball_device(int md, int level, double R, double w, const double *c0, const double *c1,
                         DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s);
 void unpack_cells_to_host(const DBuf<uint64_t> &keys, int64_t n, int dim, int md, uint32_t *coords, uint8_t *levels,
                           cudaStream_t s);
 void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s);
 std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
+int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter, double tol, bool jacobi,
+              int *iters, int *refinements, double *relres, cudaStream_t user);
+void q1f32_apply(Plan &pl, const float *x, float *y, bool bc_in, bool bc_out, cudaStream_t s);
+void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t s);
+void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,
              cudaStream_t s);
 
 }  // namespace dkt
 
-struct dkt_da_s {
-  dkt::DA da;
-};
-struct dkt_plan_s {
-  dkt::Plan pl;
-};
+#include "dkt_handles.cuh"
 
 namespace {
 thread_local std::string g_err;
@@ -202,7 +207,7 @@ static int plan_common(int dim, int order, int curve, int md, const uint32_t *no
     dkt::build_plan(pl, node_x_dev, node_lev_dev, n, cv, ip.data(), s);
     setup_operator(pl, op, tables, s);
     dkt::stale_setup(pl, ip, s);
-    dkt::q1fx_setup(pl, s);
+    if (dkt::q1fx_setup(pl, s)) dkt::tile_setup(pl, dkt::default_tile(dim), s);
     if (bdry_dev) {
       pl.bdry.alloc(nb > 0 ? nb : 1);
       if (nb > 0) DKT_CUDA(cudaMemcpyAsync(pl.bdry.p, bdry_dev, nb * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
@@ -269,6 +274,17 @@ int dkt_plan_stats(dkt_plan plan, int64_t *out4)
   out4[1] = plan->pl.n_hang;
   out4[2] = plan->pl.stale_slots;
   out4[3] = plan->pl.n_bdry;
+  return DKT_OK;
+}
+
+int dkt_plan_stats_ex(dkt_plan plan, int64_t *out, int n)
+{
+  if (!plan || !out || n < 0) return fail(DKT_E_ARG, "bad argument");
+  const dkt::Plan &pl = plan->pl;
+  const int64_t v[8] = {pl.n_leaf, pl.n_hang, pl.stale_slots, pl.n_bdry,
+                        pl.st_ready ? pl.st_n_ent : 0, pl.st_ready ? pl.st_n_runs : 0,
+                        pl.st_max_run_groups, pl.st_max_run_ents};
+  for (int k = 0; k < n && k < 8; k++) out[k] = v[k];
   return DKT_OK;
 }
 
@@ -351,6 +367,100 @@ int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter
   });
 }
 
+int dkt_batch_create(const dkt_plan *plans, int n, dkt_plan *out)
+{
+  if (!plans || n <= 0 || !out) return fail(DKT_E_ARG, "bad argument");
+  for (int k = 0; k < n; k++)
+    if (!plans[k]) return fail(DKT_E_ARG, "null plan");
+  dkt_plan_s *h = new dkt_plan_s();
+  const int rc = guarded([&]() {
+    std::vector<const dkt::Plan *> in;
+    for (int k = 0; k < n; k++) in.push_back(&plans[k]->pl);
+    dkt::batch_combine(in, h->pl, 0);
+    return DKT_OK;
+  });
+  if (rc != DKT_OK) { delete h; return rc; }
+  *out = h;
+  return DKT_OK;
+}
+
+int dkt_plan_num_meshes(dkt_plan plan, int *n)
+{
+  if (!plan || !n) return fail(DKT_E_ARG, "null argument");
+  *n = plan->pl.seg.size() >= 2 ? (int) plan->pl.seg.size() - 1 : 1;
+  return DKT_OK;
+}
+
+int dkt_plan_mesh_offsets(dkt_plan plan, int64_t *offsets)
+{
+  if (!plan || !offsets) return fail(DKT_E_ARG, "null argument");
+  if (plan->pl.seg.size() >= 2) std::copy(plan->pl.seg.begin(), plan->pl.seg.end(), offsets);
+  else { offsets[0] = 0; offsets[1] = plan->pl.n_nodes; }
+  return DKT_OK;
+}
+
+int dkt_plan_autotune(dkt_plan plan, int *best_tile, double *best_ms)
+{
+  if (!plan) return fail(DKT_E_ARG, "null argument");
+  if (!plan->pl.fx_ready) return fail(DKT_E_UNSUP, "tiles need a Q1 built-in operator");
+  return guarded([&]() {
+    dkt::Plan &pl = plan->pl;
+    const int cand[4] = {0, pl.dim == 4 ? 64 : 128, pl.dim == 4 ? 128 : 256, pl.dim == 4 ? 256 : 512};
+    dkt::DBuf<double> x(pl.n_nodes), y(pl.n_nodes);
+    DKT_CUDA(cudaMemset(x.p, 0, pl.n_nodes * sizeof(double)));
+    cudaEvent_t e0, e1;
+    DKT_CUDA(cudaEventCreate(&e0));
+    DKT_CUDA(cudaEventCreate(&e1));
+    int best = -1;
+    double bms = 1e300;
+    const bool saved = pl.timing;
+    pl.timing = false;
+    for (int T : cand) {
+      dkt::tile_setup(pl, T, 0);
+      dkt::fematrix_matvec(pl, x.p, y.p, 1.0, 0);
+      DKT_CUDA(cudaEventRecord(e0, 0));
+      for (int k = 0; k < 5; k++) dkt::fematrix_matvec(pl, x.p, y.p, 1.0, 0);
+      DKT_CUDA(cudaEventRecord(e1, 0));
+      DKT_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      DKT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms / 5 < bms) { bms = ms / 5; best = T; }
+    }
+    pl.timing = saved;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dkt::tile_setup(pl, best, 0);
+    if (best_tile) *best_tile = best;
+    if (best_ms) *best_ms = bms;
+    return DKT_OK;
+  });
+}
+
+int dkt_pcg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int precision, int max_iter, double tol,
+                  int jacobi, int *iters, int *refinements, double *relres, void *stream)
+{
+  if (!plan || !b_dev || !x_dev || max_iter < 0 || !(tol > 0) || precision < 0 || precision > 1)
+    return fail(DKT_E_ARG, "bad argument");
+  if (precision == 1 && !plan->pl.f32_ready)
+    return fail(DKT_E_UNSUP, "mixed precision needs a Q1 built-in operator without stale parent reads");
+  return guarded([&]() {
+    return dkt::pcg_solve(plan->pl, b_dev, x_dev, precision, max_iter, tol, jacobi != 0, iters, refinements,
+                          relres, (cudaStream_t) stream);
+  });
+}
+
+int dkt_matvec_f32(dkt_plan plan, const float *x_dev, float *y_dev, void *stream)
+{
+  if (!plan || !x_dev || !y_dev) return fail(DKT_E_ARG, "null argument");
+  if (!plan->pl.f32_ready)
+    return fail(DKT_E_UNSUP, "binary32 product needs a Q1 built-in operator without stale parent reads");
+  return guarded([&]() {
+    const bool bc = dkt::op_has_bc(plan->pl.op.kind);
+    dkt::q1f32_apply(plan->pl, x_dev, y_dev, bc, bc, (cudaStream_t) stream);
+    return DKT_OK;
+  });
+}
+
 int dkt_plan_set_arithmetic(dkt_plan plan, int mode)
 {
   if (!plan || mode < 0 || mode > 2) return fail(DKT_E_ARG, "bad argument");
@@ -379,6 +489,25 @@ int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t 
     pl.timing = enable != 0;
     return DKT_OK;
   });
+}
+
+int dkt_plan_set_tile(dkt_plan plan, int tile_leaves)
+{
+  if (!plan || tile_leaves < 0) return fail(DKT_E_ARG, "bad argument");
+  if (tile_leaves > 0 && !dkt::tile_size_supported(plan->pl.dim, tile_leaves))
+    return fail(DKT_E_ARG, "unsupported tile size");
+  if (tile_leaves > 0 && !plan->pl.fx_ready) return fail(DKT_E_UNSUP, "tiles need a Q1 built-in operator");
+  return guarded([&]() {
+    dkt::tile_setup(plan->pl, tile_leaves, 0);
+    return DKT_OK;
+  });
+}
+
+int dkt_plan_launch_count(dkt_plan plan, int64_t *count)
+{
+  if (!plan || !count) return fail(DKT_E_ARG, "null argument");
+  *count = plan->pl.n_launch;
+  return DKT_OK;
 }
 
 void dkt_plan_destroy(dkt_plan plan)
@@ -450,6 +579,39 @@ int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double 
     uint8_t *l = (uint8_t *) std::malloc((size_t) n + 1);
     if (!c || !l) { std::free(c); std::free(l); return fail(DKT_E_NOMEM, "host allocation failed"); }
     dkt::unpack_cells_to_host(keys, n, 4, max_depth, c, l, 0);
+    *n_out = n;
+    *coords = c;
+    *levels = l;
+    return DKT_OK;
+  });
+}
+
+int dkt_mesh_sphere_shell(int dim, int max_depth, int level, double radius, double halfwidth, const double *centre,
+                          int64_t *n_out, uint32_t **coords, uint8_t **levels)
+{
+  if (!centre || !n_out || !coords || !levels || dim < 2 || dim > 4 || level < 1 || level > max_depth ||
+      dim * max_depth + 6 > 64)
+    return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    const auto cells = dkt::sphere_shell_tree(dim, max_depth, level, radius, halfwidth, centre);
+    return export_cells(cells, dim, n_out, coords, levels);
+  });
+}
+
+int dkt_mesh_sphere_shell_device(int dim, int max_depth, int level, double radius, double halfwidth,
+                                 const double *centre, int64_t *n_out, uint32_t **coords, uint8_t **levels)
+{
+  if (!centre || !n_out || !coords || !levels || dim < 2 || dim > 4 || level < 1 || level > max_depth ||
+      dim * max_depth + 6 > 64)
+    return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    dkt::DBuf<uint64_t> keys;
+    int64_t n = 0;
+    dkt::sphere_shell_device(dim, max_depth, level, radius, halfwidth, centre, keys, n, 0);
+    uint32_t *c = (uint32_t *) std::malloc((size_t) n * dim * sizeof(uint32_t) + 1);
+    uint8_t *l = (uint8_t *) std::malloc((size_t) n + 1);
+    if (!c || !l) { std::free(c); std::free(l); return fail(DKT_E_NOMEM, "host allocation failed"); }
+    dkt::unpack_cells_to_host(keys, n, dim, max_depth, c, l, 0);
     *n_out = n;
     *coords = c;
     *levels = l;

@@ -2,6 +2,7 @@
 // (FEM/examples/src/heatMat.cpp:164-325), with an optional Jacobi
 // preconditioner.  All vectors stay on the device; reductions are two-stage
 // with a fixed summation order, so a solve is bitwise reproducible.
+#include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
 
@@ -78,9 +79,13 @@ __global__ void k_pupdate(double *__restrict__ p, const double *__restrict__ z, 
 // Diagonal of the element operators assembled over the directly owned ranks
 // of every leaf (interpolated hanging contributions are left out, which keeps
 // it a valid Jacobi scaling).  Boundary rows, which feMatrix zeroes, get 1.
+// Accumulated in int64 fixed point (scale 2^sc from the largest element
+// diagonal) so that the sum, and every solve that uses it, is bitwise
+// reproducible whatever the order of the atomics.
 __global__ void k_diag(const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, int64_t n_leaf, int npe,
                        const double *__restrict__ A, const double *__restrict__ B, const double *__restrict__ alpha,
-                       const double *__restrict__ beta, const double *__restrict__ table, double *__restrict__ diag)
+                       const double *__restrict__ beta, const double *__restrict__ table, int sc,
+                       unsigned long long *__restrict__ dq)
 {
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_leaf) return;
@@ -90,8 +95,13 @@ __global__ void k_diag(const int32_t *__restrict__ e2n, const uint32_t *__restri
     if (n < 0) continue;
     const double v = table ? table[((int64_t) L * npe + r) * npe + r]
                            : alpha[L] * A[r * npe + r] + beta[L] * B[r * npe + r];
-    atomicAdd(&diag[n], v);
+    atomicAdd(dq + n, (unsigned long long) __double2ll_rn(ldexp(v, sc)));
   }
+}
+__global__ void k_diag_out(const long long *__restrict__ dq, double *__restrict__ d, int64_t n, int sc)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = ldexp((double) dq[i], -sc);
 }
 __global__ void k_invert_diag(double *__restrict__ d, int64_t n)
 {
@@ -106,15 +116,31 @@ __global__ void k_set_at(double *__restrict__ v, const uint32_t *__restrict__ id
 
 void diagonal(const Plan &pl, double *diag, cudaStream_t s)
 {
-  DKT_CUDA(cudaMemsetAsync(diag, 0, pl.n_nodes * sizeof(double), s));
   const bool custom = pl.op.kind == OP_CUSTOM;
+  // largest |element diagonal entry| over the levels, from the host copies
+  double mx = 0.0;
+  const int npe = pl.npe, nlev = pl.md + 1;
+  for (int L = 0; L < nlev; L++)
+    for (int r = 0; r < npe; r++) {
+      const double v = custom ? pl.op.table[((size_t) L * npe + r) * npe + r]
+                              : pl.op.alpha[L] * pl.op.A[(size_t) r * npe + r] + pl.op.beta[L] * pl.op.B[(size_t) r * npe + r];
+      mx = std::max(mx, std::fabs(v));
+    }
+  int e = 0;
+  if (mx > 0.0) std::frexp(mx, &e);          // mx < 2^e
+  const int sc = 62 - 8 - e;                 // up to 256 contributions per node
+  DBuf<unsigned long long> dq(pl.n_nodes);
+  DKT_CUDA(cudaMemsetAsync(dq.p, 0, pl.n_nodes * sizeof(unsigned long long), s));
   k_diag<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.e2n.p, pl.info.p, pl.n_leaf, pl.npe, pl.opA.p, pl.opB.p,
-                                             pl.opAlpha.p, pl.opBeta.p, custom ? pl.opTable.p : nullptr, diag);
+                                             pl.opAlpha.p, pl.opBeta.p, custom ? pl.opTable.p : nullptr, sc, dq.p);
   check_launch("diag");
+  k_diag_out<<<grid_for(pl.n_nodes), 256, 0, s>>>((const long long *) dq.p, diag, pl.n_nodes, sc);
+  check_launch("diag_out");
   if (op_has_bc(pl.op.kind) && pl.n_bdry > 0) {
     k_set_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(diag, pl.bdry.p, pl.n_bdry, 1.0);
     check_launch("diag_bdry");
   }
+  DKT_CUDA(cudaStreamSynchronize(s));   // dq is freed on return
 }
 
 int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,

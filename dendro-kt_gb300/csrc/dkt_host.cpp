@@ -374,4 +374,37 @@ std::vector<Cell> moving_ball_tree(int md, int level, double R, double w, const 
   return balance(leaves, 4, md);
 }
 
+// Static sphere shell in dim 2..4 (same arithmetic as the device test).
+static void shell_refine(const Cell &c, int dim, int md, int level, double R, double w, const double *ctr,
+                         std::vector<Cell> &leaves)
+{
+  const double sc = std::ldexp(1.0, -md), h = std::ldexp(1.0, -(int) c.lev);
+  double s_near = 0.0, s_far = 0.0;
+  for (int d = 0; d < dim; d++) {
+    const double lo = (double) c.x[d] * sc, hi = lo + h;
+    const double g = ctr[d] < lo ? lo - ctr[d] : (ctr[d] > hi ? ctr[d] - hi : 0.0);
+    const double f = std::max(std::fabs(ctr[d] - lo), std::fabs(hi - ctr[d]));
+    s_near = s_near + g * g;
+    s_far = s_far + f * f;
+  }
+  const bool meets = (std::sqrt(s_near) <= R + w) && (std::sqrt(s_far) >= R - w);
+  if (!meets || (int) c.lev >= level) { leaves.push_back(c); return; }
+  const uint32_t cl = 1u << (md - c.lev - 1);
+  for (int ch = 0; ch < (1 << dim); ch++) {
+    Cell k = c;
+    k.lev = c.lev + 1;
+    for (int d = 0; d < dim; d++) k.x[d] = c.x[d] | (((ch >> d) & 1) ? cl : 0u);
+    shell_refine(k, dim, md, level, R, w, ctr, leaves);
+  }
+}
+
+std::vector<Cell> sphere_shell_tree(int dim, int md, int level, double R, double w, const double *ctr)
+{
+  Cell root{};
+  root.lev = 0;
+  std::vector<Cell> leaves;
+  shell_refine(root, dim, md, level, R, w, ctr, leaves);
+  return balance(leaves, dim, md);
+}
+
 }  // namespace dkt

@@ -20,5 +20,6 @@ struct Cell {
 void gaussian_points(int64_t n, int dim, int md, double mean, double sd, uint64_t seed, uint32_t *out);
 std::vector<Cell> tree_from_points(const uint32_t *pts, int64_t n, int dim, int md, int64_t max_pts);
 std::vector<Cell> moving_ball_tree(int md, int level, double R, double w, const double *c0, const double *c1);
+std::vector<Cell> sphere_shell_tree(int dim, int md, int level, double R, double w, const double *ctr);
 
 }  // namespace dkt

@@ -177,10 +177,29 @@ struct Plan {
   DBuf<long long> fx_fm, xq, yq;
   DBuf<int> fx_fe, fx_sx;
   DBuf<unsigned long long> fx_amax;
+  // binary32 variant of the same Q1 operators (inner solves).
+  bool f32_ready = false;
+  DBuf<float> f32_f, x32;
+  // Tiles of the Q1 kernels (dkt_tile.cu): T leaves per tile, per-tile
+  // distinct-node lists and 16-bit local maps.
+  bool tl_ready = false;
+  int tl_T = 0;
+  int64_t tl_n = 0, tl_sum_u = 0;
+  uint32_t tl_umax = 0;
+  DBuf<int64_t> tl_off, tl_lstart;   // per tile: node-list offset, first leaf
+  DBuf<uint32_t> tl_nodes, tl_fm;     // distinct nodes (| exclusive flag); reflected fill masks
+  DBuf<uint16_t> tl_e2l, tl_p2l;
   // Optional CUDA-event timing of the leaf kernel on its launching stream.
   bool timing = false;
   std::vector<cudaEvent_t> ev;       // start/stop pairs of the current window
   int64_t timed_launches = 0;
+  // Kernels this plan's products have launched (all of them, cumulative).
+  int64_t n_launch = 0;
+  // batches (dkt_batch.cu): node offset of every mesh, plus the end; empty
+  // for a single mesh
+  std::vector<int64_t> seg;
+  // stale-chain shape: longest run in groups and in entries
+  int64_t st_max_run_groups = 0, st_max_run_ents = 0;
 };
 
 }  // namespace dkt

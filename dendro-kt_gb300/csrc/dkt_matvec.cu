@@ -205,6 +205,7 @@ static void launch_leaf(Plan &pl, const double *x, double *y, double scale, cuda
                                       pl.op.uses_scale ? scale : 1.0, ST_ARGS);
   }
   check_launch("matvec_leaf");
+  pl.n_launch++;
   if (pl.timing) {
     DKT_CUDA(cudaEventRecord(e1, s));
     pl.ev.push_back(e0);
@@ -245,11 +246,13 @@ void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStr
   if (pl.n_bdry > 0) {
     k_zero_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(pl.xin.p, pl.bdry.p, pl.n_bdry);
     check_launch("zero_bdry_in");
+    pl.n_launch++;
   }
   matvec(pl, pl.xin.p, y, scale, s);
   if (pl.n_bdry > 0) {
     k_zero_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(y, pl.bdry.p, pl.n_bdry);
     check_launch("zero_bdry_out");
+    pl.n_launch++;
   }
 }
 

@@ -47,6 +47,17 @@ template <> __device__ __forceinline__ unsigned key_digit<Key128>(const Key128 &
 }
 
 // Device buffer with RAII.
+// Device bytes held through DBuf by the calling host thread (current and
+// peak); a served request reads its own footprint from it.
+struct MemCounter {
+  int64_t cur = 0, peak = 0;
+};
+inline MemCounter &mem_counter()
+{
+  static thread_local MemCounter m;
+  return m;
+}
+
 template <typename T>
 struct DBuf {
   T *p = nullptr;
@@ -57,11 +68,19 @@ struct DBuf {
   {
     free();
     n = count;
-    if (count) DKT_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    if (count) {
+      DKT_CUDA(cudaMalloc(&p, count * sizeof(T)));
+      MemCounter &m = mem_counter();
+      m.cur += (int64_t) (count * sizeof(T));
+      if (m.cur > m.peak) m.peak = m.cur;
+    }
   }
   void free()
   {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      mem_counter().cur -= (int64_t) (n * sizeof(T));
+    }
     p = nullptr;
     n = 0;
   }

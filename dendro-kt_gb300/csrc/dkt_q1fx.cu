@@ -19,44 +19,38 @@
 // 2^(54-dim) and a node can absorb 256 of them; y = yq * 2^-(sx+c).
 #include <cmath>
 #include "dkt_internal.cuh"
+#include "dkt_q1.cuh"
 
 namespace dkt {
-
-__device__ __forceinline__ long long mulshift(long long v, long long m, int e)
-{
-  // floor(v * m / 2^e) with a 128-bit intermediate, 1 <= e <= 126
-  const long long hi = __mul64hi(v, m);
-  const unsigned long long lo = (unsigned long long) v * (unsigned long long) m;
-  if (e >= 64) return hi >> (e - 64);
-  return (long long) ((lo >> e) | ((unsigned long long) hi << (64 - e)));
-}
 
 // One thread per four lexicographic ranks of a leaf (2^dim / 4 lanes per
 // leaf): butterflies along axes 0 and 1 stay in registers, along the higher
 // axes they are warp shuffles between the lanes of the leaf.  Each lane reads
-// its four node indices with one 16-byte load.  The integer steps are the
-// same as evaluating the leaf sequentially, so results are bit-identical.
-template <int DIM>
-__device__ __forceinline__ void bfly_reg(long long *v, int d)
+// its four node indices with one 16-byte load.  In fixed point the integer
+// steps are the same as evaluating the leaf sequentially, so results are
+// bit-identical.
+template <typename T>
+__device__ __forceinline__ void bfly_reg(T *v, int d)
 {
   // axis d in {0, 1} inside the thread's four ranks
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     if (k & (1 << d)) continue;
-    const long long a = v[k], b = v[k | (1 << d)];
+    const T a = v[k], b = v[k | (1 << d)];
     v[k] = a + b;
     v[k | (1 << d)] = a - b;
   }
 }
 
-template <int DIM>
-__global__ void __launch_bounds__(256) k_matvec_q1fx(
+template <int DIM, typename AR>
+__global__ void __launch_bounds__(256) k_matvec_q1(
     const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
-    const long long *__restrict__ fm, const int *__restrict__ fe, const long long *__restrict__ xq,
-    unsigned long long *__restrict__ yq, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
-    const long long *__restrict__ stvq, int conforming)
+    const void *__restrict__ fm, const int *__restrict__ fe, const typename AR::T *__restrict__ xq,
+    typename AR::T *__restrict__ yq, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
+    const typename AR::T *__restrict__ stvq, int conforming)
 {
+  using T = typename AR::T;
   constexpr int NPE = 1 << DIM, LPL = NPE / 4;
   const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t i = tid / LPL;
@@ -70,15 +64,15 @@ __global__ void __launch_bounds__(256) k_matvec_q1fx(
   int4 e = make_int4(-1, -1, -1, -1);
   if (valid) e = __ldg(reinterpret_cast<const int4 *>(e2n + i * NPE + rb));
   const int nd[4] = {e.x, e.y, e.z, e.w};
-  long long v[4];
+  T v[4];
 #pragma unroll
-  for (int k = 0; k < 4; k++) v[k] = nd[k] >= 0 ? __ldg(xq + nd[k]) : 0ll;
+  for (int k = 0; k < 4; k++) v[k] = nd[k] >= 0 ? __ldg(xq + nd[k]) : T(0);
   int64_t h = 0;
   uint32_t fmask = 0xFFFFu;
   int pn[4] = {-1, -1, -1, -1};
   const bool grp_hang = (LPL > 1) ? (bool) __any_sync(0xffffffffu, hang) : hang;
   if (grp_hang) {
-    long long xp[4] = {0, 0, 0, 0};
+    T xp[4] = {T(0), T(0), T(0), T(0)};
     if (hang) {
       h = __ldg(hidx + i);
       fmask = __ldg(fill + h * 3);
@@ -101,7 +95,7 @@ __global__ void __launch_bounds__(256) k_matvec_q1fx(
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         if (k & (1 << d)) continue;
-        const long long m = (xp[k] + xp[k | (1 << d)]) >> 1;
+        const T m = AR::half_sum(xp[k], xp[k | (1 << d)]);
         if (cb) xp[k] = m; else xp[k | (1 << d)] = m;
       }
     }
@@ -111,8 +105,8 @@ __global__ void __launch_bounds__(256) k_matvec_q1fx(
       const bool mine = (sub >> (d - 2)) & 1;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        const long long o = __shfl_xor_sync(0xffffffffu, xp[k], 1 << (d - 2));
-        if (mine != cb) xp[k] = (xp[k] + o) >> 1;
+        const T o = __shfl_xor_sync(0xffffffffu, xp[k], 1 << (d - 2));
+        if (mine != cb) xp[k] = AR::half_sum(xp[k], o);
       }
     }
     if (hang) {
@@ -122,49 +116,49 @@ __global__ void __launch_bounds__(256) k_matvec_q1fx(
     }
   }
   // Walsh-Hadamard transform, per-mode scaling, transform back
-  bfly_reg<DIM>(v, 0);
-  bfly_reg<DIM>(v, 1);
+  bfly_reg<T>(v, 0);
+  bfly_reg<T>(v, 1);
 #pragma unroll
   for (int d = 2; d < DIM; d++) {
     const bool mine = (sub >> (d - 2)) & 1;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const long long o = __shfl_xor_sync(0xffffffffu, v[k], 1 << (d - 2));
+      const T o = __shfl_xor_sync(0xffffffffu, v[k], 1 << (d - 2));
       v[k] = mine ? (o - v[k]) : (v[k] + o);
     }
   }
   if (valid) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k] = mulshift(v[k], __ldg(fm + L * NPE + rb + k), __ldg(fe + L * NPE + rb + k));
+    for (int k = 0; k < 4; k++) v[k] = AR::scale(v[k], fm, fe, L * NPE + rb + k);
   }
-  bfly_reg<DIM>(v, 0);
-  bfly_reg<DIM>(v, 1);
+  bfly_reg<T>(v, 0);
+  bfly_reg<T>(v, 1);
 #pragma unroll
   for (int d = 2; d < DIM; d++) {
     const bool mine = (sub >> (d - 2)) & 1;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const long long o = __shfl_xor_sync(0xffffffffu, v[k], 1 << (d - 2));
+      const T o = __shfl_xor_sync(0xffffffffu, v[k], 1 << (d - 2));
       v[k] = mine ? (o - v[k]) : (v[k] + o);
     }
   }
 #pragma unroll
   for (int k = 0; k < 4; k++)
-    if (nd[k] >= 0) atomicAdd(yq + nd[k], (unsigned long long) v[k]);
+    if (nd[k] >= 0) AR::add(yq + nd[k], v[k]);
   if (grp_hang) {
     // transpose of the interpolation on the unfilled ranks, into the parent nodes
-    long long z[4];
+    T z[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) z[k] = (hang && !((fmask >> (rb + k)) & 1u)) ? v[k] : 0ll;
+    for (int k = 0; k < 4; k++) z[k] = (hang && !((fmask >> (rb + k)) & 1u)) ? v[k] : T(0);
 #pragma unroll
     for (int d = 0; d < 2; d++) {
       const bool cb = (child >> d) & 1u;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         if (k & (1 << d)) continue;
-        const long long a = z[k], b = z[k | (1 << d)];
-        if (cb) { z[k] = a >> 1; z[k | (1 << d)] = b + (a >> 1); }
-        else { z[k] = a + (b >> 1); z[k | (1 << d)] = b >> 1; }
+        const T a = z[k], b = z[k | (1 << d)];
+        if (cb) { z[k] = AR::half(a); z[k | (1 << d)] = b + AR::half(a); }
+        else { z[k] = a + AR::half(b); z[k | (1 << d)] = AR::half(b); }
       }
     }
 #pragma unroll
@@ -173,15 +167,14 @@ __global__ void __launch_bounds__(256) k_matvec_q1fx(
       const bool mine = (sub >> (d - 2)) & 1;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        const long long o = __shfl_xor_sync(0xffffffffu, z[k], 1 << (d - 2));
-        z[k] = (mine == cb) ? z[k] + (o >> 1) : (z[k] >> 1);
+        const T o = __shfl_xor_sync(0xffffffffu, z[k], 1 << (d - 2));
+        z[k] = (mine == cb) ? z[k] + AR::half(o) : AR::half(z[k]);
       }
     }
     if (hang) {
 #pragma unroll
       for (int k = 0; k < 4; k++)
-        if (pn[k] >= 0 && (conforming || !((fmask >> (rb + k)) & 1u)))
-          atomicAdd(yq + pn[k], (unsigned long long) z[k]);
+        if (pn[k] >= 0 && (conforming || !((fmask >> (rb + k)) & 1u))) AR::add(yq + pn[k], z[k]);
     }
   }
 }
@@ -280,13 +273,17 @@ bool q1fx_setup(Plan &pl, cudaStream_t s)
   std::vector<int> fe((size_t) nlev * NPE);
   for (size_t k = 0; k < D.size(); k++) {
     const double f = std::ldexp(D[k], c);
-    if (f == 0.0) { fm[k] = 0; fe[k] = 1; continue; }
+    if (f == 0.0) { fm[k] = 0; fe[k] = 64; continue; }
     int ef = 0;
     std::frexp(f, &ef);                       // f < 2^ef, ef <= -6-dim
     const int e = 62 - ef;                    // fm = f * 2^e < 2^62
     fe[k] = std::min(e, 126);
     fm[k] = (long long) std::llround(std::ldexp(f, fe[k]));
   }
+  std::vector<float> f32(D.size());
+  for (size_t k = 0; k < D.size(); k++) f32[k] = (float) D[k];
+  pl.f32_f.upload(f32.data(), f32.size(), s);
+  pl.f32_ready = !pl.st_ready || pl.st_n_runs == 0;
   pl.fx_c = c;
   pl.fx_fm.upload(fm.data(), fm.size(), s);
   pl.fx_fe.upload(fe.data(), fe.size(), s);
@@ -298,6 +295,9 @@ bool q1fx_setup(Plan &pl, cudaStream_t s)
   return true;
 }
 
+void tiled_fixed(Plan &pl, cudaStream_t s);
+void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s);
+
 template <int DIM>
 static void launch_q1fx(Plan &pl, cudaStream_t s)
 {
@@ -308,16 +308,66 @@ static void launch_q1fx(Plan &pl, cudaStream_t s)
     DKT_CUDA(cudaEventCreate(&e1));
     DKT_CUDA(cudaEventRecord(e0, s));
   }
-  k_matvec_q1fx<DIM><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
+  if (pl.tl_ready) tiled_fixed(pl, s);
+  else k_matvec_q1<DIM, FixedArith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.fx_fe.p,
-      (const long long *) pl.xq.p, (unsigned long long *) pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr,
-      pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0);
-  check_launch("matvec_q1fx");
+      pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0);
+  if (!pl.tl_ready) {
+    check_launch("matvec_q1fx");
+    pl.n_launch++;
+  }
   if (pl.timing) {
     DKT_CUDA(cudaEventRecord(e1, s));
     pl.ev.push_back(e0);
     pl.ev.push_back(e1);
     pl.timed_launches++;
+  }
+}
+
+template <int DIM>
+static void launch_q1f32(Plan &pl, const float *x, float *y, cudaStream_t s)
+{
+  const unsigned threads = 256;
+  if (pl.tl_ready) { tiled_f32(pl, x, y, s); return; }
+  k_matvec_q1<DIM, F32Arith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
+      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.f32_f.p, nullptr, x, y,
+      nullptr, nullptr, nullptr, pl.conforming ? 1 : 0);
+  check_launch("matvec_q1f32");
+  pl.n_launch++;
+}
+
+__global__ void k_zero_ids_f(float *__restrict__ v, const uint32_t *__restrict__ ids, int64_t nb)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nb) v[ids[i]] = 0.0f;
+}
+
+// Binary32 product with the Q1 operator of the plan.  bc_in / bc_out zero the
+// domain-boundary entries of the input (through a scratch copy) and of the
+// output, as feMatrix::matVec does for the operators with boundary steps.
+void q1f32_apply(Plan &pl, const float *x, float *y, bool bc_in, bool bc_out, cudaStream_t s)
+{
+  if (!pl.f32_ready) throw std::runtime_error("binary32 product needs a Q1 built-in operator without stale parent reads");
+  const int64_t n = pl.n_nodes;
+  if (bc_in && pl.n_bdry > 0) {
+    if (pl.x32.n < (size_t) n) pl.x32.alloc(n);
+    DKT_CUDA(cudaMemcpyAsync(pl.x32.p, x, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    k_zero_ids_f<<<grid_for(pl.n_bdry), 256, 0, s>>>(pl.x32.p, pl.bdry.p, pl.n_bdry);
+    check_launch("zero_in_f32");
+    pl.n_launch++;
+    x = pl.x32.p;
+  }
+  DKT_CUDA(cudaMemsetAsync(y, 0, n * sizeof(float), s));
+  switch (pl.dim) {
+    case 2: launch_q1f32<2>(pl, x, y, s); break;
+    case 3: launch_q1f32<3>(pl, x, y, s); break;
+    case 4: launch_q1f32<4>(pl, x, y, s); break;
+    default: throw std::runtime_error("unsupported dim");
+  }
+  if (bc_out && pl.n_bdry > 0) {
+    k_zero_ids_f<<<grid_for(pl.n_bdry), 256, 0, s>>>(y, pl.bdry.p, pl.n_bdry);
+    check_launch("zero_out_f32");
+    pl.n_launch++;
   }
 }
 
@@ -342,9 +392,11 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
   k_absmax<<<608, 256, 0, s>>>(x, n, pl.fx_amax.p);
   k_to_fixed<<<608, 256, 0, s>>>(x, pl.xq.p, n, pl.fx_amax.p, pl.fx_sx.p, pl.dim);
   check_launch("to_fixed");
+  pl.n_launch += 2;
   if (bc && pl.n_bdry > 0) {
     k_zero_ids_ll<<<grid_for(pl.n_bdry), 256, 0, s>>>(pl.xq.p, pl.bdry.p, pl.n_bdry);
     check_launch("zero_in");
+    pl.n_launch++;
   }
   DKT_CUDA(cudaMemsetAsync(pl.yq.p, 0, n * sizeof(long long), s));
   stale_eval(pl, nullptr, pl.xq.p, s);
@@ -356,13 +408,16 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
   }
   k_from_fixed<<<608, 256, 0, s>>>(pl.yq.p, y, n, pl.fx_sx.p, pl.fx_c);
   check_launch("from_fixed");
+  pl.n_launch++;
   if (bc && pl.n_bdry > 0) {
     k_zero_ids_d<<<grid_for(pl.n_bdry), 256, 0, s>>>(y, pl.bdry.p, pl.n_bdry);
     check_launch("zero_out");
+    pl.n_launch++;
   }
   if (scale != 1.0 && pl.op.uses_scale) {
     // the built-in operators are linear in scale
     scale_vector(y, n, scale, s);
+    pl.n_launch++;
   }
 }
 

@@ -1,0 +1,466 @@
+// Device-resident Jacobi-preconditioned CG and mixed-precision iterative
+// refinement on the feMatrix operator of a plan -- one mesh, or a batch of
+// independent meshes concatenated into one block-diagonal plan
+// (dkt_batch.cu), each with its own scalars and its own convergence.
+//
+// The vectors are cut into chunks that never straddle two meshes; one CTA
+// per chunk does the vector work and writes per-chunk partial sums, and a
+// one-thread-per-mesh kernel adds each mesh's partials in a fixed order, so
+// every dot product accumulates in FP64 and is bitwise reproducible.  All
+// scalars (alpha, beta, r.z, r.r, a converged flag) stay on the device, so a
+// block of iterations has no host synchronisation and is captured once into
+// a CUDA graph that is relaunched until every mesh has converged.  A
+// converged mesh is frozen (alpha = 0, p kept), so the iterations that run
+// past its convergence change nothing.
+//
+// Mixed precision: the outer loop forms r = b - A x with the exact FP64
+// (fixed-point) product and FP64 vectors, normalises it per mesh, solves
+// A d = r/|r| with binary32 vectors and the binary32 Q1 product to a loose
+// tolerance, and adds |r| d to x in FP64 -- classic iterative refinement, so
+// the final residual is an FP64 residual.
+#include <algorithm>
+#include <cmath>
+#include "dkt_internal.cuh"
+
+namespace dkt {
+
+void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
+void q1f32_apply(Plan &pl, const float *x, float *y, bool bc_in, bool bc_out, cudaStream_t s);
+void diagonal(const Plan &pl, double *diag, cudaStream_t s);
+
+namespace {
+
+constexpr int ST = 256;                 // threads of the vector kernels
+constexpr int64_t CHK = 16384;          // nodes per chunk
+constexpr int CHUNK_IT = 16;            // CG iterations per captured graph
+
+struct CgScal {
+  double rz, pq, rr, alpha, beta, rr_stop;
+  int done, it, conv_it, pad;
+};
+
+struct Chunks {
+  int64_t n = 0;                        // chunks
+  int P = 1;                            // meshes
+  DBuf<int64_t> lo, hi;                 // node range of chunk c
+  DBuf<int32_t> prob;                   // mesh of chunk c
+  DBuf<int32_t> first;                  // chunks of mesh p: [first[p], first[p+1])
+};
+
+void make_chunks(const Plan &pl, Chunks &c, cudaStream_t s)
+{
+  std::vector<int64_t> seg = pl.seg;
+  if (seg.size() < 2) seg = {0, pl.n_nodes};
+  c.P = (int) seg.size() - 1;
+  std::vector<int64_t> lo, hi;
+  std::vector<int32_t> prob, first;
+  for (int p = 0; p < c.P; p++) {
+    first.push_back((int32_t) lo.size());
+    for (int64_t a = seg[p]; a < seg[p + 1]; a += CHK) {
+      lo.push_back(a);
+      hi.push_back(std::min(a + CHK, seg[p + 1]));
+      prob.push_back(p);
+    }
+  }
+  first.push_back((int32_t) lo.size());
+  c.n = (int64_t) lo.size();
+  if (c.n == 0) { lo.push_back(0); hi.push_back(0); prob.push_back(0); }
+  c.lo.upload(lo.data(), lo.size(), s);
+  c.hi.upload(hi.data(), hi.size(), s);
+  c.prob.upload(prob.data(), prob.size(), s);
+  c.first.upload(first.data(), first.size(), s);
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  v = (threadIdx.x < blockDim.x / 32) ? sh[threadIdx.x] : 0.0;
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// part[c] = sum over chunk c of a*b (FP64 accumulation)
+template <typename T>
+__global__ void __launch_bounds__(ST) k_dot(const T *__restrict__ a, const T *__restrict__ b,
+                                           const int64_t *__restrict__ lo, const int64_t *__restrict__ hi,
+                                           double *__restrict__ part)
+{
+  __shared__ double sh[ST / 32];
+  double s = 0.0;
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) s += (double) a[i] * (double) b[i];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// per mesh: sum of its chunks' partials, in chunk order
+__device__ __forceinline__ double mesh_sum(const double *part, int stride, int off, int c0, int c1)
+{
+  double s = 0.0;
+  for (int c = c0; c < c1; c++) s += part[(int64_t) c * stride + off];
+  return s;
+}
+
+// alpha = r.z / p.q (0 once converged or on breakdown)
+__global__ void k_fin_alpha(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
+                            CgScal *__restrict__ sc)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const double pq = mesh_sum(part, 1, 0, first[p], first[p + 1]);
+  CgScal &q = sc[p];
+  q.pq = pq;
+  q.alpha = (q.done || !(pq != 0.0)) ? 0.0 : q.rz / pq;
+}
+
+// x += alpha p; r -= alpha q; z = dinv r; partial sums of r.z and r.r
+template <typename T>
+__global__ void __launch_bounds__(ST) k_update(T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
+                                              const T *__restrict__ p, const T *__restrict__ q,
+                                              const T *__restrict__ dinv, const int64_t *__restrict__ lo,
+                                              const int64_t *__restrict__ hi, const int32_t *__restrict__ prob,
+                                              const CgScal *__restrict__ sc, double *__restrict__ part)
+{
+  __shared__ double sh[ST / 32];
+  const double a = sc[prob[blockIdx.x]].alpha;
+  const T at = (T) a;
+  double srz = 0.0, srr = 0.0;
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) {
+    T ri = r[i];
+    if (a != 0.0) {
+      x[i] += at * p[i];
+      ri -= at * q[i];
+      r[i] = ri;
+    }
+    const T zi = dinv ? ri * dinv[i] : ri;
+    z[i] = zi;
+    srz += (double) ri * (double) zi;
+    srr += (double) ri * (double) ri;
+  }
+  srz = block_sum(srz, sh);
+  srr = block_sum(srr, sh);
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = srz; part[2 * blockIdx.x + 1] = srr; }
+}
+
+// beta = rz_new / rz; convergence test on r.r
+__global__ void k_fin_beta(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
+                           CgScal *__restrict__ sc, int count, int *__restrict__ n_done)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const double a = mesh_sum(part, 2, 0, first[p], first[p + 1]);
+  const double b = mesh_sum(part, 2, 1, first[p], first[p + 1]);
+  CgScal &q = sc[p];
+  if (!q.done) {
+    if (count) q.it++;
+    q.beta = (q.rz != 0.0) ? a / q.rz : 0.0;
+    q.rz = a;
+    q.rr = b;
+    if (b <= q.rr_stop || !(b == b)) {
+      q.done = 1;
+      q.conv_it = q.it;
+      atomicAdd(n_done, 1);
+    }
+  } else {
+    q.beta = 0.0;
+  }
+}
+
+template <typename T>
+__global__ void k_pupd(T *__restrict__ p, const T *__restrict__ z, const int64_t *__restrict__ lo,
+                       const int64_t *__restrict__ hi, const int32_t *__restrict__ prob, const CgScal *__restrict__ sc,
+                       int first)
+{
+  const CgScal &q = sc[prob[blockIdx.x]];
+  if (q.done && !first) return;
+  const T b = (T) q.beta;
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) p[i] = first ? z[i] : z[i] + b * p[i];
+}
+
+__global__ void k_residual(const double *__restrict__ b, const double *__restrict__ ax, double *__restrict__ r,
+                           int64_t n)
+{
+  for (int64_t i = (int64_t) blockIdx.x * ST + threadIdx.x; i < n; i += (int64_t) gridDim.x * ST) r[i] = b[i] - ax[i];
+}
+
+// per mesh: nrm[p] = sqrt(sum of its partials)
+__global__ void k_norms(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
+                        double *__restrict__ nrm)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  nrm[p] = sqrt(mesh_sum(part, 1, 0, first[p], first[p + 1]));
+}
+
+// r32 = r / |r| on meshes still above tolerance, 0 elsewhere
+__global__ void k_scale_down(const double *__restrict__ r, float *__restrict__ r32, const int64_t *__restrict__ lo,
+                             const int64_t *__restrict__ hi, const int32_t *__restrict__ prob,
+                             const double *__restrict__ nrm, const int *__restrict__ active)
+{
+  const int p = prob[blockIdx.x];
+  const double s = (active[p] && nrm[p] > 0.0) ? 1.0 / nrm[p] : 0.0;
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) r32[i] = (float) (r[i] * s);
+}
+__global__ void k_add_scaled(double *__restrict__ x, const float *__restrict__ d, const int64_t *__restrict__ lo,
+                             const int64_t *__restrict__ hi, const int32_t *__restrict__ prob,
+                             const double *__restrict__ nrm, const int *__restrict__ active)
+{
+  const int p = prob[blockIdx.x];
+  if (!active[p]) return;
+  const double s = nrm[p];
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) x[i] += s * (double) d[i];
+}
+__global__ void k_invert(const double *__restrict__ d, double *__restrict__ o64, float *__restrict__ o32, int64_t n)
+{
+  for (int64_t i = (int64_t) blockIdx.x * ST + threadIdx.x; i < n; i += (int64_t) gridDim.x * ST) {
+    const double v = (d[i] != 0.0) ? 1.0 / d[i] : 1.0;
+    if (o64) o64[i] = v;
+    if (o32) o32[i] = (float) v;
+  }
+}
+__global__ void k_init_scal(CgScal *sc, int P, const double *__restrict__ rr_stop, double rr_stop_all,
+                            int *__restrict__ n_done)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0) *n_done = 0;
+  if (p >= P) return;
+  CgScal &q = sc[p];
+  q.rz = q.pq = q.rr = q.alpha = q.beta = 0.0;
+  q.rr_stop = rr_stop ? rr_stop[p] : rr_stop_all;
+  q.done = 0;
+  q.it = 0;
+  q.conv_it = -1;
+}
+
+// The operator of one CG: FP64 feMatrix product or binary32 product.
+template <typename T> struct CgOp;
+template <> struct CgOp<double> {
+  static void apply(Plan &pl, const double *x, double *y, cudaStream_t s) { fematrix_matvec(pl, x, y, 1.0, s); }
+};
+template <> struct CgOp<float> {
+  // CG vectors keep zero boundary entries, so the input needs no clearing
+  static void apply(Plan &pl, const float *x, float *y, cudaStream_t s) { q1f32_apply(pl, x, y, false, true, s); }
+};
+
+inline unsigned pgrid(int P) { return (unsigned) ((P + 127) / 128); }
+
+// Jacobi-PCG on all meshes of the plan, in type T (FP64 dots).  r must hold
+// b - A x on entry.
+template <typename T>
+struct Cg {
+  Plan &pl;
+  const Chunks &ch;
+  int64_t n;
+  DBuf<T> z, p, q;
+  DBuf<double> part;
+  DBuf<CgScal> sc;
+  DBuf<int> n_done;
+  std::vector<CgScal> hsc;
+  int *h_done = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  T *gx = nullptr, *gr = nullptr;
+  const T *gd = nullptr;
+  int64_t graph_count = 0;   // kernels in one launch of the graph
+
+  Cg(Plan &pl_, const Chunks &ch_)
+      : pl(pl_), ch(ch_), n(pl_.n_nodes), z(n), p(n), q(n), part(2 * std::max<int64_t>(ch_.n, 1)), sc(ch_.P),
+        n_done(1), hsc(ch_.P)
+  {
+    DKT_CUDA(cudaMallocHost(&h_done, sizeof(int)));
+  }
+  ~Cg()
+  {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (h_done) cudaFreeHost(h_done);
+  }
+
+  void iteration(T *x, T *r, const T *dinv, cudaStream_t s)
+  {
+    const unsigned nb = (unsigned) ch.n;
+    CgOp<T>::apply(pl, p.p, q.p, s);
+    k_dot<T><<<nb, ST, 0, s>>>(p.p, q.p, ch.lo.p, ch.hi.p, part.p);
+    k_fin_alpha<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p);
+    k_update<T><<<nb, ST, 0, s>>>(x, r, z.p, p.p, q.p, dinv, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, part.p);
+    k_fin_beta<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 1, n_done.p);
+    k_pupd<T><<<nb, ST, 0, s>>>(p.p, z.p, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, 0);
+    check_launch("cg_iteration");
+    pl.n_launch += 5;
+  }
+
+  // Runs until every mesh converged or max_iter iterations; per-mesh
+  // results in hsc (conv_it = -1: not converged).
+  void solve(T *x, T *r, const T *dinv, const double *rr_stop_dev, double rr_stop, int max_iter, cudaStream_t s)
+  {
+    if (ch.n == 0) return;
+    const unsigned nb = (unsigned) ch.n;
+    k_init_scal<<<pgrid(ch.P), 128, 0, s>>>(sc.p, ch.P, rr_stop_dev, rr_stop, n_done.p);
+    // z = dinv r, r.z, r.r (alpha = 0 leaves x and r unchanged), p = z
+    k_update<T><<<nb, ST, 0, s>>>(x, r, z.p, p.p, q.p, dinv, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, part.p);
+    k_fin_beta<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 0, n_done.p);
+    k_pupd<T><<<nb, ST, 0, s>>>(p.p, z.p, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, 1);
+    check_launch("cg_start");
+    pl.n_launch += 4;
+    if (exec == nullptr || gx != x || gr != r || gd != dinv) {
+      if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+      cudaGraph_t g = nullptr;
+      const int64_t before = pl.n_launch;
+      DKT_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        for (int k = 0; k < CHUNK_IT; k++) iteration(x, r, dinv, s);
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        pl.n_launch = before;
+        throw;
+      }
+      DKT_CUDA(cudaStreamEndCapture(s, &g));
+      graph_count = pl.n_launch - before;
+      pl.n_launch = before;
+      const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      DKT_CUDA(e);
+      gx = x; gr = r; gd = dinv;
+    }
+    int done_iters = 0;
+    for (;;) {
+      DKT_CUDA(cudaMemcpyAsync(h_done, n_done.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      DKT_CUDA(cudaStreamSynchronize(s));
+      if (*h_done >= ch.P || done_iters >= max_iter) break;
+      DKT_CUDA(cudaGraphLaunch(exec, s));
+      pl.n_launch += graph_count;
+      done_iters += CHUNK_IT;
+    }
+    DKT_CUDA(cudaMemcpyAsync(hsc.data(), sc.p, ch.P * sizeof(CgScal), cudaMemcpyDeviceToHost, s));
+    DKT_CUDA(cudaStreamSynchronize(s));
+  }
+};
+
+}  // namespace
+
+// FP64 Jacobi-PCG (precision 0) or mixed-precision refinement (precision 1)
+// on every mesh of the plan.  Per mesh: iterations, refinements and the
+// relative residual ||b - A x|| / ||b||.  Returns 0 when every mesh reached
+// tol, -5 otherwise.
+int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter, double tol, bool jacobi,
+              int *iters, int *refinements, double *relres, cudaStream_t user)
+{
+  const int64_t n = pl.n_nodes;
+  if (precision == 1 && !pl.f32_ready)
+    throw std::runtime_error("mixed precision needs a Q1 built-in operator without stale parent reads");
+  const bool saved_timing = pl.timing;
+  pl.timing = false;
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev = nullptr;
+  DKT_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  DKT_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  DKT_CUDA(cudaEventRecord(ev, user));
+  DKT_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  int rc = -5;
+  try {
+    Chunks ch;
+    make_chunks(pl, ch, s);
+    const int P = ch.P;
+    const unsigned nb = (unsigned) std::max<int64_t>(ch.n, 1);
+    std::vector<int> tot(P, 0), outer(P, 0), h_active(P, 1);
+    std::vector<double> rel(P, 0.0), hb(P), hr(P);
+    DBuf<double> d(n), dinv(jacobi ? n : 0), ax(n), part(std::max<int64_t>(ch.n, 1)), bnrm(P), rnrm(P);
+    DBuf<float> dinv32(jacobi && precision == 1 ? n : 0);
+    DBuf<int> active(P);
+    if (jacobi) {
+      diagonal(pl, d.p, s);
+      k_invert<<<608, ST, 0, s>>>(d.p, dinv.p, dinv32.p, n);
+      pl.n_launch += 2;
+    }
+    // per-mesh ||b||
+    k_dot<double><<<nb, ST, 0, s>>>(b, b, ch.lo.p, ch.hi.p, part.p);
+    k_norms<<<pgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, bnrm.p);
+    pl.n_launch += 2;
+    DKT_CUDA(cudaMemcpyAsync(hb.data(), bnrm.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
+    DKT_CUDA(cudaStreamSynchronize(s));
+    for (int p = 0; p < P; p++) if (!(hb[p] > 0.0)) hb[p] = 1.0;
+    if (precision == 0) {
+      Cg<double> cg(pl, ch);
+      DBuf<double> r(n), stop(P);
+      std::vector<double> hs(P);
+      for (int p = 0; p < P; p++) hs[p] = tol * tol * hb[p] * hb[p];
+      stop.upload(hs.data(), P, s);
+      fematrix_matvec(pl, x, ax.p, 1.0, s);
+      k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
+      pl.n_launch++;
+      cg.solve(x, r.p, jacobi ? dinv.p : nullptr, stop.p, 0.0, max_iter, s);
+      rc = 0;
+      for (int p = 0; p < P; p++) {
+        const CgScal &q = cg.hsc[p];
+        tot[p] = q.conv_it >= 0 ? q.conv_it : q.it;
+        rel[p] = std::sqrt(q.rr) / hb[p];
+        if (!(q.done && q.rr <= hs[p])) rc = -5;
+      }
+    } else {
+      Cg<float> cg(pl, ch);
+      DBuf<float> dx(n), r32(n);
+      DBuf<double> r(n);
+      const double inner_tol = 1e-5;
+      int used = 0;
+      for (int step = 0; step < 60; step++) {
+        fematrix_matvec(pl, x, ax.p, 1.0, s);
+        k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
+        k_dot<double><<<nb, ST, 0, s>>>(r.p, r.p, ch.lo.p, ch.hi.p, part.p);
+        k_norms<<<pgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, rnrm.p);
+        pl.n_launch += 3;
+        DKT_CUDA(cudaMemcpyAsync(hr.data(), rnrm.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
+        DKT_CUDA(cudaStreamSynchronize(s));
+        int n_active = 0;
+        for (int p = 0; p < P; p++) {
+          rel[p] = hr[p] / hb[p];
+          h_active[p] = rel[p] > tol ? 1 : 0;
+          n_active += h_active[p];
+        }
+        if (n_active == 0) { rc = 0; break; }
+        if (used >= max_iter) break;
+        for (int p = 0; p < P; p++) outer[p] += h_active[p];
+        active.upload(h_active.data(), P, s);
+        // r32 = r / |r| on active meshes, dx = 0, inner solve A dx = r32
+        k_scale_down<<<nb, ST, 0, s>>>(r.p, r32.p, ch.lo.p, ch.hi.p, ch.prob.p, rnrm.p, active.p);
+        DKT_CUDA(cudaMemsetAsync(dx.p, 0, n * sizeof(float), s));
+        pl.n_launch++;
+        cg.solve(dx.p, r32.p, jacobi ? dinv32.p : nullptr, nullptr, inner_tol * inner_tol, max_iter - used, s);
+        int most = 0;
+        for (int p = 0; p < P; p++) {
+          const CgScal &q = cg.hsc[p];
+          const int it = q.conv_it >= 0 ? q.conv_it : q.it;
+          if (h_active[p]) tot[p] += it;
+          most = std::max(most, it);
+        }
+        used += std::max(most, 1);
+        // x += |r| dx on active meshes
+        k_add_scaled<<<nb, ST, 0, s>>>(x, dx.p, ch.lo.p, ch.hi.p, ch.prob.p, rnrm.p, active.p);
+        pl.n_launch++;
+      }
+    }
+    check_launch("pcg");
+    DKT_CUDA(cudaEventRecord(ev, s));
+    DKT_CUDA(cudaStreamWaitEvent(user, ev, 0));
+    DKT_CUDA(cudaStreamSynchronize(s));
+    for (int p = 0; p < P; p++) {
+      if (iters) iters[p] = tot[p];
+      if (refinements) refinements[p] = outer[p];
+      if (relres) relres[p] = rel[p];
+    }
+  } catch (...) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    cudaEventDestroy(ev);
+    pl.timing = saved_timing;
+    throw;
+  }
+  cudaStreamDestroy(s);
+  cudaEventDestroy(ev);
+  pl.timing = saved_timing;
+  return rc;
+}
+
+}  // namespace dkt

@@ -15,6 +15,7 @@
 // independent runs of consecutive hanging leaves, and evaluates each run per
 // product with one thread walking it in order.  The leaf kernels then read
 // the run results in place of the unrefilled slots.
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <vector>
@@ -150,6 +151,11 @@ void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s)
   }
   pl.st_n_ent = n_ent;
   pl.st_n_runs = (int64_t) runs.size() / 2;
+  pl.st_max_run_groups = pl.st_max_run_ents = 0;
+  for (size_t k = 0; k + 1 < runs.size(); k += 2) {
+    pl.st_max_run_groups = std::max<int64_t>(pl.st_max_run_groups, runs[k + 1] - runs[k]);
+    pl.st_max_run_ents = std::max<int64_t>(pl.st_max_run_ents, gstart[runs[k + 1]] - gstart[runs[k]]);
+  }
   // keep every upload non-empty
   if (fidx.empty()) { fidx.push_back(0); fw.push_back(0.0); }
   if (sidx.empty()) { sidx.push_back(0); sw.push_back(0.0); }
@@ -188,27 +194,87 @@ __global__ void k_stale_fresh(int64_t n_ent, const int32_t *__restrict__ row, co
   f[e] = acc;
 }
 
-// The chained part: one warp per run walks its groups in order; lanes split
-// the entries of a group.  Values of the previous group were written by the
-// same warp before the __syncwarp.
+// The chained part: one block per run.  The run is cut into chunks of
+// consecutive groups (at most CH_E entries and ch_t stale terms); the block
+// stages a chunk's fresh parts and terms in shared memory with coalesced
+// loads, one warp walks the groups in order (lanes split a group's entries;
+// every term refers to the previous group, whose values are in shared
+// memory), then the block writes the chunk's values out.  The walk touches
+// shared memory only, so a step costs a few shared-memory latencies.
+constexpr int CH_E = 512;      // entries per chunk
+constexpr int CH_G = 128;      // groups per chunk
+constexpr int CH_THREADS = 128;
+static_assert(CH_G == CH_THREADS, "one group test per thread");
+
 template <bool FIXED>
-__global__ void k_stale_chain(const int32_t *__restrict__ runs, int64_t n_runs, const int32_t *__restrict__ gstart,
-                              const int32_t *__restrict__ srow, const int32_t *__restrict__ sidx,
-                              const double *__restrict__ sw, const double *__restrict__ f, double *__restrict__ v,
-                              long long *__restrict__ vq)
+__global__ void __launch_bounds__(CH_THREADS) k_stale_chain(
+    const int32_t *__restrict__ runs, int64_t n_runs, const int32_t *__restrict__ gstart,
+    const int32_t *__restrict__ srow, const int32_t *__restrict__ sidx, const double *__restrict__ sw,
+    const double *__restrict__ f, double *__restrict__ v, long long *__restrict__ vq, int ch_t, int max_grp)
 {
-  const int64_t wid = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (wid >= n_runs) return;
-  for (int32_t grp = runs[2 * wid]; grp < runs[2 * wid + 1]; grp++) {
-    for (int32_t e = gstart[grp] + lane; e < gstart[grp + 1]; e += 32) {
-      double acc = f[e];
-      for (int32_t k = srow[e]; k < srow[e + 1]; k++) acc += sw[k] * __ldcg(v + sidx[k]);
-      __stcg(v + e, acc);
-      if (FIXED) vq[e] = __double2ll_rn(acc);
+  extern __shared__ __align__(16) unsigned char smem[];
+  double *wS = reinterpret_cast<double *>(smem);            // [ch_t]
+  double *fS = wS + ch_t;                                   // [CH_E]
+  double *vals = fS + CH_E;                                 // [CH_E]
+  double *carry = vals + CH_E;                              // [max_grp]
+  int32_t *iS = reinterpret_cast<int32_t *>(carry + max_grp);   // [ch_t]
+  int32_t *rS = iS + ch_t;                                  // [CH_E + 1]
+  int32_t *gS = rS + CH_E + 1;                              // [CH_G + 1]
+  const int64_t run = blockIdx.x;
+  if (run >= n_runs) return;
+  const int32_t g_end = runs[2 * run + 1];
+  int32_t g0 = runs[2 * run];
+  int32_t carry_base = 0;   // entry id of carry[0]
+  while (g0 < g_end) {
+    const int32_t e0 = gstart[g0], t0 = srow[e0];
+    // chunk length: the groups [g0, g0 + cg) that fit (monotone test)
+    int ok = 0;
+    for (int t = threadIdx.x; t < CH_G; t += CH_THREADS) {
+      const int32_t g = g0 + t;
+      if (g < g_end) {
+        const int32_t ee = gstart[g + 1];
+        if (ee - e0 <= CH_E && srow[ee] - t0 <= ch_t) ok++;
+      }
     }
-    __syncwarp();
-    __threadfence_block();
+    const int cg_raw = __syncthreads_count(ok);   // CH_G == CH_THREADS: ok is 0 or 1
+    const int cg = cg_raw > 0 ? cg_raw : 1;
+    const int32_t e1 = gstart[g0 + cg], t1 = srow[e1];
+    for (int k = threadIdx.x; k <= cg; k += CH_THREADS) gS[k] = gstart[g0 + k] - e0;
+    for (int32_t e = threadIdx.x; e < e1 - e0; e += CH_THREADS) {
+      fS[e] = f[e0 + e];
+      rS[e] = srow[e0 + e] - t0;
+    }
+    if (threadIdx.x == 0) rS[e1 - e0] = t1 - t0;
+    for (int32_t k = threadIdx.x; k < t1 - t0; k += CH_THREADS) {
+      iS[k] = sidx[t0 + k];
+      wS[k] = sw[t0 + k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      for (int j = 0; j < cg; j++) {
+        for (int e = gS[j] + (int) threadIdx.x; e < gS[j + 1]; e += 32) {
+          double acc = fS[e];
+          for (int k = rS[e]; k < rS[e + 1]; k++) {
+            const int32_t id = iS[k];
+            acc += wS[k] * (j == 0 ? carry[id - carry_base] : vals[id - e0]);
+          }
+          vals[e] = acc;
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int32_t e = threadIdx.x; e < e1 - e0; e += CH_THREADS) {
+      const double a = vals[e];
+      v[e0 + e] = a;
+      if (FIXED) vq[e0 + e] = __double2ll_rn(a);
+    }
+    // the last group's values become the carry of the next chunk
+    const int32_t lb = gS[cg - 1];
+    for (int32_t e = lb + threadIdx.x; e < gS[cg]; e += CH_THREADS) carry[e - lb] = vals[e];
+    carry_base = e0 + lb;
+    __syncthreads();
+    g0 += cg;
   }
 }
 
@@ -216,20 +282,28 @@ void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
 {
   if (!pl.st_ready || pl.st_n_runs == 0) return;
   const int64_t ne = pl.st_n_ent;
+  const int npe = pl.npe;
+  const int ch_t = std::max(4096, npe * npe);
+  const size_t smem = (size_t) ch_t * 12 + (size_t) 2 * CH_E * 8 + (size_t) npe * 8 + (size_t) (CH_E + 1) * 4
+                      + (size_t) (CH_G + 1) * 4 + 64;
+  const unsigned blocks = (unsigned) pl.st_n_runs;
   if (xq) {
     k_stale_fresh<true><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, nullptr, xq,
                                                            pl.st_f.p);
-    k_stale_chain<true><<<grid_for(pl.st_n_runs * 32, 128), 128, 0, s>>>(
-        pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p, pl.st_sw.p, pl.st_f.p, pl.st_v.p,
-        pl.st_vq.p);
+    auto kfn = k_stale_chain<true>;
+    DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    kfn<<<blocks, CH_THREADS, smem, s>>>(pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p,
+                                         pl.st_sw.p, pl.st_f.p, pl.st_v.p, pl.st_vq.p, ch_t, npe);
   } else {
     k_stale_fresh<false><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, x, nullptr,
                                                             pl.st_f.p);
-    k_stale_chain<false><<<grid_for(pl.st_n_runs * 32, 128), 128, 0, s>>>(
-        pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p, pl.st_sw.p, pl.st_f.p, pl.st_v.p,
-        nullptr);
+    auto kfn = k_stale_chain<false>;
+    DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    kfn<<<blocks, CH_THREADS, smem, s>>>(pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p,
+                                         pl.st_sw.p, pl.st_f.p, pl.st_v.p, nullptr, ch_t, npe);
   }
   check_launch("stale_eval");
+  pl.n_launch += 2;
 }
 
 }  // namespace dkt

@@ -1,0 +1,408 @@
+// Tiled Q1 leaf kernel.
+//
+// The flattened traversal is cut into tiles of T consecutive leaves (SFC
+// order).  Once per plan, every tile gets the sorted list of the distinct
+// nodes its leaves touch (own nodes and, for hanging leaves, parent nodes)
+// and 16-bit tile-local copies of the element-to-node and parent-to-node
+// maps.  Per product, one CTA per tile
+//   1. gathers the tile's node values into shared memory (one global read per
+//      distinct node instead of one per leaf slot),
+//   2. runs one thread per leaf entirely in registers: parent interpolation,
+//      Walsh-Hadamard transform along every axis, per-mode scaling, inverse
+//      transform, transpose of the interpolation -- no warp shuffles,
+//   3. accumulates into a shared-memory copy of the tile's output and
+//   4. flushes it with one global atomic per distinct node, or a plain store
+//      for nodes that no other tile touches.
+// SFC locality makes a tile's node set small (about two nodes per 4D leaf),
+// so global gathers and atomics drop from ~2*2^dim per leaf to ~2, and the
+// 16-bit maps halve the map bytes.
+//
+// Hanging leaves are stored reflected to child 0: the maps of a leaf with
+// Morton child number c list rank k ^ c at position k (and its fill mask is
+// permuted the same way).  The element matrix of a cube is invariant under
+// reflections, so the product is unchanged, while the parent interpolation
+// and its transpose always take the child-0 form -- no per-axis selects.
+// Fixed point stays deterministic; in reflected coordinates some Hadamard
+// modes change sign, so individual roundings of the mode scaling may differ
+// by one unit (2^-50 of max|x|) from the per-leaf kernel.
+#include <algorithm>
+#include "dkt_internal.cuh"
+#include "dkt_q1.cuh"
+
+namespace dkt {
+
+constexpr uint16_t TL_NONE = 0xFFFFu;
+constexpr uint32_t TL_EXCL = 0x80000000u;
+
+// ---------------------------------------------------------------------------
+// Plan-time tile build: one CTA per tile sorts the tile's (node, slot) pairs
+// in shared memory (bitonic), marks the distinct nodes and ranks them.
+//   mode 0: count the distinct nodes per tile and, per node, the tiles that
+//           touch it;
+//   mode 1: write the node list (with the exclusive flag) and the local maps.
+// Slot s < T*npe is rank s%npe of local leaf s/npe; slot T*npe + j*npe + q is
+// parent slot q of local leaf j (hanging leaves only).
+// ---------------------------------------------------------------------------
+constexpr int TB_THREADS = 512;
+
+__global__ void __launch_bounds__(TB_THREADS) k_tile_build(
+    int mode, const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+    const int32_t *__restrict__ p2n, int64_t n_leaf, int npe, int T, int cap, uint32_t *__restrict__ node_tiles,
+    uint32_t *__restrict__ tile_cnt, const int64_t *__restrict__ tile_off, uint32_t *__restrict__ tile_nodes,
+    uint16_t *__restrict__ e2l, uint16_t *__restrict__ p2l)
+// (mode 1 writes the maps of hanging leaves reflected: rank r at position r ^ c)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t *key = reinterpret_cast<uint64_t *>(smem);            // [cap]
+  __shared__ uint32_t part[TB_THREADS];
+  const int64_t tile = blockIdx.x;
+  const int64_t l0 = tile * T;
+  const int nl = (int) (n_leaf - l0 < T ? n_leaf - l0 : T);
+  for (int s = threadIdx.x; s < cap; s += TB_THREADS) {
+    int32_t node = -1;
+    const int half = T * npe;
+    if (s < half) {
+      const int j = s / npe;
+      if (j < nl) node = e2n[(l0 + j) * npe + s % npe];
+    } else {
+      const int j = (s - half) / npe;
+      if (j < nl && ((info[l0 + j] >> 16) & 1u)) node = p2n[(int64_t) hidx[l0 + j] * npe + (s - half) % npe];
+    }
+    key[s] = node >= 0 ? (((uint64_t) (uint32_t) node << 32) | (uint32_t) s) : ~0ull;
+  }
+  __syncthreads();
+  // bitonic sort, ascending
+  for (int k = 2; k <= cap; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < cap; i += TB_THREADS) {
+        const int p = i ^ j;
+        if (p > i) {
+          const uint64_t a = key[i], b = key[p];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) { key[i] = b; key[p] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // distinct-node ranks: each thread owns a contiguous run of cap/TB_THREADS keys
+  const int per = cap / TB_THREADS;   // cap is a multiple of TB_THREADS
+  const int b0 = threadIdx.x * per;
+  uint32_t cnt = 0;
+  for (int k = b0; k < b0 + per; k++) {
+    const uint64_t a = key[k];
+    if (a != ~0ull && (k == 0 || (key[k - 1] >> 32) != (a >> 32))) cnt++;
+  }
+  part[threadIdx.x] = cnt;
+  __syncthreads();
+  // inclusive scan of part (Hillis-Steele)
+  for (int o = 1; o < TB_THREADS; o <<= 1) {
+    const uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  const uint32_t total = part[TB_THREADS - 1];
+  uint32_t rank = part[threadIdx.x] - cnt;   // heads before this run
+  if (mode == 0 && threadIdx.x == 0) tile_cnt[tile] = total;
+  const int64_t base = mode == 1 ? tile_off[tile] : 0;
+  for (int k = b0; k < b0 + per; k++) {
+    const uint64_t a = key[k];
+    if (a == ~0ull) break;
+    const uint32_t node = (uint32_t) (a >> 32);
+    const bool head = (k == 0 || (key[k - 1] >> 32) != (a >> 32));
+    if (head) {
+      rank++;
+      if (mode == 0) atomicAdd(node_tiles + node, 1u);
+      else tile_nodes[base + rank - 1] = node | (node_tiles[node] == 1u ? TL_EXCL : 0u);
+    }
+    if (mode == 1) {
+      const int s = (int) (uint32_t) a;
+      const int half = T * npe;
+      const uint16_t lr = (uint16_t) (rank - 1);
+      if (s < half) {
+        const int j = s / npe;
+        const uint32_t inf = info[l0 + j];
+        const int c = ((inf >> 16) & 1u) ? (int) ((inf >> 8) & 0xFFu) : 0;
+        e2l[(l0 + j) * npe + ((s % npe) ^ c)] = lr;
+      } else {
+        const int j = (s - half) / npe;
+        const int c = (int) ((info[l0 + j] >> 8) & 0xFFu);
+        p2l[(int64_t) hidx[l0 + j] * npe + (((s - half) % npe) ^ c)] = lr;
+      }
+    }
+  }
+}
+
+// Reflected fill masks: bit k = fill bit (k ^ c) of hanging leaf h (Q1: nPe <= 16).
+__global__ void k_tile_fmask(const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+                             const uint32_t *__restrict__ fill, int64_t n_leaf, int npe, uint32_t *__restrict__ fm)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_leaf) return;
+  const uint32_t inf = info[i];
+  if (!((inf >> 16) & 1u)) return;
+  const int c = (int) ((inf >> 8) & 0xFFu);
+  const int64_t h = hidx[i];
+  const uint32_t f = fill[h * 3];
+  uint32_t m = 0;
+  for (int k = 0; k < npe; k++) m |= ((f >> (k ^ c)) & 1u) << k;
+  fm[h] = m;
+}
+__global__ void k_tile_lstart(int64_t *__restrict__ ls, int64_t n_tile, int64_t T, int64_t n_leaf)
+{
+  const int64_t t = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t <= n_tile) ls[t] = t < n_tile ? t * T : n_leaf;
+}
+
+void tile_setup(Plan &pl, int T, cudaStream_t s)
+{
+  pl.tl_ready = false;
+  pl.tl_T = 0;
+  if (pl.order != 1 || pl.n_leaf == 0 || T <= 0) return;
+  if (T < 32 || T > 1024 || (T & (T - 1))) throw std::invalid_argument("tile size must be a power of two in [32, 1024]");
+  const int npe = pl.npe;
+  int cap = 1;
+  while (cap < 2 * T * npe) cap <<= 1;
+  cap = std::max(cap, TB_THREADS);
+  if (cap > 65536) throw std::invalid_argument("tile too large");   // 16-bit local indices
+  const int64_t n_tile = (pl.n_leaf + T - 1) / T;
+  DBuf<uint32_t> node_tiles(pl.n_nodes), cnt(n_tile);
+  DKT_CUDA(cudaMemsetAsync(node_tiles.p, 0, pl.n_nodes * sizeof(uint32_t), s));
+  const size_t smem = (size_t) cap * sizeof(uint64_t);
+  DKT_CUDA(cudaFuncSetAttribute(k_tile_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+  k_tile_build<<<(unsigned) n_tile, TB_THREADS, smem, s>>>(0, pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.n_leaf,
+                                                          npe, T, cap, node_tiles.p, cnt.p, nullptr, nullptr,
+                                                          nullptr, nullptr);
+  check_launch("tile_count");
+  // offsets (host scan: one value per tile) and the largest tile
+  std::vector<uint32_t> hc(n_tile);
+  DKT_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_tile * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  DKT_CUDA(cudaStreamSynchronize(s));
+  std::vector<int64_t> ho(n_tile + 1, 0);
+  uint32_t umax = 0;
+  for (int64_t t = 0; t < n_tile; t++) {
+    ho[t + 1] = ho[t] + hc[t];
+    umax = std::max(umax, hc[t]);
+  }
+  pl.tl_off.upload(ho.data(), ho.size(), s);
+  pl.tl_nodes.alloc(std::max<int64_t>(ho[n_tile], 1));
+  pl.tl_e2l.alloc((size_t) pl.n_leaf * npe);
+  pl.tl_p2l.alloc((size_t) std::max<int64_t>(pl.n_hang, 1) * npe);
+  DKT_CUDA(cudaMemsetAsync(pl.tl_e2l.p, 0xFF, (size_t) pl.n_leaf * npe * sizeof(uint16_t), s));
+  DKT_CUDA(cudaMemsetAsync(pl.tl_p2l.p, 0xFF, (size_t) std::max<int64_t>(pl.n_hang, 1) * npe * sizeof(uint16_t), s));
+  k_tile_build<<<(unsigned) n_tile, TB_THREADS, smem, s>>>(1, pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.n_leaf,
+                                                          npe, T, cap, node_tiles.p, cnt.p, pl.tl_off.p,
+                                                          pl.tl_nodes.p, pl.tl_e2l.p, pl.tl_p2l.p);
+  check_launch("tile_fill");
+  pl.tl_fm.alloc(std::max<int64_t>(pl.n_hang, 1));
+  k_tile_fmask<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.info.p, pl.hidx.p, pl.fill.p, pl.n_leaf, npe, pl.tl_fm.p);
+  pl.tl_lstart.alloc(n_tile + 1);
+  k_tile_lstart<<<grid_for(n_tile + 1), 256, 0, s>>>(pl.tl_lstart.p, n_tile, T, pl.n_leaf);
+  check_launch("tile_masks");
+  DKT_CUDA(cudaStreamSynchronize(s));
+  pl.tl_T = T;
+  pl.tl_n = n_tile;
+  pl.tl_umax = umax;
+  pl.tl_sum_u = ho[n_tile];
+  pl.tl_ready = true;
+}
+
+// ---------------------------------------------------------------------------
+// The tiled leaf kernel.  One thread per leaf; blockDim.x == T.
+// ---------------------------------------------------------------------------
+template <int DIM, typename T>
+__device__ __forceinline__ void wht(T (&v)[1 << DIM])
+{
+#pragma unroll
+  for (int d = 0; d < DIM; d++)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (1 << d))) {
+        const T a = v[k], b = v[k | (1 << d)];
+        v[k] = a + b;
+        v[k | (1 << d)] = a - b;
+      }
+}
+
+// One row of NPE 16-bit local indices as NPE/2 packed words (16-byte loads).
+template <int NPE>
+__device__ __forceinline__ void load_row16(const uint16_t *__restrict__ row, uint32_t (&w)[NPE / 2])
+{
+  if constexpr (NPE == 16) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(row));
+    const uint4 b = __ldg(reinterpret_cast<const uint4 *>(row) + 1);
+    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w; w[4] = b.x; w[5] = b.y; w[6] = b.z; w[7] = b.w;
+  } else if constexpr (NPE == 8) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(row));
+    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+  } else {
+    const uint2 a = __ldg(reinterpret_cast<const uint2 *>(row));
+    w[0] = a.x; w[1] = a.y;
+  }
+}
+template <int NPE>
+__device__ __forceinline__ uint32_t idx16(const uint32_t (&w)[NPE / 2], int k)
+{
+  return (w[k >> 1] >> ((k & 1) * 16)) & 0xFFFFu;
+}
+
+template <int DIM, int T_LEAVES, typename AR>
+__global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
+    const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
+    const int32_t *__restrict__ hidx, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
+    const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
+    const int *__restrict__ fe, int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
+    const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
+    int conforming)
+{
+  using V = typename AR::T;
+  using F = typename AR::Factor;
+  constexpr int NPE = 1 << DIM;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int64_t tile = blockIdx.x;
+  const int64_t u0 = tile_off[tile];
+  const int U = (int) (tile_off[tile + 1] - u0);
+  F *fac = reinterpret_cast<F *>(smem);
+  V *xs = reinterpret_cast<V *>(fac + n_fac);
+  V *ys = xs + U;
+  for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) fac[k] = AR::load_factor(fm, fe, k);
+  for (int u = threadIdx.x; u < U; u += T_LEAVES) {
+    const uint32_t id = __ldg(tile_nodes + u0 + u) & ~TL_EXCL;
+    xs[u] = __ldg(xq + id);
+    ys[u] = V(0);
+  }
+  __syncthreads();
+  const int64_t i = tile_ls[tile] + threadIdx.x;
+  if (i < tile_ls[tile + 1]) {
+    const uint32_t inf = __ldg(info + i);
+    const int L = inf & 0xFFu;
+    const bool hang = (inf >> 16) & 1u;
+    uint32_t w[NPE / 2];   // two 16-bit local indices per word
+    load_row16<NPE>(e2l + i * NPE, w);
+    auto lidx = [&](int k) -> uint32_t { return idx16<NPE>(w, k); };
+    V v[NPE];
+    uint32_t fmask = 0xFFFFFFFFu;
+    int64_t h = -1;
+    if (hang) {
+      h = __ldg(hidx + i);
+      fmask = __ldg(fmask_r + h);
+      const int c = (int) ((inf >> 8) & 0xFFu);
+      const int32_t hz = hzoff ? __ldg(hzoff + h) : -1;
+      uint32_t pw[NPE / 2];
+      load_row16<NPE>(p2l + h * NPE, pw);
+#pragma unroll
+      for (int k = 0; k < NPE; k++) {
+        const uint32_t p = idx16<NPE>(pw, k);
+        v[k] = V(0);
+        if (p != TL_NONE) v[k] = xs[p];
+        else if (hz >= 0) {
+          const int32_t id = __ldg(hztab + (int64_t) hz * NPE + (k ^ c));
+          if (id >= 0) v[k] = __ldg(stvq + id);
+        }
+      }
+      // parent -> child-0 interpolation, axes in order
+#pragma unroll
+      for (int d = 0; d < DIM; d++)
+#pragma unroll
+        for (int k = 0; k < NPE; k++)
+          if (!(k & (1 << d))) v[k | (1 << d)] = AR::half_sum(v[k], v[k | (1 << d)]);
+#pragma unroll
+      for (int k = 0; k < NPE; k++)
+        if ((fmask >> k) & 1u) v[k] = xs[lidx(k)];
+    } else {
+#pragma unroll
+      for (int k = 0; k < NPE; k++) {
+        const uint32_t l = lidx(k);
+        v[k] = l != TL_NONE ? xs[l] : V(0);
+      }
+    }
+    wht<DIM, V>(v);
+#pragma unroll
+    for (int k = 0; k < NPE; k++) v[k] = AR::apply(v[k], fac[L * NPE + k]);
+    wht<DIM, V>(v);
+#pragma unroll
+    for (int k = 0; k < NPE; k++) {
+      const uint32_t l = lidx(k);
+      if (l != TL_NONE) AR::add(ys + l, v[k]);
+    }
+    if (hang) {
+      // transpose of the child-0 interpolation on the unfilled ranks, into the parent nodes
+#pragma unroll
+      for (int k = 0; k < NPE; k++)
+        if ((fmask >> k) & 1u) v[k] = V(0);
+#pragma unroll
+      for (int d = 0; d < DIM; d++)
+#pragma unroll
+        for (int k = 0; k < NPE; k++)
+          if (!(k & (1 << d))) {
+            const V hb = AR::half(v[k | (1 << d)]);
+            v[k] = v[k] + hb;
+            v[k | (1 << d)] = hb;
+          }
+      uint32_t pw[NPE / 2];
+      load_row16<NPE>(p2l + h * NPE, pw);
+#pragma unroll
+      for (int k = 0; k < NPE; k++) {
+        const uint32_t p = idx16<NPE>(pw, k);
+        if (p != TL_NONE && (conforming || !((fmask >> k) & 1u))) AR::add(ys + p, v[k]);
+      }
+    }
+  }
+  __syncthreads();
+  for (int u = threadIdx.x; u < U; u += T_LEAVES) {
+    const uint32_t id = __ldg(tile_nodes + u0 + u);
+    const V a = ys[u];
+    if (id & TL_EXCL) yq[id & ~TL_EXCL] = a;
+    else if (a != V(0)) AR::add(yq + id, a);
+  }
+}
+
+template <int DIM, int TL, typename AR>
+static void launch_tiled(Plan &pl, const void *fm, const int *fe, const typename AR::T *x, typename AR::T *y,
+                         const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, cudaStream_t s)
+{
+  auto kfn = k_matvec_q1t<DIM, TL, AR>;
+  const int n_fac = (pl.md + 1) * (1 << DIM);
+  const size_t smem = (size_t) n_fac * sizeof(typename AR::Factor) + (size_t) 2 * pl.tl_umax * sizeof(typename AR::T);
+  if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+  kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.hidx.p, pl.tl_fm.p, pl.tl_off.p,
+                                           pl.tl_lstart.p, pl.tl_nodes.p, fm, fe, n_fac, x, y, hzoff, hztab, stv,
+                                           pl.conforming ? 1 : 0);
+}
+
+template <typename AR>
+static void launch_tiled_dim(Plan &pl, const void *fm, const int *fe, const typename AR::T *x, typename AR::T *y,
+                             const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, cudaStream_t s)
+{
+#define DKT_TL_CASE(D, TL) \
+  case (D) * 10000 + (TL): launch_tiled<D, TL, AR>(pl, fm, fe, x, y, hzoff, hztab, stv, s); break;
+  switch (pl.dim * 10000 + pl.tl_T) {
+    DKT_TL_CASE(2, 128) DKT_TL_CASE(2, 256) DKT_TL_CASE(2, 512)
+    DKT_TL_CASE(3, 128) DKT_TL_CASE(3, 256) DKT_TL_CASE(3, 512)
+    DKT_TL_CASE(4, 64) DKT_TL_CASE(4, 128) DKT_TL_CASE(4, 256)
+    default: throw std::runtime_error("unsupported dim / tile size for the tiled kernel");
+  }
+#undef DKT_TL_CASE
+  check_launch("matvec_q1t");
+  pl.n_launch++;
+}
+
+void tiled_fixed(Plan &pl, cudaStream_t s)
+{
+  launch_tiled_dim<FixedArith>(pl, pl.fx_fm.p, pl.fx_fe.p, pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr,
+                               pl.st_hztab.p, pl.st_vq.p, s);
+}
+
+void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
+{
+  launch_tiled_dim<F32Arith>(pl, pl.f32_f.p, nullptr, x, y, nullptr, nullptr, nullptr, s);
+}
+
+bool tile_size_supported(int dim, int T)
+{
+  if (dim == 4) return T == 64 || T == 128 || T == 256;
+  return T == 128 || T == 256 || T == 512;
+}
+
+}  // namespace dkt

@@ -258,6 +258,85 @@ __global__ void k_not_flag(const uint32_t *__restrict__ f, uint32_t *__restrict_
   if (i < n) g[i] = f[i] ? 0u : 1u;
 }
 
+// Static sphere shell in dim 2..4: refine every cell of level < `level` whose
+// box meets |‖x - c‖ - R| <= w (exact box distance interval).
+struct ShellParams {
+  double R, w, c[MAX_DIM];
+};
+
+__global__ void k_shell_test(const uint64_t *__restrict__ cells, int64_t n, int dim, int md, int level,
+                             ShellParams sp, uint32_t *__restrict__ refine)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t a[MAX_DIM];
+  int lev;
+  tdecode(cells[i], dim, md, a, lev);
+  const double sc = ldexp(1.0, -md), h = ldexp(1.0, -lev);
+  double s_near = 0.0, s_far = 0.0;
+  for (int d = 0; d < dim; d++) {
+    const double lo = __dmul_rn((double) a[d], sc), hi = __dadd_rn(lo, h);
+    const double g = sp.c[d] < lo ? __dsub_rn(lo, sp.c[d]) : (sp.c[d] > hi ? __dsub_rn(sp.c[d], hi) : 0.0);
+    const double f = fmax(fabs(__dsub_rn(sp.c[d], lo)), fabs(__dsub_rn(hi, sp.c[d])));
+    s_near = __dadd_rn(s_near, __dmul_rn(g, g));
+    s_far = __dadd_rn(s_far, __dmul_rn(f, f));
+  }
+  const bool meets = (sqrt(s_near) <= sp.R + sp.w) && (sqrt(s_far) >= sp.R - sp.w);
+  refine[i] = (meets && lev < level) ? 1u : 0u;
+}
+
+// Level-by-level refinement driven by a refine-flag kernel, then 2:1 balance.
+template <typename TestFn>
+static void refine_device(int dim, int md, TestFn test, DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s)
+{
+  DBuf<uint64_t> frontier(1);
+  const uint32_t z[MAX_DIM] = {0, 0, 0, 0};
+  const uint64_t root = cell_key(z, 0, dim, md);
+  frontier.upload(&root, 1, s);
+  int64_t nf = 1;
+  DBuf<uint64_t> leaves;
+  int64_t nl = 0;
+  const int nc = 1 << dim;
+  while (nf > 0) {
+    DBuf<uint32_t> flag(nf), pos(nf), keep(nf), kpos(nf);
+    test(frontier.p, nf, flag.p);
+    check_launch("refine_test");
+    const int64_t nr = (int64_t) exclusive_scan_total<uint32_t>(flag.p, pos.p, nf, s);
+    k_not_flag<<<grid_for(nf), 256, 0, s>>>(flag.p, keep.p, nf);
+    const int64_t nk = (int64_t) exclusive_scan_total<uint32_t>(keep.p, kpos.p, nf, s);
+    if (nk) {
+      DBuf<uint64_t> kept(nk);
+      scatter_if_kernel<uint64_t><<<grid_for(nf), 256, 0, s>>>(frontier.p, keep.p, kpos.p, kept.p, nf);
+      check_launch("refine_keep");
+      t_concat(leaves, nl, kept.p, nk, s);
+    }
+    DBuf<uint64_t> next(nr * nc > 0 ? nr * nc : 1);
+    if (nr) {
+      k_children<<<grid_for(nf), 256, 0, s>>>(frontier.p, flag.p, pos.p, next.p, nf, dim, md);
+      check_launch("refine_children");
+    }
+    DKT_CUDA(cudaStreamSynchronize(s));
+    frontier = std::move(next);
+    nf = nr * nc;
+  }
+  balance_device(leaves, nl, dim, md, s);
+  out = std::move(leaves);
+  n_out = nl;
+}
+
+void sphere_shell_device(int dim, int md, int level, double R, double w, const double *c, DBuf<uint64_t> &out,
+                         int64_t &n_out, cudaStream_t s)
+{
+  if (dim < 2 || dim > MAX_DIM) throw std::invalid_argument("sphere shell: dim must be 2..4");
+  ShellParams sp;
+  sp.R = R;
+  sp.w = w;
+  for (int d = 0; d < MAX_DIM; d++) sp.c[d] = d < dim ? c[d] : 0.0;
+  refine_device(dim, md, [&](const uint64_t *cells, int64_t n, uint32_t *flag) {
+    k_shell_test<<<grid_for(n), 256, 0, s>>>(cells, n, dim, md, level, sp, flag);
+  }, out, n_out, s);
+}
+
 void moving_ball_device(int md, int level, double R, double w, const double *c0, const double *c1,
                         DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s)
 {
@@ -265,38 +344,9 @@ void moving_ball_device(int md, int level, double R, double w, const double *c0,
   bp.R = R;
   bp.w = w;
   for (int d = 0; d < 3; d++) { bp.c0[d] = c0[d]; bp.c1[d] = c1[d]; }
-  DBuf<uint64_t> frontier(1);
-  const uint32_t z[4] = {0, 0, 0, 0};
-  const uint64_t root = cell_key(z, 0, 4, md);
-  frontier.upload(&root, 1, s);
-  int64_t nf = 1;
-  DBuf<uint64_t> leaves;
-  int64_t nl = 0;
-  while (nf > 0) {
-    DBuf<uint32_t> flag(nf), pos(nf), keep(nf), kpos(nf);
-    k_ball_test<<<grid_for(nf), 256, 0, s>>>(frontier.p, nf, md, level, bp, flag.p);
-    check_launch("ball_test");
-    const int64_t nr = (int64_t) exclusive_scan_total<uint32_t>(flag.p, pos.p, nf, s);
-    k_not_flag<<<grid_for(nf), 256, 0, s>>>(flag.p, keep.p, nf);
-    const int64_t nk = (int64_t) exclusive_scan_total<uint32_t>(keep.p, kpos.p, nf, s);
-    if (nk) {
-      DBuf<uint64_t> kept(nk);
-      scatter_if_kernel<uint64_t><<<grid_for(nf), 256, 0, s>>>(frontier.p, keep.p, kpos.p, kept.p, nf);
-      check_launch("ball_keep");
-      t_concat(leaves, nl, kept.p, nk, s);
-    }
-    DBuf<uint64_t> next(nr * 16 > 0 ? nr * 16 : 1);
-    if (nr) {
-      k_children<<<grid_for(nf), 256, 0, s>>>(frontier.p, flag.p, pos.p, next.p, nf, 4, md);
-      check_launch("ball_children");
-    }
-    DKT_CUDA(cudaStreamSynchronize(s));
-    frontier = std::move(next);
-    nf = nr * 16;
-  }
-  balance_device(leaves, nl, 4, md, s);
-  out = std::move(leaves);
-  n_out = nl;
+  refine_device(4, md, [&](const uint64_t *cells, int64_t n, uint32_t *flag) {
+    k_ball_test<<<grid_for(n), 256, 0, s>>>(cells, n, md, level, bp, flag);
+  }, out, n_out, s);
 }
 
 __global__ void k_unpack_cells(const uint64_t *__restrict__ k, uint32_t *__restrict__ x, uint8_t *__restrict__ lev,

@@ -107,6 +107,11 @@ int64_t dkt_plan_num_nodes(dkt_plan plan);
  * zero there), [3] boundary nodes. */
 int dkt_plan_stats(dkt_plan plan, int64_t *out4);
 
+/* Extended counts, up to n of: leaves, hanging leaves, stale slots, boundary
+ * nodes, stale-chain entries, stale-chain runs, longest run (hanging leaves),
+ * longest run (entries).  Instrumentation, no reference counterpart. */
+int dkt_plan_stats_ex(dkt_plan plan, int64_t *out, int n);
+
 /* Host copy of the flattened traversal (for inspection and tests):
  * e2n [leaves][nPe] node of each lexicographic rank or -1; info [leaves]
  * level | child<<8 | hanging<<16; hidx [leaves] hanging record or -1;
@@ -153,6 +158,50 @@ int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream);
 int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int jacobi,
                  int *iters, double *relres, void *stream);
 
+#define DKT_PREC_FP64 0
+#define DKT_PREC_MIXED 1
+
+/* Device-resident CG on the same operator: scalars stay on the device and
+ * blocks of 16 iterations run as one CUDA graph.  For a batch plan every
+ * mesh converges on its own (relative to its own ||b||); iters, refinements
+ * and relres are then arrays with one entry per mesh.  DKT_PREC_FP64: Jacobi-PCG
+ * in FP64.  DKT_PREC_MIXED: iterative refinement -- FP64 residual
+ * b - A x (exact fixed-point product), inner Jacobi-PCG on binary32 vectors
+ * with the binary32 Q1 product to 1e-5 relative, FP64 correction of x --
+ * repeated until ||b - A x||_2 <= tol ||b||_2 (FP64 residual).  Dot products
+ * accumulate in FP64 in both.  Mixed needs a Q1 built-in operator without
+ * stale parent reads (a conforming plan, or a mesh without them); it is the
+ * solver of HeatMat::cgSolve (FEM/examples/src/heatMat.cpp:164-325) with the
+ * precision split that the reference does not have.  iters = CG iterations
+ * (all inner iterations for mixed), refinements = outer steps (0 for FP64).
+ * Returns DKT_OK on convergence, -5 when max_iter was reached. */
+int dkt_pcg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int precision, int max_iter, double tol,
+                  int jacobi, int *iters, int *refinements, double *relres, void *stream);
+
+/* Batch of independent meshes as one block-diagonal plan: the flattened
+ * traversals (and tiles) of n plans are concatenated, so one launch of the
+ * leaf kernel computes all n products and dkt_pcg_solve solves all n
+ * systems at once, each mesh with its own scalars and convergence test.
+ * Vectors are the meshes' vectors one after another (dkt_plan_mesh_offsets).
+ * The plans must share dim, order, max_depth, operator (built-in), traversal
+ * and tile size, and have no stale parent reads; they stay valid and
+ * independent.  No counterpart in the reference (one mesh per ot::DA). */
+int dkt_batch_create(const dkt_plan *plans, int n, dkt_plan *out);
+
+/* Meshes in a plan (1 unless it is a batch) and their node offsets (n+1). */
+int dkt_plan_num_meshes(dkt_plan plan, int *n);
+int dkt_plan_mesh_offsets(dkt_plan plan, int64_t *offsets);
+
+/* Times the feMatrix product with every supported tile size (and the
+ * untiled kernel) on this plan and keeps the fastest. */
+int dkt_plan_autotune(dkt_plan plan, int *best_tile, double *best_ms);
+
+/* Binary32 feMatrix product y = A x with the Q1 built-in operator of the
+ * plan (boundary entries zeroed in and out as feMatrix::matVec does for the
+ * operators with Dirichlet steps).  No counterpart in the reference, which is
+ * FP64 only; accuracy about 1e-6 relative. */
+int dkt_matvec_f32(dkt_plan plan, const float *x_dev, float *y_dev, void *stream);
+
 /* Arithmetic of the leaf kernel.  AUTO (default) uses FIXED where it applies:
  * the Q1 built-in operators are diagonal in the Hadamard basis and run in
  * exact int64 fixed point (deterministic, ~2^-50 relative to max|x|*|K|,
@@ -170,6 +219,18 @@ int dkt_plan_set_arithmetic(dkt_plan plan, int mode);
  * last event), then sets the new state. */
 int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t *launches);
 
+/* Leaf tiling of the Q1 built-in operators: tile_leaves consecutive leaves
+ * (64/128/256 in 4D, 128/256/512 in 2D/3D) share one CTA, a per-tile list of
+ * distinct nodes and 16-bit local maps; 0 selects the untiled kernel.  The
+ * result does not depend on it (fixed point: bitwise).  A tuning knob with no
+ * reference counterpart; plans start with 128 (4D) or 256. */
+int dkt_plan_set_tile(dkt_plan plan, int tile_leaves);
+
+/* Number of kernels this plan's matrix-vector products and solves have
+ * launched so far (cumulative; every kernel of the library, not only the
+ * leaf kernel).  Instrumentation with no counterpart in the reference. */
+int dkt_plan_launch_count(dkt_plan plan, int64_t *count);
+
 void dkt_plan_destroy(dkt_plan plan);
 
 /* Throughput probes of the current device (no counterpart in the reference):
@@ -177,6 +238,43 @@ void dkt_plan_destroy(dkt_plan plan);
 int dkt_probe_device(double *out4);
 
 const char *dkt_last_error(void);
+
+/* ---------------------------------------------------------------------------
+ * Serving: a request loop for Q1 Poisson solves (-Laplace u = f, homogeneous
+ * Dirichlet, conforming traversal).  No counterpart in the reference, which
+ * solves one mesh per process.  Requests are admitted against a device-memory
+ * budget in arrival order and run concurrently on `workers` host threads,
+ * each on its own stream, so kernels of different requests overlap; a
+ * finished request frees its memory and admits the next ones.  The right-hand
+ * side is b = uniform[-1,1] (counter-based, seeded) with Dirichlet rows
+ * zeroed; the solver is dkt_pcg_solve with the server's precision and
+ * tolerance.  Times are seconds since dkt_server_create.
+ * ------------------------------------------------------------------------- */
+typedef struct dkt_server_s *dkt_server;
+
+typedef struct {
+  int rc;                       /* DKT_OK, -5 (not converged) or an error */
+  int dim;
+  int64_t n_elem, n_nodes;
+  int iterations, refinements;
+  double relres;                /* ||b - A x||_2 / ||b||_2 */
+  double t_submit, t_admit, t_start, t_done;
+  int64_t device_bytes;         /* peak device bytes of the request */
+  double est_bytes;             /* footprint the admission used */
+} dkt_solve_report;
+
+int dkt_server_create(int workers, double budget_bytes, int precision, double tol, dkt_server *out);
+/* Copies the tree; returns at once with a ticket. */
+int dkt_server_submit(dkt_server srv, int dim, int max_depth, const uint32_t *tree_coords, const uint8_t *tree_levels,
+                      int64_t n_elem, uint64_t rhs_seed, int64_t *ticket);
+/* Blocks until the request is done. */
+int dkt_server_wait(dkt_server srv, int64_t ticket, dkt_solve_report *report);
+/* Copies the solution (n_nodes values, DA node order) of a finished request. */
+int dkt_server_solution(dkt_server srv, int64_t ticket, double *x_host, int64_t capacity);
+/* Drops a finished request's stored result. */
+int dkt_server_release(dkt_server srv, int64_t ticket);
+/* Finishes the admitted requests, drops the queued ones, joins the workers. */
+void dkt_server_destroy(dkt_server srv);
 
 #ifdef __cplusplus
 }

@@ -37,6 +37,17 @@ int dkt_mesh_moving_ball(int max_depth, int level, double radius, double halfwid
 int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double halfwidth, const double *c0,
                                 const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels);
 
+/* Sphere-shell refinement in dim 2..4, built on the device: every cell of
+ * level < `level` whose box meets | ||x - centre|| - radius | <= halfwidth is
+ * split (exact box distance interval), then the tree is 2:1 balanced.  The
+ * workload generator of the served request stream (refinement on a random
+ * sphere); no reference counterpart beyond SFC_Tree::locTreeBalancing
+ * (src/tsort.cpp:826-854) for the balance.  Arrays are freed with dkt_free. */
+int dkt_mesh_sphere_shell(int dim, int max_depth, int level, double radius, double halfwidth, const double *centre,
+                          int64_t *n_out, uint32_t **coords, uint8_t **levels);   /* host build, same tree */
+int dkt_mesh_sphere_shell_device(int dim, int max_depth, int level, double radius, double halfwidth,
+                                 const double *centre, int64_t *n_out, uint32_t **coords, uint8_t **levels);
+
 void dkt_free(void *p);
 
 #ifdef __cplusplus

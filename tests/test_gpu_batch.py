@@ -1,0 +1,91 @@
+"""Batches of independent meshes as one block-diagonal plan: the batched
+product equals the products of the meshes one by one, and the batched
+solvers converge every mesh to 1e-10 on its own, to the same solutions as
+solving the meshes one at a time."""
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dkt():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return ge.load_package()
+
+
+def _meshes(dkt, sizes, dim=3, md=10):
+    out = []
+    for k, n in enumerate(sizes):
+        tc, tl = dkt.tree_from_points(dkt.cluster_points(n, dim, md, seed=k), dim, md)
+        out.append(dkt.DA(tc, tl, dim, order=1, max_depth=md))
+    return out
+
+
+def _mv(A, x):
+    import torch
+    xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    yd = torch.empty_like(xd)
+    A.matvec(xd, yd)
+    return yd.cpu().numpy()
+
+
+def test_batched_product_equals_single_products(dkt):
+    das = _meshes(dkt, [300, 1200, 50, 2500])
+    mats = [dkt.Matrix(d, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING) for d in das]
+    B = dkt.Matrix.batch(mats)
+    off = B.mesh_offsets()
+    assert B.num_meshes() == 4 and off[-1] == sum(d.n for d in das) == B.n
+    xs = [dkt.uniform_pm1(10 + k, d.n) for k, d in enumerate(das)]
+    yb = _mv(B, np.concatenate(xs))
+    for k, (A, x) in enumerate(zip(mats, xs)):
+        y = _mv(A, x)
+        seg = yb[off[k]:off[k + 1]]
+        assert np.linalg.norm(seg - y) <= 1e-12 * np.linalg.norm(y), k
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_pcg_per_mesh_convergence(dkt, precision):
+    import torch
+    das = _meshes(dkt, [400, 2000, 100, 3000, 800])
+    mats = [dkt.Matrix(d, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING) for d in das]
+    B = dkt.Matrix.batch(mats)
+    off = B.mesh_offsets()
+    bs = []
+    for k, d in enumerate(das):
+        b = dkt.uniform_pm1(20 + k, d.n)
+        b[d.boundary_ids()] = 0.0
+        bs.append(b)
+    bd = torch.from_numpy(np.concatenate(bs)).cuda()
+    xd = torch.zeros_like(bd)
+    it, ref, rr, ok = B.pcg(bd, xd, precision=precision, tol=1e-10)
+    assert ok and len(it) == 5 and np.all(rr <= 1e-10), (it, ref, rr)
+    x = xd.cpu().numpy()
+    for k, (A, d) in enumerate(zip(mats, das)):
+        xk = x[off[k]:off[k + 1]]
+        r = bs[k] - _mv(A, xk)
+        assert np.linalg.norm(r) <= 2e-10 * np.linalg.norm(bs[k]), k
+        bk = torch.from_numpy(bs[k]).cuda()
+        x1 = torch.zeros_like(bk)
+        it1, ref1, rr1, ok1 = A.pcg(bk, x1, precision=precision, tol=1e-10)
+        assert ok1
+        x1 = x1.cpu().numpy()
+        assert np.linalg.norm(xk - x1) <= 1e-6 * np.linalg.norm(x1), k
+        if precision == 0:
+            assert abs(int(it[k]) - it1) <= 2, (k, it[k], it1)
+
+
+def test_autotune_keeps_result(dkt):
+    import torch
+    (d,) = _meshes(dkt, [5000])
+    A = dkt.Matrix(d, op=dkt.OP_LAPMASS)
+    x = dkt.uniform_pm1(3, d.n)
+    y0 = _mv(A, x)
+    T, ms = A.autotune()
+    assert T in (0, 128, 256, 512) and ms > 0
+    y1 = _mv(A, x)
+    assert np.linalg.norm(y1 - y0) <= 1e-14 * np.linalg.norm(y0)

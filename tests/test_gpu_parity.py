@@ -299,3 +299,42 @@ def test_conforming_traversal_vs_oracle(dkt, order):
     finally:
         orc.set_conforming(0)
         orc.set_stale_mode(0)
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_tiled_kernel_bitwise_equals_untiled(dkt, dim):
+    """The tiled Q1 kernel (every supported tile size) agrees with the
+    per-leaf kernel to a few fixed-point units (it evaluates hanging leaves
+    reflected to child 0, which can move single roundings of the mode
+    scaling by one unit), stale parent reads included; every tile size
+    gives bitwise the same product."""
+    if dim == 4:
+        md = 10
+        tc, tl = dkt.moving_ball_tree(max_depth=md, level=5)
+        sizes = (64, 128, 256)
+    else:
+        md = 9
+        tc, tl = dkt.tree_from_points(dkt.gaussian_points(3000, dim, md, seed=7), dim, md)
+        sizes = (128, 256, 512)
+    da = dkt.DA(tc, tl, dim, order=1, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    x = dkt.uniform_pm1(9, da.n)
+    A.set_tile(0)
+    y0 = _gpu_mv(A, x)
+    yt = None
+    for T in sizes:
+        A.set_tile(T)
+        y = _gpu_mv(A, x)
+        assert _rel(y, y0) <= 1e-13, T
+        if yt is None:
+            yt = y
+        assert np.array_equal(y, yt), T
+
+
+def test_device_sphere_shell_equals_host(dkt):
+    for dim, level in ((2, 7), (3, 6), (4, 4)):
+        ctr = [0.45, 0.5, 0.55, 0.5][:dim]
+        hc, hl = dkt.sphere_shell_tree(dim, 10, level, ctr, 0.3, device=False)
+        dc, dl = dkt.sphere_shell_tree(dim, 10, level, ctr, 0.3, device=True)
+        key = lambda c, l: sorted(map(tuple, np.concatenate([c.astype(np.int64), l[:, None].astype(np.int64)], 1)))
+        assert len(hl) == len(dl) and key(hc, hl) == key(dc, dl), dim

@@ -1,0 +1,132 @@
+"""Device-resident CG and mixed-precision refinement (Poisson on adaptive
+meshes, conforming traversal).  The final residual is checked with the FP64
+product and with the oracle's own matvec; the binary32 product is checked
+against the FP64 one."""
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+import oracle_port as orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dkt():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return ge.load_package()
+
+
+def _t(a, dtype=None):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a if dtype is None else a.astype(dtype))).cuda()
+
+
+def _poisson_rhs(dkt, da, seed):
+    """b = M f, f = prod sin(pi x_d) + N(0, 0.1^2) noise at the nodes, Dirichlet rows zeroed."""
+    import torch
+    f = dkt.sine_load(da, noise_sd=0.1, seed=seed)
+    M = dkt.Matrix(da, op=dkt.OP_MASS, traversal=dkt.TRAVERSAL_CONFORMING)
+    fd, bd = _t(f), torch.empty(da.n, dtype=torch.float64, device="cuda")
+    M.matvec(fd, bd)
+    b = bd.cpu().numpy()
+    b[da.boundary_ids()] = 0.0
+    return b
+
+
+def _mesh(dkt, kind):
+    if kind == "gauss3d":
+        md = 9
+        pts = dkt.gaussian_points(4000, 3, md, seed=1)
+        tc, tl = dkt.tree_from_points(pts, 3, md)
+        return dkt.DA(tc, tl, 3, order=1, max_depth=md), 3, md
+    md, level = 8, 4
+    tc, tl = dkt.moving_ball_tree(max_depth=md, level=level)
+    return dkt.DA(tc, tl, 4, order=1, max_depth=md), 4, md
+
+
+@pytest.mark.parametrize("kind", ["gauss3d", "ball4d"])
+def test_f32_product_close_to_fp64(dkt, kind):
+    import torch
+    da, dim, md = _mesh(dkt, kind)
+    for trav in (dkt.TRAVERSAL_CONFORMING, dkt.TRAVERSAL_REFERENCE):
+        A = dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=trav)
+        if trav == dkt.TRAVERSAL_REFERENCE and A.stats()["stale_slots"] > 0:
+            continue
+        x = dkt.uniform_pm1(3, da.n)
+        y64 = torch.empty(da.n, dtype=torch.float64, device="cuda")
+        A.matvec(_t(x), y64)
+        y32 = torch.empty(da.n, dtype=torch.float32, device="cuda")
+        A.matvec_f32(_t(x, np.float32), y32)
+        a, b = y32.double().cpu().numpy(), y64.cpu().numpy()
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 2e-6
+
+
+@pytest.mark.parametrize("kind", ["gauss3d", "ball4d"])
+def test_fp64_and_mixed_pcg_reach_1e10(dkt, kind):
+    import torch
+    da, dim, md = _mesh(dkt, kind)
+    A = dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
+    b = _poisson_rhs(dkt, da, seed=3)
+    bd = _t(b)
+    sols = {}
+    for prec in (dkt.PREC_FP64, dkt.PREC_MIXED):
+        xd = torch.zeros_like(bd)
+        it, ref, rr, ok = A.pcg(bd, xd, precision=prec, tol=1e-10)
+        assert ok and rr <= 1e-10, (prec, it, ref, rr)
+        ax = torch.empty_like(bd)
+        A.matvec(xd, ax)
+        true_rel = np.linalg.norm(b - ax.cpu().numpy()) / np.linalg.norm(b)
+        assert true_rel <= 2e-10, (prec, true_rel)
+        if prec == dkt.PREC_MIXED:
+            assert ref >= 1
+        sols[prec] = xd.cpu().numpy()
+    x64, xm = sols[dkt.PREC_FP64], sols[dkt.PREC_MIXED]
+    assert np.linalg.norm(x64 - xm) / np.linalg.norm(x64) <= 1e-6
+
+
+def test_mixed_solution_against_oracle(dkt):
+    """4D moving-ball Poisson: the mixed-precision solution satisfies the
+    oracle's own (conforming) operator to 1e-10 and matches the oracle's FP64
+    CG solution."""
+    import torch
+    da, dim, md = _mesh(dkt, "ball4d")
+    A = dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
+    b = _poisson_rhs(dkt, da, seed=3)
+    bd = _t(b)
+    xd = torch.zeros_like(bd)
+    it, ref, rr, ok = A.pcg(bd, xd, precision=dkt.PREC_MIXED, tol=1e-10)
+    assert ok
+    x = xd.cpu().numpy()
+    orc.set_curve(dim, md)
+    orc.set_conforming(1)
+    orc.set_stale_mode(1)
+    try:
+        sc, sl = da.tree()
+        ora = orc.DA(sc, sl, dim, 1, dkt.OP_LAPLACE)
+        r = b - ora.matvec(x)
+        assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-10
+        xo, ito, rro = ora.cg(b, max_iter=20000, tol=1e-12)
+        assert rro <= 1e-12
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) <= 1e-7
+    finally:
+        orc.set_conforming(0)
+        orc.set_stale_mode(0)
+
+
+def test_pcg_repeatable_and_graph_free_of_drift(dkt):
+    """Two solves from the same start give bitwise the same x (fixed
+    reduction order, integer products)."""
+    import torch
+    da, dim, md = _mesh(dkt, "gauss3d")
+    A = dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
+    b = _poisson_rhs(dkt, da, seed=5)
+    bd = _t(b)
+    xs = []
+    for _ in range(2):
+        xd = torch.zeros_like(bd)
+        A.pcg(bd, xd, precision=dkt.PREC_FP64, tol=1e-10)
+        xs.append(xd.cpu().numpy())
+    assert np.array_equal(xs[0], xs[1])
