@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solve-level", type=int, default=7,
                     help="moving-ball level of the Poisson solves (FP64 vs mixed PCG); 0 skips them")
+    ap.add_argument("--batch", type=int, default=512, help="problems in the batched 3D Poisson solve; 0 skips it")
+    ap.add_argument("--batch-max-elements", type=float, default=1e6)
+    ap.add_argument("--serve", type=int, default=48, help="requests in the served stream; 0 skips it")
+    ap.add_argument("--serve-max-elements", type=float, default=5e5)
     return ap.parse_args()
 
 
@@ -121,11 +125,13 @@ def traffic(kernel, leaf_visits):
 
 
 def algorithmic_bytes(stats, n_nodes, npe):
-    """Bytes a leaf kernel must move per launch: x read + y write (8 B per node
-    each), per leaf visit nPe int32 node slots and one info word, per hanging
-    leaf nPe int32 parent slots, three fill-mask words and its index."""
+    """Algorithmic bytes of one product (the map layout of the reference
+    traversal, whatever the kernel actually stores): x read and y written
+    once (8 B per node each), per leaf visit nPe int32 node slots and one
+    level/flags word, per hanging leaf nPe int32 parent slots and one
+    child/mask word."""
     nl, nh = stats["leaves"], stats["hanging_leaves"]
-    return 16 * n_nodes + (4 * npe + 4) * nl + (4 * npe + 12 + 4) * nh
+    return 16 * n_nodes + (4 * npe + 4) * nl + (4 * npe + 4) * nh
 
 
 def moving_ball(dkt, level, device=False):
@@ -215,7 +221,9 @@ def run_solves(a, dkt, dev):
     out = {"workload": "4D Q1 Poisson, moving-ball level %d (%d elements, %d nodes), conforming traversal, "
                        "Jacobi-PCG to 1e-10 relative 2-norm residual" % (a.solve_level, da.n_elem, da.n)}
     stream = torch.cuda.current_stream(dev)
-    for name, prec in (("fp64", dkt.PREC_FP64), ("mixed", dkt.PREC_MIXED)):
+    for name, prec, arith in (("fp64_native", dkt.PREC_FP64, dkt.ARITH_FP64), ("fp64", dkt.PREC_FP64, dkt.ARITH_AUTO),
+                              ("mixed", dkt.PREC_MIXED, dkt.ARITH_AUTO)):
+        A.set_arithmetic(arith)
         x = torch.zeros_like(b)
         A.pcg(b, x, precision=prec, tol=1e-10, max_iter=64)      # warm-up: graphs, buffers
         x.zero_()
@@ -233,6 +241,158 @@ def run_solves(a, dkt, dev):
         out[name] = {"solves_per_s": 1e3 / ms, "ms": ms, "iterations": it, "refinements": ref,
                      "relres": rr, "true_relres": true_rel, "converged": bool(ok)}
     out["mixed_over_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    out["mixed_over_fp64_native"] = out["fp64_native"]["ms"] / out["mixed"]["ms"]
+    out["note"] = ("fp64_native: FP64 PCG on the dense native-FP64 leaf kernel (the plain FP64 path); fp64: FP64 PCG "
+                   "on the exact int64 fixed-point product; mixed: binary32 inner PCG, FP64 refinement")
+    return out
+
+
+def batch_trees(dkt, n_prob, lo, hi, md=10):
+    """Batched workload: element targets log-uniform in [lo, hi] (numpy PCG64
+    stream 12345); mesh k refined around the 1-4 Gaussian clusters (sd 0.05)
+    of cluster_points(seed=k), the point count adjusted to land within 10%
+    of the target (two corrections at most).  Built on host threads."""
+    import concurrent.futures as cf
+    rng = np.random.default_rng(12345)
+    targets = np.exp(rng.uniform(np.log(lo), np.log(hi), n_prob)).astype(np.int64)
+
+    def build(k):
+        t = int(targets[k])
+        n = max(4, t // 6)
+        for _ in range(3):
+            c, l = dkt.tree_from_points(dkt.cluster_points(n, 3, md, seed=k), 3, md)
+            r = len(l) / t
+            if 0.9 <= r <= 1.1:
+                break
+            n = max(4, int(n / r))
+        return c, l
+
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        return list(ex.map(build, range(n_prob))), targets
+
+
+def run_batch(a, dkt, dev):
+    """512 independent 3D Q1 Poisson problems (conforming traversal, uniform
+    [-1,1] right-hand sides with Dirichlet rows zeroed) as one block-diagonal
+    plan: every product, vector update and reduction is one launch over all
+    problems, the CG iterations are captured in CUDA graphs, the tile size is
+    picked by timing; mixed-precision refinement against FP64 PCG, both to
+    1e-10 per problem."""
+    import concurrent.futures as cf
+    import torch
+    md = 10
+    t0 = time.perf_counter()
+    trees, targets = batch_trees(dkt, a.batch, 1e3, a.batch_max_elements, md)
+    t_mesh = time.perf_counter() - t0
+
+    def plan(k):
+        c, l = trees[k]
+        da = dkt.DA(c, l, 3, order=1, max_depth=md)
+        return da, dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=8) as ex:
+        built = list(ex.map(plan, range(a.batch)))
+    B = dkt.Matrix.batch([m for _, m in built])
+    t_plan = time.perf_counter() - t0
+    tile, tile_ms = B.autotune()
+    off = B.mesh_offsets()
+    b = np.empty(B.n)
+    for k, (da, _) in enumerate(built):
+        bk = dkt.uniform_pm1(1000 + k, da.n)
+        bk[da.boundary_ids()] = 0.0
+        b[off[k]:off[k + 1]] = bk
+    n_elem = int(sum(da.n_elem for da, _ in built))
+    del built
+    bd = torch.from_numpy(b).to(dev)
+    out = {"workload": "%d 3D Q1 Poisson problems, element targets log-uniform in [1e3, %.0e], 1-4 Gaussian "
+                       "clusters (sd 0.05) each; %d elements, %d nodes in one block-diagonal plan"
+                       % (a.batch, a.batch_max_elements, n_elem, B.n),
+           "setup_s": {"meshes_host": t_mesh, "plans": t_plan}, "tile": tile, "tile_product_ms": tile_ms}
+    stream = torch.cuda.current_stream(dev)
+    for name, prec, arith in (("fp64_native", dkt.PREC_FP64, dkt.ARITH_FP64), ("fp64", dkt.PREC_FP64, dkt.ARITH_AUTO),
+                              ("mixed", dkt.PREC_MIXED, dkt.ARITH_AUTO)):
+        B.set_arithmetic(arith)
+        x = torch.zeros_like(bd)
+        B.pcg(bd, x, precision=prec, tol=1e-10, max_iter=32)       # warm-up
+        x.zero_()
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        it, ref, rr, ok = B.pcg(bd, x, precision=prec, tol=1e-10)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        out[name] = {"problems_per_s": a.batch * 1e3 / ms, "ms": ms, "converged": bool(ok),
+                     "max_relres": float(np.max(rr)), "iterations_p50": float(np.percentile(it, 50)),
+                     "iterations_max": int(np.max(it))}
+        if prec == dkt.PREC_MIXED:
+            out[name]["refinements_max"] = int(np.max(ref))
+    out["mixed_over_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    out["mixed_over_fp64_native"] = out["fp64_native"]["ms"] / out["mixed"]["ms"]
+    return out
+
+
+def serve_requests(dkt, n_req, max_elem, rate=200.0, seed=4):
+    """Served stream: Poisson arrivals (mean `rate` per s, numpy PCG64 stream
+    `seed`); dim in {2,3,4} with probabilities 0.3/0.4/0.3; element targets
+    log-uniform in [1e3, max_elem]; half of the meshes refined on a random
+    sphere shell (built on the GPU), half around random point clusters."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    out = []
+    md = {2: 14, 3: 10, 4: 8}
+    for k in range(n_req):
+        dim = int(rng.choice([2, 3, 4], p=[0.3, 0.4, 0.3]))
+        target = float(np.exp(rng.uniform(np.log(1e3), np.log(max_elem))))
+        if rng.uniform() < 0.5:
+            ctr = rng.uniform(0.3, 0.7, dim)
+            rad = float(rng.uniform(0.15, 0.3))
+            level, (c, l) = 2, dkt.sphere_shell_tree(dim, md[dim], 2, ctr, rad)
+            while len(l) < target and level < md[dim]:
+                level += 1
+                c, l = dkt.sphere_shell_tree(dim, md[dim], level, ctr, rad)
+        else:
+            n = max(4, int(target / (2.0 * dim)))
+            c, l = dkt.tree_from_points(dkt.cluster_points(n, dim, md[dim], seed=10000 + k), dim, md[dim])
+        out.append((float(t[k]), dim, md[dim], c, l, 5000 + k))
+    return out
+
+
+def run_serve(a, dkt):
+    """Served request stream through the native request loop (admission
+    against a 150 GB budget, 8 workers, mixed precision) against the same
+    requests solved one after another on the plain FP64 path."""
+    reqs = serve_requests(dkt, a.serve, a.serve_max_elements)
+
+    def play(workers, precision):
+        srv = dkt.Server(workers=workers, budget_bytes=150e9, precision=precision)
+        t_start = time.perf_counter()
+        tickets = []
+        for (t, dim, md, c, l, seed) in reqs:
+            delay = t_start + t - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append((time.perf_counter() - t_start, srv.submit(c, l, dim, md, seed)))
+        res = [(ts, srv.wait(tk, solution=False)) for ts, tk in tickets]
+        wall = time.perf_counter() - t_start
+        srv.close()
+        lat = np.array([r["t_done"] - r["t_submit"] for _, r in res])
+        ok = all(r["rc"] == 0 and r["relres"] <= 1e-10 for _, r in res)
+        return {"requests_per_s": len(res) / wall, "wall_s": wall, "latency_p50_s": float(np.percentile(lat, 50)),
+                "latency_p99_s": float(np.percentile(lat, 99)), "all_converged_1e-10": ok,
+                "max_device_gb": max(r["device_bytes"] for _, r in res) / 1e9}
+
+    out = {"workload": "%d requests, Poisson arrivals at 200/s (seed 4), dim 2/3/4 w.p. 0.3/0.4/0.3, elements "
+                       "log-uniform in [1e3, %.0e], sphere-shell or cluster refinement, Q1 Poisson to 1e-10"
+                       % (a.serve, a.serve_max_elements),
+           "elements_total": int(sum(len(r[4]) for r in reqs))}
+    out["served_mixed"] = play(8, dkt.PREC_MIXED)
+    out["serial_fp64_native"] = play(1, 2)
+    out["serial_fp64"] = play(1, dkt.PREC_FP64)
+    out["served_over_serial_fp64_native"] = (out["served_mixed"]["requests_per_s"]
+                                             / out["serial_fp64_native"]["requests_per_s"])
     return out
 
 
@@ -306,7 +466,7 @@ def run_gpu(a, rank, world, local_rank):
         return
     peak, peak_kind = peaks()
     fixed = a.order == 1
-    kname = "k_matvec_q1fx" if fixed else "k_matvec_leaf"
+    kname = "k_matvec_q1t" if fixed else "k_matvec_leaf"
     dtype = "i64 (exact fixed point, f64 in/out)" if fixed else "f64"
     B = algorithmic_bytes(st, n, npe)
     k_avg_s = (k_ms / max(k_launches, 1)) / 1e3
@@ -330,6 +490,10 @@ def run_gpu(a, rank, world, local_rank):
     }
     if a.solve_level > 0:
         out["solve"] = run_solves(a, dkt, dev)
+    if a.batch > 0:
+        out["batch"] = run_batch(a, dkt, dev)
+    if a.serve > 0:
+        out["serve"] = run_serve(a, dkt)
     if world == 1 and not a.no_cpu_baseline:
         sample_level = min(a.level, 5)
         r, sne, calls, used = cpu_baseline(sample_level, a.order, 1, 3, a.cpu_seconds, procs=1)

@@ -89,6 +89,7 @@ def load(build_if_missing=True):
         "dkt_mesh_moving_ball_device": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
         "dkt_mesh_sphere_shell_device": ([I, I, I, ctypes.c_double, ctypes.c_double, P, P, P, P], I),
         "dkt_mesh_sphere_shell": ([I, I, I, ctypes.c_double, ctypes.c_double, P, P, P, P], I),
+        "dkt_curve_tables": ([I, I, P, P, P], I),
         "dkt_server_create": ([I, ctypes.c_double, I, ctypes.c_double, P], I),
         "dkt_server_submit": ([P, I, I, P, P, I64, ctypes.c_uint64, P], I),
         "dkt_server_wait": ([P, I64, P], I),
@@ -352,6 +353,16 @@ def tree_from_points(points, dim, max_depth, max_pts=1):
     _check(load().dkt_mesh_tree_from_points(_p(pts), pts.shape[0], dim, max_depth, max_pts, ctypes.byref(n),
                                             ctypes.byref(c), ctypes.byref(lv)))
     return _take_cells(n, c, lv, dim)
+
+
+def curve_tables(curve, dim):
+    """(rot, ht) rotation tables of CURVE_MORTON or CURVE_HILBERT for dim 2..4."""
+    rot = np.zeros(192 * 32, np.int8)
+    ht = np.zeros(192 * 16, np.int32)
+    n = ctypes.c_int(0)
+    _check(load().dkt_curve_tables(int(curve), int(dim), _p(rot), _p(ht), ctypes.byref(n)))
+    nc = 1 << dim
+    return rot[:n.value * 2 * nc].copy(), ht[:n.value * nc].copy()
 
 
 def sphere_shell_tree(dim, max_depth, level, centre, radius, halfwidth=None, device=True):

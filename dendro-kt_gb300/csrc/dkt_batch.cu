@@ -72,6 +72,7 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
   if (a.tl_ready) {
     out.tl_off.alloc(nt + 1);
     out.tl_lstart.alloc(nt + 1);
+    out.tl_hb.alloc(nt + 1);
     out.tl_fm.alloc(std::max<int64_t>(nh, 1));
     out.tl_nodes.alloc(std::max<int64_t>(su, 1));
     out.tl_e2l.alloc((size_t) nl * npe);
@@ -91,6 +92,7 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
     if (a.tl_ready) {
       k_offset_i64<<<grid_for(p->tl_n + 1), 256, 0, s>>>(p->tl_off.p, out.tl_off.p + bt, p->tl_n + 1, bu);
       k_offset_i64<<<grid_for(p->tl_n + 1), 256, 0, s>>>(p->tl_lstart.p, out.tl_lstart.p + bt, p->tl_n + 1, bl);
+      k_offset_i64<<<grid_for(p->tl_n), 256, 0, s>>>(p->tl_hb.p, out.tl_hb.p + bt, p->tl_n, bh);
       copy_to(out.tl_fm.p + bh, p->tl_fm.p, (size_t) p->n_hang, s);
       if (p->tl_sum_u)
         k_offset_u32<<<grid_for(p->tl_sum_u), 256, 0, s>>>(p->tl_nodes.p, out.tl_nodes.p + bu, p->tl_sum_u,

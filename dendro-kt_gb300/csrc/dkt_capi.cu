@@ -24,7 +24,7 @@ void diagonal(const Plan &pl, double *diag, cudaStream_t s);
 bool q1fx_setup(Plan &pl, cudaStream_t s);
 void tile_setup(Plan &pl, int T, cudaStream_t s);
 bool tile_size_supported(int dim, int T);
-inline int default_tile(int dim) { return dim == 4 ? 128 : 256; }
+inline int default_tile(int dim) { return dim == 4 ? 64 : 256; }
 void sphere_shell_device(int dim, int md, int level, double R, double w, const double *c, DBuf<uint64_t> &out,
                          int64_t &n_out, cudaStream_t s);
 void moving_ball_device(int md, int level, double R, double w, const double *c0, const double *c1,
@@ -78,10 +78,18 @@ int check_cfg(int dim, int order, int curve, int md)
   if (dim < 2 || dim > 4) return fail(DKT_E_ARG, "dim must be 2, 3 or 4");
   if (order < 1 || order > 2) return fail(DKT_E_UNSUP, "element order must be 1 or 2");
   if (curve != DKT_CURVE_MORTON && curve != DKT_CURVE_HILBERT) return fail(DKT_E_ARG, "unknown curve");
-  if (curve == DKT_CURVE_HILBERT) return fail(DKT_E_UNSUP, "Hilbert ordering is not available in this build");
   if (md < 1 || md > 30) return fail(DKT_E_ARG, "max_depth out of range");
   if (dim * md + 6 > 64) return fail(DKT_E_UNSUP, "dim * max_depth too large (cell keys are 64-bit)");
   return DKT_OK;
+}
+
+void set_curve(dkt::CurveHost &cv, int curve, int dim)
+{
+  if (curve == DKT_CURVE_HILBERT) {
+    dkt::hilbert_tables(dim, cv.rot, cv.ht, cv.nrot);
+  } else {
+    cv.morton(dim);
+  }
 }
 
 void setup_operator(dkt::Plan &pl, int op, const double *tables, cudaStream_t s)
@@ -135,7 +143,7 @@ int dkt_da_create(int dim, int order, int curve, int max_depth, const uint32_t *
     dkt_da_s *h = new dkt_da_s();
     dkt::DA &da = h->da;
     da.dim = dim; da.order = order; da.md = max_depth; da.curve = curve; da.n_elem = n_elem;
-    da.cv.morton(dim);
+    set_curve(da.cv, curve, dim);
     da.cv.upload();
     cudaStream_t s = 0;
     try {
@@ -201,7 +209,7 @@ static int plan_common(int dim, int order, int curve, int md, const uint32_t *no
     pl.conforming = (traversal == DKT_TRAVERSAL_CONFORMING);
     cudaStream_t s = 0;
     dkt::CurveHost cv;
-    cv.morton(dim);
+    set_curve(cv, curve, dim);
     cv.upload();
     const std::vector<double> ip = interp_tables(order);
     dkt::build_plan(pl, node_x_dev, node_lev_dev, n, cv, ip.data(), s);
@@ -582,6 +590,20 @@ int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double 
     *n_out = n;
     *coords = c;
     *levels = l;
+    return DKT_OK;
+  });
+}
+
+int dkt_curve_tables(int curve, int dim, int8_t *rot, int32_t *ht, int *nrot)
+{
+  if (!rot || !ht || !nrot || dim < 2 || dim > 4) return fail(DKT_E_ARG, "bad argument");
+  if (curve != DKT_CURVE_MORTON && curve != DKT_CURVE_HILBERT) return fail(DKT_E_ARG, "unknown curve");
+  return guarded([&]() {
+    dkt::CurveHost cv;
+    set_curve(cv, curve, dim);
+    std::copy(cv.rot.begin(), cv.rot.end(), rot);
+    std::copy(cv.ht.begin(), cv.ht.end(), ht);
+    *nrot = cv.nrot;
     return DKT_OK;
   });
 }

@@ -13,6 +13,7 @@
 //    bucketing.
 //  * the moving-ball spacetime mesh (dim 4).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -396,6 +397,90 @@ static void shell_refine(const Cell &c, int dim, int md, int level, double R, do
     for (int d = 0; d < dim; d++) k.x[d] = c.x[d] | (((ch >> d) & 1) ? cl : 0u);
     shell_refine(k, dim, md, level, R, w, ctr, leaves);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Harmonious Hilbert curve (H. Haverkort, "Harmonious Hilbert curves and other
+// extradimensional space-filling curves", 2012; refinement rule of p. 23).
+//
+// A cell orientation is a symmetry of the cube: an axis permutation followed
+// by a reflection.  Here it is held as its action on the 2^K child indices of
+// a cell (Morton numbers), so composing two orientations is composing two
+// index maps.  The refinement rule says, for the child with curve rank r of
+// a cell in the canonical orientation, where it sits and how it is oriented:
+//   position  g(r) = r xor (r >> 1)                      (reflected Gray code)
+//   mirror    0 for r = 0, else g(r-1) with its last bit set to not(last bit of g(r))
+//   axes      reading the bits of r from the most significant one, a bit that
+//             differs from r's last bit sends its axis to the front block
+//             (filled from the back), the others to the back block
+// (Haverkort numbers bits from the left, so his index i is integer bit K-1-i.)
+// The table for an orientation O then lists, for every rank r, the Morton
+// child O(g(r)) and the orientation O composed with the child's.
+// ---------------------------------------------------------------------------
+namespace {
+using ChildMap = std::array<uint8_t, 16>;   // action on child indices (K <= 4)
+
+ChildMap haverkort_child(int K, unsigned r, unsigned &pos)
+{
+  pos = r ^ (r >> 1);
+  unsigned mirror = 0;
+  if (r > 0) {
+    const unsigned g = (r - 1) ^ ((r - 1) >> 1);
+    mirror = (g & ~1u) | (~pos & 1u);
+  }
+  // destination (Haverkort index, from the left) of every source axis
+  int dest[4];
+  const unsigned last = r & 1u;
+  int front = 0;
+  for (int i = 0; i < K; i++) front += (((r >> (K - 1 - i)) & 1u) != last);
+  int fpos = front - 1, bpos = K - 1;
+  for (int i = 0; i < K; i++) dest[i] = (((r >> (K - 1 - i)) & 1u) != last) ? fpos-- : bpos--;
+  // action: output bit (from the left) i takes input bit dest[i], then the mirror
+  ChildMap m{};
+  for (unsigned x = 0; x < (1u << K); x++) {
+    unsigned y = 0;
+    for (int i = 0; i < K; i++) y = (y << 1) | ((x >> (K - 1 - dest[i])) & 1u);
+    m[x] = (uint8_t) (y ^ mirror);
+  }
+  return m;
+}
+}  // namespace
+
+void hilbert_tables(int K, std::vector<int8_t> &rot, std::vector<int32_t> &ht, int &nrot)
+{
+  if (K < 2 || K > 4) throw std::invalid_argument("Hilbert tables: dim must be 2..4");
+  const unsigned nc = 1u << K;
+  unsigned pos[16];
+  ChildMap child[16];
+  for (unsigned r = 0; r < nc; r++) child[r] = haverkort_child(K, r, pos[r]);
+  ChildMap id{};
+  for (unsigned x = 0; x < nc; x++) id[x] = (uint8_t) x;
+  // every orientation reachable from the identity, numbered in discovery order
+  std::vector<ChildMap> orients{id};
+  auto index_of = [&](const ChildMap &m) -> int {
+    for (size_t k = 0; k < orients.size(); k++)
+      if (std::equal(m.begin(), m.begin() + nc, orients[k].begin())) return (int) k;
+    orients.push_back(m);
+    return (int) orients.size() - 1;
+  };
+  rot.clear();
+  ht.clear();
+  for (size_t o = 0; o < orients.size(); o++) {
+    const ChildMap O = orients[o];
+    std::vector<int8_t> row(2 * nc);
+    std::vector<int32_t> hrow(nc);
+    for (unsigned r = 0; r < nc; r++) {
+      const unsigned morton = O[pos[r]];
+      ChildMap c{};
+      for (unsigned x = 0; x < nc; x++) c[x] = O[child[r][x]];
+      row[r] = (int8_t) morton;
+      row[nc + morton] = (int8_t) r;
+      hrow[morton] = index_of(c);
+    }
+    rot.insert(rot.end(), row.begin(), row.end());
+    ht.insert(ht.end(), hrow.begin(), hrow.end());
+  }
+  nrot = (int) orients.size();
 }
 
 std::vector<Cell> sphere_shell_tree(int dim, int md, int level, double R, double w, const double *ctr)

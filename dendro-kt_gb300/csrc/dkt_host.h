@@ -21,5 +21,9 @@ void gaussian_points(int64_t n, int dim, int md, double mean, double sd, uint64_
 std::vector<Cell> tree_from_points(const uint32_t *pts, int64_t n, int dim, int md, int64_t max_pts);
 std::vector<Cell> moving_ball_tree(int md, int level, double R, double w, const double *c0, const double *c1);
 std::vector<Cell> sphere_shell_tree(int dim, int md, int level, double R, double w, const double *ctr);
+// Rotation tables of the harmonious Hilbert curve: per orientation, 2^dim
+// Morton children in curve order then the curve rank of every Morton child
+// (rot), and the orientation of every Morton child (ht).
+void hilbert_tables(int dim, std::vector<int8_t> &rot, std::vector<int32_t> &ht, int &nrot);
 
 }  // namespace dkt

@@ -154,7 +154,7 @@ struct Plan {
   int64_t n_nodes = 0, n_leaf = 0, n_hang = 0, n_bdry = 0;
   int64_t stale_slots = 0;           // parent slots read unfilled with nonzero weight
   DBuf<int32_t> e2n;                 // [n_leaf][npe]  node index or -1
-  DBuf<uint32_t> info;               // [n_leaf] level | child<<8 | hanging<<16
+  DBuf<uint32_t> info;               // [n_leaf] level | child<<8 | hanging<<16 | rank among the tile's hanging leaves<<17 | reads stale slots<<27
   DBuf<int32_t> hidx;                // [n_leaf] index into hanging arrays or -1
   DBuf<int32_t> p2n;                 // [n_hang][npe] parent node index (level L-1) or -1
   DBuf<uint32_t> fill;               // [n_hang][3] filled-rank bitmask of the leaf
@@ -170,6 +170,10 @@ struct Plan {
   DBuf<int32_t> st_row, st_idx, st_runs, st_hzoff, st_hztab, st_srow, st_sidx, st_gstart;
   DBuf<double> st_w, st_v, st_sw, st_f;
   DBuf<long long> st_vq;
+  DBuf<int32_t> st_hleaves;          // leaves that read stale slots (info bit 27)
+  int64_t st_n_hleaf = 0;
+  cudaStream_t st_stream = nullptr;  // side stream of the chain, with its fork/join events
+  cudaEvent_t st_fork = nullptr, st_join = nullptr;
   // Exact fixed-point path of the Q1 built-in operators (dkt_q1fx.cu).
   int arith = 0;                     // 0 auto, 1 native FP64, 2 fixed point
   bool fx_ready = false;
@@ -186,7 +190,7 @@ struct Plan {
   int tl_T = 0;
   int64_t tl_n = 0, tl_sum_u = 0;
   uint32_t tl_umax = 0;
-  DBuf<int64_t> tl_off, tl_lstart;   // per tile: node-list offset, first leaf
+  DBuf<int64_t> tl_off, tl_lstart, tl_hb;   // per tile: node-list offset, first leaf, first hanging index
   DBuf<uint32_t> tl_nodes, tl_fm;     // distinct nodes (| exclusive flag); reflected fill masks
   DBuf<uint16_t> tl_e2l, tl_p2l;
   // Optional CUDA-event timing of the leaf kernel on its launching stream.
@@ -195,11 +199,23 @@ struct Plan {
   int64_t timed_launches = 0;
   // Kernels this plan's products have launched (all of them, cumulative).
   int64_t n_launch = 0;
+  // mixed-precision solves that finished on the FP64 fallback
+  int64_t fallbacks = 0;
   // batches (dkt_batch.cu): node offset of every mesh, plus the end; empty
   // for a single mesh
   std::vector<int64_t> seg;
   // stale-chain shape: longest run in groups and in entries
   int64_t st_max_run_groups = 0, st_max_run_ents = 0;
+
+  Plan() = default;
+  Plan(const Plan &) = delete;
+  Plan &operator=(const Plan &) = delete;
+  ~Plan()
+  {
+    if (st_stream) cudaStreamDestroy(st_stream);
+    if (st_fork) cudaEventDestroy(st_fork);
+    if (st_join) cudaEventDestroy(st_join);
+  }
 };
 
 }  // namespace dkt

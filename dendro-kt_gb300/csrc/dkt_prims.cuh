@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <atomic>
 #include <vector>
 #include <stdexcept>
 #include <string>
@@ -58,6 +59,23 @@ inline MemCounter &mem_counter()
   return m;
 }
 
+// The device's default memory pool keeps freed blocks for reuse instead of
+// returning them to the driver at every synchronisation (set once per device).
+inline void keep_pool_memory()
+{
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  const unsigned long long bit = 1ull << dev;
+  if (done.load() & bit) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done.fetch_or(bit);
+}
+
 template <typename T>
 struct DBuf {
   T *p = nullptr;
@@ -69,7 +87,13 @@ struct DBuf {
     free();
     n = count;
     if (count) {
-      DKT_CUDA(cudaMalloc(&p, count * sizeof(T)));
+      // Stream-ordered allocation on the calling thread's default stream:
+      // unlike cudaMalloc/cudaFree it never synchronises the whole device,
+      // so threads serving different requests keep the GPU busy together.
+      // The sync makes the block usable on any stream at once.
+      keep_pool_memory();
+      DKT_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&p), count * sizeof(T), cudaStreamPerThread));
+      DKT_CUDA(cudaStreamSynchronize(cudaStreamPerThread));
       MemCounter &m = mem_counter();
       m.cur += (int64_t) (count * sizeof(T));
       if (m.cur > m.peak) m.peak = m.cur;
@@ -78,7 +102,9 @@ struct DBuf {
   void free()
   {
     if (p) {
-      cudaFree(p);
+      // no work on any stream may still use the block (every path in this
+      // library synchronises its streams before its buffers go)
+      cudaFreeAsync(p, cudaStreamPerThread);
       mem_counter().cur -= (int64_t) (n * sizeof(T));
     }
     p = nullptr;

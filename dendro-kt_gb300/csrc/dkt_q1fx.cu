@@ -48,15 +48,18 @@ __global__ void __launch_bounds__(256) k_matvec_q1(
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
     const void *__restrict__ fm, const int *__restrict__ fe, const typename AR::T *__restrict__ xq,
     typename AR::T *__restrict__ yq, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
-    const typename AR::T *__restrict__ stvq, int conforming)
+    const typename AR::T *__restrict__ stvq, int conforming, const int32_t *__restrict__ leaf_list = nullptr,
+    int64_t n_list = 0)
 {
   using T = typename AR::T;
   constexpr int NPE = 1 << DIM, LPL = NPE / 4;
   const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t i = tid / LPL;
+  const int64_t li = tid / LPL;
+  // every leaf, or only the leaves of leaf_list
+  const bool valid = leaf_list ? li < n_list : li < n_leaf;
+  const int64_t i = leaf_list ? (valid ? (int64_t) __ldg(leaf_list + li) : 0) : li;
   const int sub = (int) (tid % LPL);
   const int rb = sub * 4;                      // first rank of this lane
-  const bool valid = i < n_leaf;
   const uint32_t inf = valid ? __ldg(info + i) : 0u;
   const int L = inf & 0xFFu;
   const unsigned child = (inf >> 8) & 0xFFu;
@@ -295,11 +298,23 @@ bool q1fx_setup(Plan &pl, cudaStream_t s)
   return true;
 }
 
-void tiled_fixed(Plan &pl, cudaStream_t s);
+void tiled_fixed(Plan &pl, bool skip_stale, cudaStream_t s);
 void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s);
 
+// The leaves that read stale slots, after the chain (per-leaf kernel).
 template <int DIM>
-static void launch_q1fx(Plan &pl, cudaStream_t s)
+static void launch_q1fx_stale_leaves(Plan &pl, cudaStream_t s)
+{
+  const unsigned threads = 256;
+  k_matvec_q1<DIM, FixedArith><<<grid_for(pl.st_n_hleaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
+      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.fx_fe.p, pl.xq.p,
+      pl.yq.p, pl.st_hzoff.p, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0, pl.st_hleaves.p, pl.st_n_hleaf);
+  check_launch("matvec_q1fx_stale_leaves");
+  pl.n_launch++;
+}
+
+template <int DIM>
+static void launch_q1fx(Plan &pl, bool skip_stale, cudaStream_t s)
 {
   const unsigned threads = 256;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -308,7 +323,7 @@ static void launch_q1fx(Plan &pl, cudaStream_t s)
     DKT_CUDA(cudaEventCreate(&e1));
     DKT_CUDA(cudaEventRecord(e0, s));
   }
-  if (pl.tl_ready) tiled_fixed(pl, s);
+  if (pl.tl_ready) tiled_fixed(pl, skip_stale, s);
   else k_matvec_q1<DIM, FixedArith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.fx_fe.p,
       pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0);
@@ -399,12 +414,36 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
     pl.n_launch++;
   }
   DKT_CUDA(cudaMemsetAsync(pl.yq.p, 0, n * sizeof(long long), s));
-  stale_eval(pl, nullptr, pl.xq.p, s);
+  // With tiles, the stale-buffer chain runs on a side stream while the tiled
+  // kernel does every leaf that does not read stale slots; those few leaves
+  // follow once the chain has joined.
+  const bool split = pl.tl_ready && pl.st_ready && pl.st_n_runs > 0 && pl.st_n_hleaf > 0;
+  if (split) {
+    if (!pl.st_stream) {
+      DKT_CUDA(cudaStreamCreateWithFlags(&pl.st_stream, cudaStreamNonBlocking));
+      DKT_CUDA(cudaEventCreateWithFlags(&pl.st_fork, cudaEventDisableTiming));
+      DKT_CUDA(cudaEventCreateWithFlags(&pl.st_join, cudaEventDisableTiming));
+    }
+    DKT_CUDA(cudaEventRecord(pl.st_fork, s));
+    DKT_CUDA(cudaStreamWaitEvent(pl.st_stream, pl.st_fork, 0));
+    stale_eval(pl, nullptr, pl.xq.p, pl.st_stream);
+    DKT_CUDA(cudaEventRecord(pl.st_join, pl.st_stream));
+  } else {
+    stale_eval(pl, nullptr, pl.xq.p, s);
+  }
   switch (pl.dim) {
-    case 2: launch_q1fx<2>(pl, s); break;
-    case 3: launch_q1fx<3>(pl, s); break;
-    case 4: launch_q1fx<4>(pl, s); break;
+    case 2: launch_q1fx<2>(pl, split, s); break;
+    case 3: launch_q1fx<3>(pl, split, s); break;
+    case 4: launch_q1fx<4>(pl, split, s); break;
     default: throw std::runtime_error("unsupported dim");
+  }
+  if (split) {
+    DKT_CUDA(cudaStreamWaitEvent(s, pl.st_join, 0));
+    switch (pl.dim) {
+      case 2: launch_q1fx_stale_leaves<2>(pl, s); break;
+      case 3: launch_q1fx_stale_leaves<3>(pl, s); break;
+      case 4: launch_q1fx_stale_leaves<4>(pl, s); break;
+    }
   }
   k_from_fixed<<<608, 256, 0, s>>>(pl.yq.p, y, n, pl.fx_sx.p, pl.fx_c);
   check_launch("from_fixed");

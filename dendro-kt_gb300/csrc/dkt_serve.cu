@@ -113,6 +113,7 @@ struct Server {
     try {
       check(dkt_da_create(r.dim, 1, DKT_CURVE_MORTON, r.md, r.coords.data(), r.levels.data(), r.n_elem, 0, &da));
       check(dkt_plan_create_ex(da, DKT_OP_LAPLACE, nullptr, DKT_TRAVERSAL_CONFORMING, &plan));
+      if (precision == 2) check(dkt_plan_set_arithmetic(plan, DKT_ARITH_FP64));
       Plan &pl = plan->pl;
       const int64_t n = pl.n_nodes;
       r.n_nodes = n;
@@ -121,7 +122,8 @@ struct Server {
       if (pl.n_bdry > 0) k_zero_rows<<<grid_for(pl.n_bdry), 256>>>(b.p, pl.bdry.p, pl.n_bdry);
       DKT_CUDA(cudaMemsetAsync(x.p, 0, n * sizeof(double)));
       check_launch("serve_rhs");
-      r.rc = pcg_solve(pl, b.p, x.p, precision, max_iter, tol, true, &r.iters, &r.refinements, &r.relres, 0);
+      r.rc = pcg_solve(pl, b.p, x.p, precision == 1 ? 1 : 0, max_iter, tol, true, &r.iters, &r.refinements,
+                       &r.relres, 0);
       r.x.resize(n);
       DKT_CUDA(cudaMemcpy(r.x.data(), x.p, n * sizeof(double), cudaMemcpyDeviceToHost));
     } catch (const std::exception &e) {
@@ -172,7 +174,7 @@ extern "C" {
 
 int dkt_server_create(int workers, double budget_bytes, int precision, double tol, dkt_server *out)
 {
-  if (!out || workers < 1 || workers > 64 || !(budget_bytes > 0) || precision < 0 || precision > 1 || !(tol > 0)) {
+  if (!out || workers < 1 || workers > 64 || !(budget_bytes > 0) || precision < 0 || precision > 2 || !(tol > 0)) {
     return DKT_E_ARG;
   }
   dkt_server_s *h = new dkt_server_s();

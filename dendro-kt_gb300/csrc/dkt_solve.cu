@@ -17,7 +17,10 @@
 // (fixed-point) product and FP64 vectors, normalises it per mesh, solves
 // A d = r/|r| with binary32 vectors and the binary32 Q1 product to a loose
 // tolerance, and adds |r| d to x in FP64 -- classic iterative refinement, so
-// the final residual is an FP64 residual.
+// the final residual is an FP64 residual.  A refinement step that gains less
+// than 10x on some mesh means binary32 cannot resolve that system (condition
+// number near 1/eps32); the solve then finishes with FP64 PCG from the
+// current x, so it always reaches the tolerance it was given.
 #include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
@@ -260,7 +263,8 @@ struct Cg {
   DBuf<CgScal> sc;
   DBuf<int> n_done;
   std::vector<CgScal> hsc;
-  int *h_done = nullptr;
+  int h_done_v = 0;
+  int *h_done = &h_done_v;   // pageable: pinned memory would cost a device-wide sync to free
   cudaGraphExec_t exec = nullptr;
   T *gx = nullptr, *gr = nullptr;
   const T *gd = nullptr;
@@ -270,12 +274,10 @@ struct Cg {
       : pl(pl_), ch(ch_), n(pl_.n_nodes), z(n), p(n), q(n), part(2 * std::max<int64_t>(ch_.n, 1)), sc(ch_.P),
         n_done(1), hsc(ch_.P)
   {
-    DKT_CUDA(cudaMallocHost(&h_done, sizeof(int)));
   }
   ~Cg()
   {
     if (exec) cudaGraphExecDestroy(exec);
-    if (h_done) cudaFreeHost(h_done);
   }
 
   void iteration(T *x, T *r, const T *dinv, cudaStream_t s)
@@ -382,7 +384,11 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
     DKT_CUDA(cudaMemcpyAsync(hb.data(), bnrm.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
     DKT_CUDA(cudaStreamSynchronize(s));
     for (int p = 0; p < P; p++) if (!(hb[p] > 0.0)) hb[p] = 1.0;
-    if (precision == 0) {
+    // FP64 Jacobi-PCG from the current x on every mesh (meshes already at
+    // tolerance stop at once); used by precision 0 and as the fallback of
+    // the mixed solver
+    int used = 0;
+    auto fp64_pcg = [&](int budget) {
       Cg<double> cg(pl, ch);
       DBuf<double> r(n), stop(P);
       std::vector<double> hs(P);
@@ -391,20 +397,24 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
       fematrix_matvec(pl, x, ax.p, 1.0, s);
       k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
       pl.n_launch++;
-      cg.solve(x, r.p, jacobi ? dinv.p : nullptr, stop.p, 0.0, max_iter, s);
+      cg.solve(x, r.p, jacobi ? dinv.p : nullptr, stop.p, 0.0, budget, s);
       rc = 0;
       for (int p = 0; p < P; p++) {
         const CgScal &q = cg.hsc[p];
-        tot[p] = q.conv_it >= 0 ? q.conv_it : q.it;
+        tot[p] += q.conv_it >= 0 ? q.conv_it : q.it;
         rel[p] = std::sqrt(q.rr) / hb[p];
         if (!(q.done && q.rr <= hs[p])) rc = -5;
       }
+    };
+    if (precision == 0) {
+      fp64_pcg(max_iter);
     } else {
       Cg<float> cg(pl, ch);
       DBuf<float> dx(n), r32(n);
       DBuf<double> r(n);
       const double inner_tol = 1e-5;
-      int used = 0;
+      std::vector<double> prev(P, 0.0);
+      bool stalled = false;
       for (int step = 0; step < 60; step++) {
         fematrix_matvec(pl, x, ax.p, 1.0, s);
         k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
@@ -418,9 +428,13 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           rel[p] = hr[p] / hb[p];
           h_active[p] = rel[p] > tol ? 1 : 0;
           n_active += h_active[p];
+          // a refinement that gains less than 10x means binary32 cannot
+          // resolve this system (condition number near 1/eps32)
+          if (h_active[p] && step > 0 && rel[p] > 0.1 * prev[p]) stalled = true;
+          prev[p] = rel[p];
         }
         if (n_active == 0) { rc = 0; break; }
-        if (used >= max_iter) break;
+        if (used >= max_iter || stalled) break;
         for (int p = 0; p < P; p++) outer[p] += h_active[p];
         active.upload(h_active.data(), P, s);
         // r32 = r / |r| on active meshes, dx = 0, inner solve A dx = r32
@@ -439,6 +453,10 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
         // x += |r| dx on active meshes
         k_add_scaled<<<nb, ST, 0, s>>>(x, dx.p, ch.lo.p, ch.hi.p, ch.prob.p, rnrm.p, active.p);
         pl.n_launch++;
+      }
+      if (rc != 0 && used < max_iter) {
+        fp64_pcg(max_iter - used);
+        pl.fallbacks++;
       }
     }
     check_launch("pcg");

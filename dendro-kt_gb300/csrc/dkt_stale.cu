@@ -171,6 +171,18 @@ void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s)
   pl.st_runs.upload(runs.data(), runs.size(), s);
   pl.st_f.alloc(std::max<int64_t>(n_ent, 1));
   pl.st_hzoff.upload(hz_off.data(), hz_off.size(), s);
+  // leaves that read stale slots: the tiled kernel leaves them to a second,
+  // small launch that runs after the chain (info bit 27 marks them)
+  std::vector<int32_t> hl;
+  for (int64_t i = 0; i < NL; i++)
+    if (hidx[i] >= 0 && hz_off[hidx[i]] >= 0) {
+      hl.push_back((int32_t) i);
+      info[i] |= 1u << 27;
+    }
+  pl.st_n_hleaf = (int64_t) hl.size();
+  if (hl.empty()) hl.push_back(0);
+  pl.st_hleaves.upload(hl.data(), hl.size(), s);
+  DKT_CUDA(cudaMemcpyAsync(pl.info.p, info.data(), NL * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
   pl.st_hztab.upload(hz_tab.data(), hz_tab.size(), s);
   pl.st_v.alloc(std::max<int64_t>(n_ent, 1));
   pl.st_vq.alloc(std::max<int64_t>(n_ent, 1));

@@ -149,6 +149,36 @@ __global__ void k_tile_fmask(const uint32_t *__restrict__ info, const int32_t *_
   for (int k = 0; k < npe; k++) m |= ((f >> (k ^ c)) & 1u) << k;
   fm[h] = m;
 }
+// Per tile: the hanging index of its first hanging leaf (hb), and in bits
+// 17..26 of every hanging leaf's info word its rank among the tile's hanging
+// leaves, so the kernel finds a leaf's hanging records without reading hidx.
+// One CTA of `T` threads per tile.
+__global__ void k_tile_ranks(uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+                             const int64_t *__restrict__ ls, int64_t *__restrict__ hb)
+{
+  __shared__ uint32_t wc[32];
+  const int64_t t = blockIdx.x;
+  const int64_t i = ls[t] + threadIdx.x;
+  const bool valid = i < ls[t + 1];
+  uint32_t inf = valid ? info[i] : 0u;
+  const bool hang = valid && ((inf >> 16) & 1u);
+  const unsigned m = __ballot_sync(0xffffffffu, hang);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wc[w] = __popc(m);
+  __syncthreads();
+  uint32_t r = __popc(m & ((1u << lane) - 1u));
+  for (int k = 0; k < w; k++) r += wc[k];
+  if (threadIdx.x == 0) hb[t] = 0;
+  __syncthreads();
+  constexpr uint32_t RANK = 0x3FFu << 17;
+  if (hang) {
+    info[i] = (inf & ~RANK) | (r << 17);
+    if (r == 0) hb[t] = hidx[i];
+  } else if (valid) {
+    info[i] = inf & ~RANK;
+  }
+}
+
 __global__ void k_tile_lstart(int64_t *__restrict__ ls, int64_t n_tile, int64_t T, int64_t n_leaf)
 {
   const int64_t t = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -199,6 +229,8 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   k_tile_fmask<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.info.p, pl.hidx.p, pl.fill.p, pl.n_leaf, npe, pl.tl_fm.p);
   pl.tl_lstart.alloc(n_tile + 1);
   k_tile_lstart<<<grid_for(n_tile + 1), 256, 0, s>>>(pl.tl_lstart.p, n_tile, T, pl.n_leaf);
+  pl.tl_hb.alloc(n_tile + 1);
+  k_tile_ranks<<<(unsigned) n_tile, T, 0, s>>>(pl.info.p, pl.hidx.p, pl.tl_lstart.p, pl.tl_hb.p);
   check_launch("tile_masks");
   DKT_CUDA(cudaStreamSynchronize(s));
   pl.tl_T = T;
@@ -250,11 +282,11 @@ __device__ __forceinline__ uint32_t idx16(const uint32_t (&w)[NPE / 2], int k)
 template <int DIM, int T_LEAVES, typename AR>
 __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
-    const int32_t *__restrict__ hidx, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
+    const int64_t *__restrict__ tile_hb, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
     const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
     const int *__restrict__ fe, int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
-    int conforming)
+    int conforming, int skip_stale)
 {
   using V = typename AR::T;
   using F = typename AR::Factor;
@@ -263,6 +295,24 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
   const int64_t tile = blockIdx.x;
   const int64_t u0 = tile_off[tile];
   const int U = (int) (tile_off[tile + 1] - u0);
+  const int64_t i = tile_ls[tile] + threadIdx.x;
+  bool valid = i < tile_ls[tile + 1];
+  // the leaf's records first, so their latency overlaps the node gather
+  uint32_t inf = 0, fmask = 0xFFFFFFFFu;
+  uint32_t w[NPE / 2], pw[NPE / 2];
+  int64_t h = -1;
+  if (valid) {
+    inf = __ldg(info + i);
+    if (skip_stale && ((inf >> 27) & 1u)) valid = false;   // done after the stale chain
+  }
+  if (valid) {
+    load_row16<NPE>(e2l + i * NPE, w);
+    if ((inf >> 16) & 1u) {
+      h = tile_hb[tile] + ((inf >> 17) & 0x3FFu);
+      fmask = __ldg(fmask_r + h);
+      load_row16<NPE>(p2l + h * NPE, pw);
+    }
+  }
   F *fac = reinterpret_cast<F *>(smem);
   V *xs = reinterpret_cast<V *>(fac + n_fac);
   V *ys = xs + U;
@@ -273,24 +323,14 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     ys[u] = V(0);
   }
   __syncthreads();
-  const int64_t i = tile_ls[tile] + threadIdx.x;
-  if (i < tile_ls[tile + 1]) {
-    const uint32_t inf = __ldg(info + i);
+  if (valid) {
     const int L = inf & 0xFFu;
-    const bool hang = (inf >> 16) & 1u;
-    uint32_t w[NPE / 2];   // two 16-bit local indices per word
-    load_row16<NPE>(e2l + i * NPE, w);
+    const bool hang = h >= 0;
     auto lidx = [&](int k) -> uint32_t { return idx16<NPE>(w, k); };
     V v[NPE];
-    uint32_t fmask = 0xFFFFFFFFu;
-    int64_t h = -1;
     if (hang) {
-      h = __ldg(hidx + i);
-      fmask = __ldg(fmask_r + h);
       const int c = (int) ((inf >> 8) & 0xFFu);
       const int32_t hz = hzoff ? __ldg(hzoff + h) : -1;
-      uint32_t pw[NPE / 2];
-      load_row16<NPE>(p2l + h * NPE, pw);
 #pragma unroll
       for (int k = 0; k < NPE; k++) {
         const uint32_t p = idx16<NPE>(pw, k);
@@ -340,8 +380,6 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
             v[k] = v[k] + hb;
             v[k | (1 << d)] = hb;
           }
-      uint32_t pw[NPE / 2];
-      load_row16<NPE>(p2l + h * NPE, pw);
 #pragma unroll
       for (int k = 0; k < NPE; k++) {
         const uint32_t p = idx16<NPE>(pw, k);
@@ -360,23 +398,25 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
 
 template <int DIM, int TL, typename AR>
 static void launch_tiled(Plan &pl, const void *fm, const int *fe, const typename AR::T *x, typename AR::T *y,
-                         const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, cudaStream_t s)
+                         const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
+                         cudaStream_t s)
 {
   auto kfn = k_matvec_q1t<DIM, TL, AR>;
   const int n_fac = (pl.md + 1) * (1 << DIM);
   const size_t smem = (size_t) n_fac * sizeof(typename AR::Factor) + (size_t) 2 * pl.tl_umax * sizeof(typename AR::T);
   if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-  kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.hidx.p, pl.tl_fm.p, pl.tl_off.p,
+  kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
                                            pl.tl_lstart.p, pl.tl_nodes.p, fm, fe, n_fac, x, y, hzoff, hztab, stv,
-                                           pl.conforming ? 1 : 0);
+                                           pl.conforming ? 1 : 0, skip_stale ? 1 : 0);
 }
 
 template <typename AR>
 static void launch_tiled_dim(Plan &pl, const void *fm, const int *fe, const typename AR::T *x, typename AR::T *y,
-                             const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, cudaStream_t s)
+                             const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
+                             cudaStream_t s)
 {
 #define DKT_TL_CASE(D, TL) \
-  case (D) * 10000 + (TL): launch_tiled<D, TL, AR>(pl, fm, fe, x, y, hzoff, hztab, stv, s); break;
+  case (D) * 10000 + (TL): launch_tiled<D, TL, AR>(pl, fm, fe, x, y, hzoff, hztab, stv, skip_stale, s); break;
   switch (pl.dim * 10000 + pl.tl_T) {
     DKT_TL_CASE(2, 128) DKT_TL_CASE(2, 256) DKT_TL_CASE(2, 512)
     DKT_TL_CASE(3, 128) DKT_TL_CASE(3, 256) DKT_TL_CASE(3, 512)
@@ -388,15 +428,16 @@ static void launch_tiled_dim(Plan &pl, const void *fm, const int *fe, const type
   pl.n_launch++;
 }
 
-void tiled_fixed(Plan &pl, cudaStream_t s)
+// skip_stale: leave the leaves that read stale slots to a later launch
+void tiled_fixed(Plan &pl, bool skip_stale, cudaStream_t s)
 {
   launch_tiled_dim<FixedArith>(pl, pl.fx_fm.p, pl.fx_fe.p, pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr,
-                               pl.st_hztab.p, pl.st_vq.p, s);
+                               pl.st_hztab.p, pl.st_vq.p, skip_stale, s);
 }
 
 void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
 {
-  launch_tiled_dim<F32Arith>(pl, pl.f32_f.p, nullptr, x, y, nullptr, nullptr, nullptr, s);
+  launch_tiled_dim<F32Arith>(pl, pl.f32_f.p, nullptr, x, y, nullptr, nullptr, nullptr, false, s);
 }
 
 bool tile_size_supported(int dim, int T)

@@ -223,7 +223,7 @@ int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t 
  * (64/128/256 in 4D, 128/256/512 in 2D/3D) share one CTA, a per-tile list of
  * distinct nodes and 16-bit local maps; 0 selects the untiled kernel.  The
  * result does not depend on it (fixed point: bitwise).  A tuning knob with no
- * reference counterpart; plans start with 128 (4D) or 256. */
+ * reference counterpart; plans start with 64 (4D) or 256. */
 int dkt_plan_set_tile(dkt_plan plan, int tile_leaves);
 
 /* Number of kernels this plan's matrix-vector products and solves have
@@ -263,6 +263,8 @@ typedef struct {
   double est_bytes;             /* footprint the admission used */
 } dkt_solve_report;
 
+/* precision: DKT_PREC_FP64, DKT_PREC_MIXED, or 2 = FP64 PCG with the dense
+ * native-FP64 leaf kernel (DKT_ARITH_FP64: the plain FP64 path). */
 int dkt_server_create(int workers, double budget_bytes, int precision, double tol, dkt_server *out);
 /* Copies the tree; returns at once with a ticket. */
 int dkt_server_submit(dkt_server srv, int dim, int max_depth, const uint32_t *tree_coords, const uint8_t *tree_levels,

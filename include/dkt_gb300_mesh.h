@@ -43,6 +43,16 @@ int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double 
  * workload generator of the served request stream (refinement on a random
  * sphere); no reference counterpart beyond SFC_Tree::locTreeBalancing
  * (src/tsort.cpp:826-854) for the balance.  Arrays are freed with dkt_free. */
+/* Rotation tables of a space-filling curve, the data that _InitializeHcurve
+ * (src/KDhcurvedata.cpp:23-57) loads: per orientation, the Morton children
+ * in curve order then the curve rank of every Morton child (rot, 2^(dim+1)
+ * bytes), and the orientation of every Morton child (ht, 2^dim ints).
+ * DKT_CURVE_HILBERT is the harmonious Hilbert curve, generated here from
+ * Haverkort's refinement rule (not copied tables); orientations may be
+ * numbered differently from the reference's, the curve is the same.
+ * Buffers: rot >= 192*32 bytes, ht >= 192*16 ints for dim 4. */
+int dkt_curve_tables(int curve, int dim, int8_t *rot, int32_t *ht, int *nrot);
+
 int dkt_mesh_sphere_shell(int dim, int max_depth, int level, double radius, double halfwidth, const double *centre,
                           int64_t *n_out, uint32_t **coords, uint8_t **levels);   /* host build, same tree */
 int dkt_mesh_sphere_shell_device(int dim, int max_depth, int level, double radius, double halfwidth,

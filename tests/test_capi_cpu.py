@@ -45,7 +45,7 @@ def test_error_codes_without_device(dkt):
     # bad dim, bad order, Hilbert unavailable, misaligned anchor
     assert L.dkt_da_create(5, 1, 0, 10, dkt._p(c), dkt._p(lv), 1, 1, ctypes.byref(h)) == dkt.E_ARG
     assert L.dkt_da_create(3, 3, 0, 10, dkt._p(c), dkt._p(lv), 1, 1, ctypes.byref(h)) == dkt.E_UNSUP
-    assert L.dkt_da_create(3, 1, 1, 10, dkt._p(c), dkt._p(lv), 1, 1, ctypes.byref(h)) == dkt.E_UNSUP
+    assert L.dkt_da_create(3, 1, 7, 10, dkt._p(c), dkt._p(lv), 1, 1, ctypes.byref(h)) == dkt.E_ARG   # unknown curve
     c2 = np.array([[3, 0, 0]], np.uint32)
     lv2 = np.array([2], np.uint8)
     assert L.dkt_da_create(3, 1, 0, 10, dkt._p(c2), dkt._p(lv2), 1, 1, ctypes.byref(h)) == dkt.E_ARG

@@ -16,7 +16,7 @@ import trees
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
-GOLDEN = sorted(g for g in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "morton_*.npz")))
+GOLDEN = sorted(g for g in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 
 
 @pytest.fixture(scope="module")
@@ -45,9 +45,10 @@ def _gpu_mv(A, x, raw=False):
 def test_golden_da_and_matvec(dkt, path):
     g = np.load(path)
     dim, md, order, op = int(g["dim"]), int(g["md"]), int(g["order"]), int(g["op"])
+    curve = dkt.CURVE_HILBERT if os.path.basename(path).startswith("hilbert_") else dkt.CURVE_MORTON
     # shuffle the tree so the device sort is exercised
     perm = np.random.default_rng(0).permutation(g["tree_levels"].size)
-    da = dkt.DA(g["tree_coords"][perm], g["tree_levels"][perm], dim, order=order, max_depth=md)
+    da = dkt.DA(g["tree_coords"][perm], g["tree_levels"][perm], dim, order=order, max_depth=md, curve=curve)
     tc, tl = da.tree()
     assert np.array_equal(tc, g["tree_coords"]) and np.array_equal(tl, g["tree_levels"])
     nc, nl = da.nodes()

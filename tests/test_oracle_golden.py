@@ -49,6 +49,31 @@ def test_oracle_matches_reference(path):
     assert _rel(da.matvec_raw(g["x"]), g["y_raw"]) <= 1e-12
 
 
+@pytest.mark.parametrize("path", HILBERT, ids=[os.path.basename(p)[:-4] for p in HILBERT])
+def test_hilbert_tables_reproduce_reference(path):
+    """The library's own harmonious-Hilbert rotation tables (generated from
+    Haverkort's refinement rule, not taken from the reference), loaded into
+    the oracle, reproduce the reference's Hilbert-ordered trees, DA node
+    order and products."""
+    import __graft_entry__ as ge
+    dkt = ge.load_package()
+    g = np.load(path)
+    dim, md = int(g["dim"]), int(g["md"])
+    rot, ht = dkt.curve_tables(dkt.CURVE_HILBERT, dim)
+    assert ht.size >> dim == {2: 4, 3: 24, 4: 192}[dim]
+    op.set_curve(dim, md, rot, ht)
+    try:
+        tc, tl = _oracle_tree(g)
+        assert np.array_equal(tc, g["tree_coords"]) and np.array_equal(tl, g["tree_levels"])
+        da = op.DA(tc, tl, dim, int(g["order"]), int(g["op"]))
+        assert np.array_equal(da.node_coords, g["node_coords"])
+        assert np.array_equal(da.node_levels, g["node_levels"])
+        assert np.array_equal(da.bdry, g["bdry"])
+        assert _rel(da.matvec(g["x"]), g["y"]) <= 1e-12
+    finally:
+        op.set_curve(dim, md)
+
+
 @pytest.mark.parametrize("ex,dim,L,order", [
     ("1", 2, 5, 1), ("1", 3, 4, 1), ("1", 2, 4, 2), ("2", 2, 4, 1), ("2", 3, 3, 2), ("3", 2, 4, 1), ("3", 3, 4, 1),
     ("1", 4, 3, 1), ("3", 4, 3, 1)])
