@@ -13,14 +13,17 @@
 // converged mesh is frozen (alpha = 0, p kept), so the iterations that run
 // past its convergence change nothing.
 //
-// Mixed precision: the outer loop forms r = b - A x with the exact FP64
-// (fixed-point) product and FP64 vectors, normalises it per mesh, solves
-// A d = r/|r| with binary32 vectors and the binary32 Q1 product to a loose
-// tolerance, and adds |r| d to x in FP64 -- classic iterative refinement, so
-// the final residual is an FP64 residual.  A refinement step that gains less
-// than 10x on some mesh means binary32 cannot resolve that system (condition
-// number near 1/eps32); the solve then finishes with FP64 PCG from the
-// current x, so it always reaches the tolerance it was given.
+// Mixed precision (reliable updates): one Jacobi-PCG sequence runs on
+// binary32 vectors with the binary32 Q1 product, in units of the FP64
+// residual norm at the last update.  Whenever a mesh's recursive residual has
+// fallen 1000x (or claims convergence), the accumulated correction is added
+// to x in FP64, the residual is recomputed exactly (b - A x with the FP64
+// fixed-point product) and replaces the binary32 one, and the search
+// direction is rescaled -- the Krylov space is kept, so the iteration count
+// stays that of FP64 PCG.  Convergence is only ever declared on the FP64
+// residual.  If an update finds the true residual no longer falling (the
+// system is beyond binary32, condition number near 1/eps32), the solve
+// finishes with FP64 PCG from the current x.
 #include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
@@ -306,6 +309,24 @@ struct Cg {
     k_pupd<T><<<nb, ST, 0, s>>>(p.p, z.p, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, 1);
     check_launch("cg_start");
     pl.n_launch += 4;
+    ensure_graph(x, r, dinv, s);
+    int done_iters = 0;
+    for (;;) {
+      DKT_CUDA(cudaMemcpyAsync(h_done, n_done.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      DKT_CUDA(cudaStreamSynchronize(s));
+      if (*h_done >= ch.P || done_iters >= max_iter) break;
+      DKT_CUDA(cudaGraphLaunch(exec, s));
+      pl.n_launch += graph_count;
+      done_iters += CHUNK_IT;
+    }
+    DKT_CUDA(cudaMemcpyAsync(hsc.data(), sc.p, ch.P * sizeof(CgScal), cudaMemcpyDeviceToHost, s));
+    DKT_CUDA(cudaStreamSynchronize(s));
+  }
+
+  // CHUNK_IT iterations captured once into a graph (re-captured when the
+  // vectors change)
+  void ensure_graph(T *x, T *r, const T *dinv, cudaStream_t s)
+  {
     if (exec == nullptr || gx != x || gr != r || gd != dinv) {
       if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
       cudaGraph_t g = nullptr;
@@ -327,19 +348,47 @@ struct Cg {
       DKT_CUDA(e);
       gx = x; gr = r; gd = dinv;
     }
-    int done_iters = 0;
-    for (;;) {
-      DKT_CUDA(cudaMemcpyAsync(h_done, n_done.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-      DKT_CUDA(cudaStreamSynchronize(s));
-      if (*h_done >= ch.P || done_iters >= max_iter) break;
-      DKT_CUDA(cudaGraphLaunch(exec, s));
-      pl.n_launch += graph_count;
-      done_iters += CHUNK_IT;
-    }
-    DKT_CUDA(cudaMemcpyAsync(hsc.data(), sc.p, ch.P * sizeof(CgScal), cudaMemcpyDeviceToHost, s));
-    DKT_CUDA(cudaStreamSynchronize(s));
   }
 };
+
+// Reliable-update kernels (per chunk, per mesh scalars).
+// x += sig[p] * xc on the meshes whose binary32 recursion is finite; xc = 0
+__global__ void k_fold(double *__restrict__ x, float *__restrict__ xc, const int64_t *__restrict__ lo,
+                       const int64_t *__restrict__ hi, const int32_t *__restrict__ prob, const double *__restrict__ sig,
+                       const int *__restrict__ use)
+{
+  const int q = prob[blockIdx.x];
+  const double a = use[q] ? sig[q] : 0.0;
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) {
+    if (a != 0.0) x[i] += a * (double) xc[i];
+    xc[i] = 0.0f;
+  }
+}
+// r32 = r / signew (0 on finished meshes); p *= sig / signew
+__global__ void k_rescale(const double *__restrict__ r, float *__restrict__ r32, float *__restrict__ p,
+                          const int64_t *__restrict__ lo, const int64_t *__restrict__ hi,
+                          const int32_t *__restrict__ prob, const double *__restrict__ sig,
+                          const double *__restrict__ signew, const int *__restrict__ active)
+{
+  const int q = prob[blockIdx.x];
+  const bool on = active[q] && signew[q] > 0.0;
+  const double inv = on ? 1.0 / signew[q] : 0.0;
+  const float ps = on ? (float) (sig[q] / signew[q]) : 0.0f;
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) {
+    r32[i] = (float) (r[i] * inv);
+    p[i] *= ps;
+  }
+}
+// per mesh: finished meshes freeze (done), the others take alpha = 0 for the
+// z / r.z refresh that follows
+__global__ void k_mark(CgScal *__restrict__ sc, const int *__restrict__ active, int P)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P) return;
+  sc[q].alpha = 0.0;
+  sc[q].done = active[q] ? 0 : 1;
+  sc[q].rr_stop = -1.0;   // the binary32 recursion never declares convergence itself
+}
 
 }  // namespace
 
@@ -409,50 +458,106 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
     if (precision == 0) {
       fp64_pcg(max_iter);
     } else {
+      // One binary32 Krylov sequence in units of sig (the FP64 residual norm
+      // at the last reliable update); every few chunks of iterations the
+      // correction is folded into x in FP64 and the true residual replaces
+      // the recursive one (reliable updates), so the Krylov space is kept
+      // across the precision boundary.
       Cg<float> cg(pl, ch);
-      DBuf<float> dx(n), r32(n);
-      DBuf<double> r(n);
-      const double inner_tol = 1e-5;
-      std::vector<double> prev(P, 0.0);
-      bool stalled = false;
-      for (int step = 0; step < 60; step++) {
+      DBuf<float> xc(n), r32(n);
+      DBuf<double> r(n), sig(P), signew(P);
+      DBuf<int> act(P), fold_ok(P);
+      std::vector<double> hsig(P, 0.0);
+      const double delta = 1e-2;      // update once the recursive residual fell by this much
+      int since = 0, updates = 0;
+      DKT_CUDA(cudaMemsetAsync(xc.p, 0, n * sizeof(float), s));
+      auto true_residual = [&]() {
         fematrix_matvec(pl, x, ax.p, 1.0, s);
         k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
         k_dot<double><<<nb, ST, 0, s>>>(r.p, r.p, ch.lo.p, ch.hi.p, part.p);
-        k_norms<<<pgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, rnrm.p);
+        k_norms<<<pgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, signew.p);
         pl.n_launch += 3;
-        DKT_CUDA(cudaMemcpyAsync(hr.data(), rnrm.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
+        DKT_CUDA(cudaMemcpyAsync(hr.data(), signew.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
         DKT_CUDA(cudaStreamSynchronize(s));
         int n_active = 0;
         for (int p = 0; p < P; p++) {
           rel[p] = hr[p] / hb[p];
           h_active[p] = rel[p] > tol ? 1 : 0;
           n_active += h_active[p];
-          // a refinement that gains less than 10x means binary32 cannot
-          // resolve this system (condition number near 1/eps32)
-          if (h_active[p] && step > 0 && rel[p] > 0.1 * prev[p]) stalled = true;
-          prev[p] = rel[p];
         }
-        if (n_active == 0) { rc = 0; break; }
-        if (used >= max_iter || stalled) break;
-        for (int p = 0; p < P; p++) outer[p] += h_active[p];
-        active.upload(h_active.data(), P, s);
-        // r32 = r / |r| on active meshes, dx = 0, inner solve A dx = r32
-        k_scale_down<<<nb, ST, 0, s>>>(r.p, r32.p, ch.lo.p, ch.hi.p, ch.prob.p, rnrm.p, active.p);
-        DKT_CUDA(cudaMemsetAsync(dx.p, 0, n * sizeof(float), s));
-        pl.n_launch++;
-        cg.solve(dx.p, r32.p, jacobi ? dinv32.p : nullptr, nullptr, inner_tol * inner_tol, max_iter - used, s);
-        int most = 0;
-        for (int p = 0; p < P; p++) {
-          const CgScal &q = cg.hsc[p];
-          const int it = q.conv_it >= 0 ? q.conv_it : q.it;
-          if (h_active[p]) tot[p] += it;
-          most = std::max(most, it);
+        act.upload(h_active.data(), P, s);
+        return n_active;
+      };
+      if (true_residual() == 0) {
+        rc = 0;
+      } else {
+        // start: r32 = r / |r|, z, r.z, p = z
+        k_rescale<<<nb, ST, 0, s>>>(r.p, r32.p, cg.p.p, ch.lo.p, ch.hi.p, ch.prob.p, signew.p, signew.p, act.p);
+        DKT_CUDA(cudaMemcpyAsync(sig.p, signew.p, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        k_init_scal<<<pgrid(P), 128, 0, s>>>(cg.sc.p, P, nullptr, -1.0, cg.n_done.p);
+        k_mark<<<pgrid(P), 128, 0, s>>>(cg.sc.p, act.p, P);
+        k_update<float><<<nb, ST, 0, s>>>(xc.p, r32.p, cg.z.p, cg.p.p, cg.q.p, dinv32.p ? dinv32.p : nullptr,
+                                          ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, cg.part.p);
+        k_fin_beta<<<pgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
+        k_pupd<float><<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, 1);
+        pl.n_launch += 6;
+        hsig = hr;
+        cg.ensure_graph(xc.p, r32.p, jacobi ? dinv32.p : nullptr, s);
+        while (used < max_iter) {
+          DKT_CUDA(cudaGraphLaunch(cg.exec, s));
+          pl.n_launch += cg.graph_count;
+          used += CHUNK_IT;
+          since += CHUNK_IT;
+          for (int p = 0; p < P; p++) if (h_active[p]) tot[p] += CHUNK_IT;
+          DKT_CUDA(cudaMemcpyAsync(cg.hsc.data(), cg.sc.p, P * sizeof(CgScal), cudaMemcpyDeviceToHost, s));
+          DKT_CUDA(cudaStreamSynchronize(s));
+          // update when some active mesh's recursive residual fell by delta or
+          // claims convergence, or after 512 iterations without one
+          bool upd = since >= 512, restart = since >= 512;
+          for (int p = 0; p < P; p++) {
+            if (!h_active[p]) continue;
+            const double rr = cg.hsc[p].rr;   // |r32|^2, |r32| = 1 at the last update
+            if (!(rr == rr)) restart = true;
+            if (rr <= delta * delta || std::sqrt(rr) * hsig[p] <= tol * hb[p] || !(rr == rr)) upd = true;
+          }
+          if (!upd) continue;
+          std::vector<double> rec(P);
+          std::vector<int> finite(P);
+          for (int p = 0; p < P; p++) {
+            rec[p] = std::sqrt(cg.hsc[p].rr) * hsig[p];
+            finite[p] = (rec[p] == rec[p]) ? 1 : 0;   // a NaN recursion's correction is dropped
+          }
+          fold_ok.upload(finite.data(), P, s);
+          // reliable update: x += sig * xc, true residual, rescale r32 and p
+          k_fold<<<nb, ST, 0, s>>>(x, xc.p, ch.lo.p, ch.hi.p, ch.prob.p, sig.p, fold_ok.p);
+          pl.n_launch++;
+          updates++;
+          since = 0;
+          for (int p = 0; p < P; p++) outer[p] += h_active[p];
+          if (true_residual() == 0) { rc = 0; break; }
+          k_rescale<<<nb, ST, 0, s>>>(r.p, r32.p, cg.p.p, ch.lo.p, ch.hi.p, ch.prob.p, sig.p, signew.p, act.p);
+          DKT_CUDA(cudaMemcpyAsync(sig.p, signew.p, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
+          k_mark<<<pgrid(P), 128, 0, s>>>(cg.sc.p, act.p, P);
+          k_update<float><<<nb, ST, 0, s>>>(xc.p, r32.p, cg.z.p, cg.p.p, cg.q.p, jacobi ? dinv32.p : nullptr,
+                                            ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, cg.part.p);
+          k_fin_beta<<<pgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
+          pl.n_launch += 4;
+          // the kept direction only fits a residual that the recursion still
+          // tracks; where the true residual is far above the recursive one
+          // (binary32 round-off has taken over), restart from p = z
+          for (int p = 0; p < P; p++)
+            if (h_active[p] && !(hr[p] <= 10.0 * rec[p])) restart = true;
+          if (restart) {
+            k_pupd<float><<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, 1);
+            pl.n_launch++;
+          }
+          // a mesh whose true residual stopped falling is beyond binary32
+          bool stalled = false;
+          for (int p = 0; p < P; p++)
+            if (h_active[p] && hr[p] > 0.5 * hsig[p]) stalled = true;
+          hsig = hr;
+          if (stalled) break;
         }
-        used += std::max(most, 1);
-        // x += |r| dx on active meshes
-        k_add_scaled<<<nb, ST, 0, s>>>(x, dx.p, ch.lo.p, ch.hi.p, ch.prob.p, rnrm.p, active.p);
-        pl.n_launch++;
       }
       if (rc != 0 && used < max_iter) {
         fp64_pcg(max_iter - used);

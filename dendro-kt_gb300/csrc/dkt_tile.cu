@@ -26,6 +26,7 @@
 // modes change sign, so individual roundings of the mode scaling may differ
 // by one unit (2^-50 of max|x|) from the per-leaf kernel.
 #include <algorithm>
+#include <type_traits>
 #include "dkt_internal.cuh"
 #include "dkt_q1.cuh"
 
@@ -257,6 +258,38 @@ __device__ __forceinline__ void wht(T (&v)[1 << DIM])
       }
 }
 
+// Shared-memory accumulation of a tile's outputs.  Fixed point: a 64-bit sum
+// kept as two 32-bit words (low word unsigned, high word signed) updated
+// with native 32-bit shared atomics -- the carry out of the low word is
+// detected from the value the atomic returns and added to the high word --
+// which is exact for any number of contributions and cheaper than 64-bit
+// shared atomics.  Binary32: one float atomic.
+template <typename AR> struct TileAcc;
+template <> struct TileAcc<FixedArith> {
+  static constexpr int WORDS = 2;
+  __device__ static __forceinline__ void zero(uint32_t *a, int U, int u) { a[u] = 0u; a[U + u] = 0u; }
+  __device__ static __forceinline__ void add(uint32_t *a, int U, uint32_t u, long long v)
+  {
+    const uint32_t lo = (uint32_t) (unsigned long long) v;
+    const int hi = (int) (v >> 32);
+    const uint32_t old = atomicAdd(a + u, lo);
+    atomicAdd(reinterpret_cast<int *>(a + U) + u, hi + ((uint32_t) (old + lo) < old ? 1 : 0));
+  }
+  __device__ static __forceinline__ long long get(const uint32_t *a, int U, int u)
+  {
+    return (long long) (((unsigned long long) (uint32_t) a[U + u] << 32) | (unsigned long long) a[u]);
+  }
+};
+template <> struct TileAcc<F32Arith> {
+  static constexpr int WORDS = 1;
+  __device__ static __forceinline__ void zero(uint32_t *a, int, int u) { a[u] = 0u; }
+  __device__ static __forceinline__ void add(uint32_t *a, int, uint32_t u, float v)
+  {
+    atomicAdd(reinterpret_cast<float *>(a) + u, v);
+  }
+  __device__ static __forceinline__ float get(const uint32_t *a, int, int u) { return __uint_as_float(a[u]); }
+};
+
 // One row of NPE 16-bit local indices as NPE/2 packed words (16-byte loads).
 template <int NPE>
 __device__ __forceinline__ void load_row16(const uint16_t *__restrict__ row, uint32_t (&w)[NPE / 2])
@@ -277,6 +310,21 @@ template <int NPE>
 __device__ __forceinline__ uint32_t idx16(const uint32_t (&w)[NPE / 2], int k)
 {
   return (w[k >> 1] >> ((k & 1) * 16)) & 0xFFFFu;
+}
+
+// Transpose of the child-0 interpolation, axes in order (in place).
+template <int DIM, typename AR, typename V>
+__device__ __forceinline__ void transpose_child0(V *v)
+{
+#pragma unroll
+  for (int d = 0; d < DIM; d++)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (1 << d))) {
+        const V hb = AR::half(v[k | (1 << d)]);
+        v[k] = v[k] + hb;
+        v[k | (1 << d)] = hb;
+      }
 }
 
 template <int DIM, int T_LEAVES, typename AR>
@@ -313,21 +361,24 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
       load_row16<NPE>(p2l + h * NPE, pw);
     }
   }
+  using ACC = TileAcc<AR>;
   F *fac = reinterpret_cast<F *>(smem);
   V *xs = reinterpret_cast<V *>(fac + n_fac);
-  V *ys = xs + U;
+  uint32_t *ys = reinterpret_cast<uint32_t *>(xs + U);   // ACC::WORDS words per node
   for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) fac[k] = AR::load_factor(fm, fe, k);
   for (int u = threadIdx.x; u < U; u += T_LEAVES) {
     const uint32_t id = __ldg(tile_nodes + u0 + u) & ~TL_EXCL;
     xs[u] = __ldg(xq + id);
-    ys[u] = V(0);
+    ACC::zero(ys, U, u);
   }
+  __shared__ uint32_t s_max;
+  if (threadIdx.x == 0) s_max = 0u;
   __syncthreads();
+  V v[NPE], zt[std::is_same<AR, FixedArith>::value ? 1 : NPE];
   if (valid) {
     const int L = inf & 0xFFu;
     const bool hang = h >= 0;
     auto lidx = [&](int k) -> uint32_t { return idx16<NPE>(w, k); };
-    V v[NPE];
     if (hang) {
       const int c = (int) ((inf >> 8) & 0xFFu);
       const int32_t hz = hzoff ? __ldg(hzoff + h) : -1;
@@ -361,36 +412,77 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
 #pragma unroll
     for (int k = 0; k < NPE; k++) v[k] = AR::apply(v[k], fac[L * NPE + k]);
     wht<DIM, V>(v);
-#pragma unroll
-    for (int k = 0; k < NPE; k++) {
-      const uint32_t l = lidx(k);
-      if (l != TL_NONE) AR::add(ys + l, v[k]);
-    }
-    if (hang) {
-      // transpose of the child-0 interpolation on the unfilled ranks, into the parent nodes
-#pragma unroll
-      for (int k = 0; k < NPE; k++)
-        if ((fmask >> k) & 1u) v[k] = V(0);
-#pragma unroll
-      for (int d = 0; d < DIM; d++)
-#pragma unroll
-        for (int k = 0; k < NPE; k++)
-          if (!(k & (1 << d))) {
-            const V hb = AR::half(v[k | (1 << d)]);
-            v[k] = v[k] + hb;
-            v[k | (1 << d)] = hb;
-          }
+    if constexpr (std::is_same<AR, FixedArith>::value) {
 #pragma unroll
       for (int k = 0; k < NPE; k++) {
-        const uint32_t p = idx16<NPE>(pw, k);
-        if (p != TL_NONE && (conforming || !((fmask >> k) & 1u))) AR::add(ys + p, v[k]);
+        const uint32_t l = lidx(k);
+        if (l != TL_NONE) ACC::add(ys, U, l, v[k]);
+      }
+      if (hang) {
+        // transpose of the child-0 interpolation on the unfilled ranks, into the parent nodes
+#pragma unroll
+        for (int k = 0; k < NPE; k++)
+          if ((fmask >> k) & 1u) v[k] = V(0);
+        transpose_child0<DIM, AR>(v);
+#pragma unroll
+        for (int k = 0; k < NPE; k++) {
+          const uint32_t p = idx16<NPE>(pw, k);
+          if (p != TL_NONE && (conforming || !((fmask >> k) & 1u))) ACC::add(ys, U, p, v[k]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < NPE; k++) zt[k] = ((fmask >> k) & 1u) || !hang ? V(0) : v[k];
+      if (hang) transpose_child0<DIM, AR>(zt);
+    }
+  }
+  if constexpr (!std::is_same<AR, FixedArith>::value) {
+    // binary32: the tile's contributions are quantised against the tile's
+    // largest one (24 bits, a binary32 rounding) and summed with native
+    // integer shared atomics; each node's sum goes out with one float atomic
+    float m = 0.0f;
+    if (valid) {
+#pragma unroll
+      for (int k = 0; k < NPE; k++) {
+        if (idx16<NPE>(w, k) != TL_NONE) m = fmaxf(m, fabsf(v[k]));
+        m = fmaxf(m, fabsf(zt[k]));
       }
     }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&s_max, __float_as_uint(m));
+    __syncthreads();
+    int e = 0;
+    frexpf(__uint_as_float(s_max), &e);              // max < 2^e
+    const float up = ldexpf(1.0f, 23 - e);
+    if (valid) {
+#pragma unroll
+      for (int k = 0; k < NPE; k++) {
+        const uint32_t l = idx16<NPE>(w, k);
+        if (l != TL_NONE) atomicAdd(reinterpret_cast<int *>(ys) + l, __float2int_rn(v[k] * up));
+      }
+      if (h >= 0) {
+#pragma unroll
+        for (int k = 0; k < NPE; k++) {
+          const uint32_t p = idx16<NPE>(pw, k);
+          if (p != TL_NONE && (conforming || !((fmask >> k) & 1u)))
+            atomicAdd(reinterpret_cast<int *>(ys) + p, __float2int_rn(zt[k] * up));
+        }
+      }
+    }
+    __syncthreads();
+    const float down = ldexpf(1.0f, e - 23);
+    for (int u = threadIdx.x; u < U; u += T_LEAVES) {
+      const uint32_t id = __ldg(tile_nodes + u0 + u);
+      const int a = reinterpret_cast<const int *>(ys)[u];
+      if (id & TL_EXCL) yq[id & ~TL_EXCL] = (V) a * down;
+      else if (a != 0) atomicAdd(yq + id, (V) a * down);
+    }
+    return;
   }
   __syncthreads();
   for (int u = threadIdx.x; u < U; u += T_LEAVES) {
     const uint32_t id = __ldg(tile_nodes + u0 + u);
-    const V a = ys[u];
+    const V a = ACC::get(ys, U, u);
     if (id & TL_EXCL) yq[id & ~TL_EXCL] = a;
     else if (a != V(0)) AR::add(yq + id, a);
   }

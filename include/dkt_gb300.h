@@ -165,10 +165,11 @@ int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter
  * blocks of 16 iterations run as one CUDA graph.  For a batch plan every
  * mesh converges on its own (relative to its own ||b||); iters, refinements
  * and relres are then arrays with one entry per mesh.  DKT_PREC_FP64: Jacobi-PCG
- * in FP64.  DKT_PREC_MIXED: iterative refinement -- FP64 residual
- * b - A x (exact fixed-point product), inner Jacobi-PCG on binary32 vectors
- * with the binary32 Q1 product to 1e-5 relative, FP64 correction of x --
- * repeated until ||b - A x||_2 <= tol ||b||_2 (FP64 residual).  Dot products
+ * in FP64.  DKT_PREC_MIXED: Jacobi-PCG on binary32 vectors with the binary32
+ * Q1 product and reliable updates -- the correction is folded into x in FP64
+ * and the residual recomputed exactly (b - A x, fixed-point product) each
+ * time the binary32 residual has fallen 1000x -- until ||b - A x||_2 <=
+ * tol ||b||_2 (FP64 residual); refinements counts the updates.  Dot products
  * accumulate in FP64 in both.  Mixed needs a Q1 built-in operator without
  * stale parent reads (a conforming plan, or a mesh without them); it is the
  * solver of HeatMat::cgSolve (FEM/examples/src/heatMat.cpp:164-325) with the

@@ -130,3 +130,23 @@ def test_pcg_repeatable_and_graph_free_of_drift(dkt):
         A.pcg(bd, xd, precision=dkt.PREC_FP64, tol=1e-10)
         xs.append(xd.cpu().numpy())
     assert np.array_equal(xs[0], xs[1])
+
+
+def test_mixed_solver_keeps_a_finite_solution(dkt):
+    """A 4D sphere-shell Poisson problem on which the binary32 recursion
+    falls to round-off between two reliable updates: the solver restarts the
+    direction, x stays finite and the FP64 residual reaches 1e-10."""
+    import torch
+    c, l = dkt.sphere_shell_tree(4, 10, 4, (0.5, 0.5, 0.5, 0.5), 0.3)
+    da = dkt.DA(c, l, 4, order=1, max_depth=10)
+    A = dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
+    b = dkt.uniform_pm1(102, da.n)
+    b[da.boundary_ids()] = 0.0
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros_like(bd)
+    it, ref, rr, ok = A.pcg(bd, xd, precision=dkt.PREC_MIXED, tol=1e-10)
+    x = xd.cpu().numpy()
+    assert ok and np.all(np.isfinite(x))
+    ax = torch.empty_like(bd)
+    A.matvec(xd, ax)
+    assert np.linalg.norm(b - ax.cpu().numpy()) <= 2e-10 * np.linalg.norm(b)
