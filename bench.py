@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--level", type=int, default=8)
     ap.add_argument("--order", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-procs", type=int, default=0, help="reference arm: replicas (0: one per host core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solve-level", type=int, default=7,
                     help="moving-ball level of the Poisson solves (FP64 vs mixed PCG); 0 skips them")
@@ -182,7 +183,7 @@ def cpu_baseline(level, order, warmup, steps, seconds, procs=1):
 def run_reference(a, rank, world):
     if rank != 0:
         return
-    cores = os.cpu_count() or 1
+    cores = a.cpu_procs if a.cpu_procs > 0 else (os.cpu_count() or 1)
     sample_level = min(a.level, 5)
     t_start = time.perf_counter()
     value, ne, calls, used = cpu_baseline(sample_level, a.order, a.warmup, a.steps, a.cpu_seconds, procs=cores)
@@ -379,10 +380,14 @@ def run_serve(a, dkt):
         wall = time.perf_counter() - t_start
         srv.close()
         lat = np.array([r["t_done"] - r["t_submit"] for _, r in res])
-        ok = all(r["rc"] == 0 and r["relres"] <= 1e-10 for _, r in res)
-        return {"requests_per_s": len(res) / wall, "wall_s": wall, "latency_p50_s": float(np.percentile(lat, 50)),
-                "latency_p99_s": float(np.percentile(lat, 99)), "all_converged_1e-10": ok,
-                "max_device_gb": max(r["device_bytes"] for _, r in res) / 1e9}
+        bad = [r for _, r in res if not (r["rc"] == 0 and r["relres"] <= 1e-10)]
+        out = {"requests_per_s": len(res) / wall, "wall_s": wall, "latency_p50_s": float(np.percentile(lat, 50)),
+               "latency_p99_s": float(np.percentile(lat, 99)), "all_converged_1e-10": not bad,
+               "max_device_gb": max(r["device_bytes"] for _, r in res) / 1e9}
+        if bad:
+            out["failed"] = len(bad)
+            out["first_failure"] = {"rc": bad[0]["rc"], "relres": bad[0]["relres"], "error": bad[0].get("error", "")}
+        return out
 
     out = {"workload": "%d requests, Poisson arrivals at 200/s (seed 4), dim 2/3/4 w.p. 0.3/0.4/0.3, elements "
                        "log-uniform in [1e3, %.0e], sphere-shell or cluster refinement, Q1 Poisson to 1e-10"
@@ -451,11 +456,11 @@ def run_gpu(a, rank, world, local_rank):
     y_host = torch.empty(n, dtype=torch.float64).pin_memory()
     xh = x_host.numpy()
     for _ in range(2):
-        y_host.numpy()[:] = A.matvec_host(xh)
+        A.matvec_host(xh, out=y_host.numpy())
     barrier()
     e0 = time.perf_counter()
     for _ in range(a.steps):
-        y_host.numpy()[:] = A.matvec_host(xh)
+        A.matvec_host(xh, out=y_host.numpy())
     e_s = time.perf_counter() - e0
     if world > 1:
         t = torch.tensor([e_s], device=dev)

@@ -95,6 +95,7 @@ def load(build_if_missing=True):
         "dkt_server_wait": ([P, I64, P], I),
         "dkt_server_solution": ([P, I64, P, I64], I),
         "dkt_server_release": ([P, I64], I),
+        "dkt_server_error": ([P, I64, P, I], I),
         "dkt_server_destroy": ([P], None),
         "dkt_probe_device": ([P], I),
     }
@@ -240,9 +241,13 @@ class Matrix:
         """feMatrix::matVec that allocates no device memory (fixed 8 MiB scratch per device)."""
         _check(load().dkt_fematrix_matvec_noalloc(self._h, _p(x_dev), _p(y_dev), scale, _stream(stream)))
 
-    def matvec_host(self, x, scale=1.0):
+    def matvec_host(self, x, scale=1.0, out=None):
+        """feMatrix::matVec on host arrays (copies in and out; pass pinned
+        arrays, e.g. from torch's pin_memory, for direct DMA)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
-        y = np.empty(self.n)
+        y = np.empty(self.n) if out is None else out
+        if y.dtype != np.float64 or not y.flags["C_CONTIGUOUS"] or y.size != self.n:
+            raise ValueError("out must be a contiguous float64 array of the plan's size")
         _check(load().dkt_fematrix_matvec_host(self._h, _p(x), _p(y), scale))
         return y
 
@@ -421,6 +426,10 @@ class Server:
         rep = _SolveReport()
         _check(load().dkt_server_wait(self._h, ctypes.c_int64(ticket), ctypes.byref(rep)))
         out = {k: getattr(rep, k) for k, _ in _SolveReport._fields_}
+        if rep.rc not in (OK, E_NOCONV):
+            buf = ctypes.create_string_buffer(512)
+            load().dkt_server_error(self._h, ctypes.c_int64(ticket), buf, 512)
+            out["error"] = buf.value.decode(errors="replace")
         if solution and rep.n_nodes > 0:
             x = np.empty(rep.n_nodes)
             _check(load().dkt_server_solution(self._h, ctypes.c_int64(ticket), _p(x), ctypes.c_int64(x.size)))

@@ -24,7 +24,7 @@ void diagonal(const Plan &pl, double *diag, cudaStream_t s);
 bool q1fx_setup(Plan &pl, cudaStream_t s);
 void tile_setup(Plan &pl, int T, cudaStream_t s);
 bool tile_size_supported(int dim, int T);
-inline int default_tile(int dim) { return dim == 4 ? 64 : 256; }
+inline int default_tile(int dim) { return 256; }
 void sphere_shell_device(int dim, int md, int level, double R, double w, const double *c, DBuf<uint64_t> &out,
                          int64_t &n_out, cudaStream_t s);
 void moving_ball_device(int md, int level, double R, double w, const double *c0, const double *c1,

@@ -199,7 +199,7 @@ static void launch_leaf(Plan &pl, const double *x, double *y, double scale, cuda
                                       nullptr, nullptr, nullptr, nullptr, pl.opTable.p, pl.ip.p, x, y, scale, ST_ARGS);
   } else {
     auto kfn = k_matvec_leaf<DIM, P, false>;
-    if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    ensure_dyn_smem(kfn, smem);
     kfn<<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang,
                                       pl.opA.p, pl.opB.p, pl.opAlpha.p, pl.opBeta.p, nullptr, pl.ip.p, x, y,
                                       pl.op.uses_scale ? scale : 1.0, ST_ARGS);
@@ -305,7 +305,7 @@ static void launch_leaf_noalloc(const Plan &pl, const double *x, double *y, doub
                                                               pl.opTable.p, pl.ip.p, x, y, scale, ST_ARGS);
   } else {
     auto kfn = k_matvec_leaf<DIM, P, false>;
-    if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    ensure_dyn_smem(kfn, smem);
     kfn<<<blocks, threads, smem, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang,
                                       pl.opA.p, pl.opB.p, pl.opAlpha.p, pl.opBeta.p, nullptr, pl.ip.p, x, y,
                                       pl.op.uses_scale ? scale : 1.0, ST_ARGS);

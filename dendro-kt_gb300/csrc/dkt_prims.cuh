@@ -5,6 +5,9 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 #include <stdexcept>
 #include <string>
@@ -48,6 +51,26 @@ template <> __device__ __forceinline__ unsigned key_digit<Key128>(const Key128 &
 }
 
 // Device buffer with RAII.
+// Raises (never lowers) a kernel's dynamic shared-memory limit.  The limit is
+// per function and shared by all host threads, so a thread that lowered it
+// could make another thread's launch with a larger size fail; only raising
+// it, under a lock, keeps every concurrent launch within the limit.
+template <typename F>
+inline void ensure_dyn_smem(F *kfn, size_t bytes)
+{
+  if (bytes <= 48 * 1024) return;
+  static std::mutex m;
+  static std::map<std::pair<int, const void *>, size_t> cur;
+  int dev = 0;
+  DKT_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(m);
+  size_t &c = cur[{dev, reinterpret_cast<const void *>(kfn)}];
+  if (bytes > c) {
+    DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes));
+    c = bytes;
+  }
+}
+
 // Device bytes held through DBuf by the calling host thread (current and
 // peak); a served request reads its own footprint from it.
 struct MemCounter {

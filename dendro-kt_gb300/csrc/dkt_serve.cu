@@ -253,6 +253,20 @@ int dkt_server_solution(dkt_server srv, int64_t ticket, double *x, int64_t cap)
   return DKT_OK;
 }
 
+int dkt_server_error(dkt_server srv, int64_t ticket, char *buf, int capacity)
+{
+  if (!srv || !buf || capacity <= 0) return DKT_E_ARG;
+  dkt::Server &s = srv->s;
+  std::lock_guard<std::mutex> lk(s.m);
+  auto it = s.all.find(ticket);
+  if (it == s.all.end()) return DKT_E_ARG;
+  const std::string &e = it->second->err;
+  const size_t n = std::min<size_t>(e.size(), (size_t) capacity - 1);
+  std::copy(e.begin(), e.begin() + n, buf);
+  buf[n] = '\0';
+  return DKT_OK;
+}
+
 int dkt_server_release(dkt_server srv, int64_t ticket)
 {
   if (!srv) return DKT_E_ARG;

@@ -263,14 +263,36 @@ __global__ void __launch_bounds__(CH_THREADS) k_stale_chain(
     }
     __syncthreads();
     if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
       for (int j = 0; j < cg; j++) {
-        for (int e = gS[j] + (int) threadIdx.x; e < gS[j + 1]; e += 32) {
-          double acc = fS[e];
-          for (int k = rS[e]; k < rS[e + 1]; k++) {
-            const int32_t id = iS[k];
-            acc += wS[k] * (j == 0 ? carry[id - carry_base] : vals[id - e0]);
+        const int ge0 = gS[j], ne = gS[j + 1] - ge0;
+        if (ne <= 16) {
+          // two lanes per entry, each summing every other term, then one shuffle
+          const int e = ge0 + (lane >> 1);
+          const bool on = (lane >> 1) < ne;
+          double acc = 0.0;
+          if (on) {
+            const int k1 = rS[e + 1];
+            if (j == 0) {
+              for (int k = rS[e] + (lane & 1); k < k1; k += 2) acc += wS[k] * carry[iS[k] - carry_base];
+            } else {
+#pragma unroll 4
+              for (int k = rS[e] + (lane & 1); k < k1; k += 2) acc += wS[k] * vals[iS[k] - e0];
+            }
           }
-          vals[e] = acc;
+          acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+          if (on && !(lane & 1)) vals[e] = fS[e] + acc;
+        } else {
+          for (int e = ge0 + lane; e < ge0 + ne; e += 32) {
+            double acc = fS[e];
+            if (j == 0) {
+              for (int k = rS[e]; k < rS[e + 1]; k++) acc += wS[k] * carry[iS[k] - carry_base];
+            } else {
+#pragma unroll 4
+              for (int k = rS[e]; k < rS[e + 1]; k++) acc += wS[k] * vals[iS[k] - e0];
+            }
+            vals[e] = acc;
+          }
         }
         __syncwarp();
       }
@@ -303,14 +325,14 @@ void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
     k_stale_fresh<true><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, nullptr, xq,
                                                            pl.st_f.p);
     auto kfn = k_stale_chain<true>;
-    DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    ensure_dyn_smem(kfn, smem);
     kfn<<<blocks, CH_THREADS, smem, s>>>(pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p,
                                          pl.st_sw.p, pl.st_f.p, pl.st_v.p, pl.st_vq.p, ch_t, npe);
   } else {
     k_stale_fresh<false><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, x, nullptr,
                                                             pl.st_f.p);
     auto kfn = k_stale_chain<false>;
-    DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    ensure_dyn_smem(kfn, smem);
     kfn<<<blocks, CH_THREADS, smem, s>>>(pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p, pl.st_srow.p, pl.st_sidx.p,
                                          pl.st_sw.p, pl.st_f.p, pl.st_v.p, nullptr, ch_t, npe);
   }

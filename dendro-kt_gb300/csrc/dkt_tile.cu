@@ -135,6 +135,48 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(
   }
 }
 
+// Within every tile, hanging leaves first (stable): the warps of a tile then
+// run mostly one code path (a hanging leaf does the interpolation and its
+// transpose, about half again the work).  Leaf order does not matter to the
+// product (integer sums); the hanging records stay indexed by h.
+__global__ void k_tile_partition(const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info,
+                                 const int32_t *__restrict__ hidx, int32_t *__restrict__ e2n_o,
+                                 uint32_t *__restrict__ info_o, int32_t *__restrict__ hidx_o, int64_t n_leaf, int T,
+                                 int npe)
+{
+  __shared__ uint32_t wc[32];
+  const int64_t l0 = (int64_t) blockIdx.x * T;
+  const int64_t i = l0 + threadIdx.x;
+  const bool valid = i < n_leaf;
+  const int nl = (int) (n_leaf - l0 < T ? n_leaf - l0 : T);
+  const bool hang = valid && ((info[i] >> 16) & 1u);
+  const unsigned m = __ballot_sync(0xffffffffu, hang);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wc[w] = __popc(m);
+  __syncthreads();
+  uint32_t before = __popc(m & ((1u << lane) - 1u)), total = 0;
+  for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
+    if (k < w) before += wc[k];
+    total += wc[k];
+  }
+  if (!valid) return;
+  const int64_t j = l0 + (hang ? (int64_t) before : (int64_t) total + (threadIdx.x - before));
+  (void) nl;
+  for (int k = 0; k < npe; k++) e2n_o[j * npe + k] = e2n[i * npe + k];
+  info_o[j] = info[i];
+  hidx_o[j] = hidx[i];
+}
+__global__ void k_flag27(const uint32_t *__restrict__ info, uint32_t *__restrict__ f, int64_t n)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) f[i] = (info[i] >> 27) & 1u;
+}
+__global__ void k_iota_i32(int32_t *__restrict__ v, int64_t n)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (int32_t) i;
+}
+
 // Reflected fill masks: bit k = fill bit (k ^ c) of hanging leaf h (Q1: nPe <= 16).
 __global__ void k_tile_fmask(const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
                              const uint32_t *__restrict__ fill, int64_t n_leaf, int npe, uint32_t *__restrict__ fm)
@@ -198,10 +240,35 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   cap = std::max(cap, TB_THREADS);
   if (cap > 65536) throw std::invalid_argument("tile too large");   // 16-bit local indices
   const int64_t n_tile = (pl.n_leaf + T - 1) / T;
+  if (pl.seg.empty()) {
+    // hanging leaves first within each tile (a single mesh: a batch keeps the
+    // concatenated order of its meshes)
+    DBuf<int32_t> e2n_o((size_t) pl.n_leaf * npe), hidx_o(pl.n_leaf);
+    DBuf<uint32_t> info_o(pl.n_leaf);
+    k_tile_partition<<<(unsigned) n_tile, T, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, e2n_o.p, info_o.p, hidx_o.p,
+                                                     pl.n_leaf, T, npe);
+    check_launch("tile_partition");
+    DKT_CUDA(cudaStreamSynchronize(s));
+    pl.e2n = std::move(e2n_o);
+    pl.info = std::move(info_o);
+    pl.hidx = std::move(hidx_o);
+    if (pl.st_n_hleaf > 0) {
+      // the leaves that read stale slots, renumbered
+      DBuf<uint32_t> f(pl.n_leaf), pos(pl.n_leaf);
+      DBuf<int32_t> iota(pl.n_leaf);
+      k_flag27<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.info.p, f.p, pl.n_leaf);
+      k_iota_i32<<<grid_for(pl.n_leaf), 256, 0, s>>>(iota.p, pl.n_leaf);
+      const int64_t nh = (int64_t) exclusive_scan_total<uint32_t>(f.p, pos.p, pl.n_leaf, s);
+      scatter_if_kernel<int32_t><<<grid_for(pl.n_leaf), 256, 0, s>>>(iota.p, f.p, pos.p, pl.st_hleaves.p, pl.n_leaf);
+      check_launch("stale_leaves");
+      DKT_CUDA(cudaStreamSynchronize(s));
+      if (nh != pl.st_n_hleaf) throw std::runtime_error("stale leaf list changed size");
+    }
+  }
   DBuf<uint32_t> node_tiles(pl.n_nodes), cnt(n_tile);
   DKT_CUDA(cudaMemsetAsync(node_tiles.p, 0, pl.n_nodes * sizeof(uint32_t), s));
   const size_t smem = (size_t) cap * sizeof(uint64_t);
-  DKT_CUDA(cudaFuncSetAttribute(k_tile_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+  ensure_dyn_smem(k_tile_build, smem);
   k_tile_build<<<(unsigned) n_tile, TB_THREADS, smem, s>>>(0, pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.n_leaf,
                                                           npe, T, cap, node_tiles.p, cnt.p, nullptr, nullptr,
                                                           nullptr, nullptr);
@@ -496,7 +563,7 @@ static void launch_tiled(Plan &pl, const void *fm, const int *fe, const typename
   auto kfn = k_matvec_q1t<DIM, TL, AR>;
   const int n_fac = (pl.md + 1) * (1 << DIM);
   const size_t smem = (size_t) n_fac * sizeof(typename AR::Factor) + (size_t) 2 * pl.tl_umax * sizeof(typename AR::T);
-  if (smem > 48 * 1024) DKT_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+  ensure_dyn_smem(kfn, smem);
   kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
                                            pl.tl_lstart.p, pl.tl_nodes.p, fm, fe, n_fac, x, y, hzoff, hztab, stv,
                                            pl.conforming ? 1 : 0, skip_stale ? 1 : 0);

@@ -224,7 +224,7 @@ int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t 
  * (64/128/256 in 4D, 128/256/512 in 2D/3D) share one CTA, a per-tile list of
  * distinct nodes and 16-bit local maps; 0 selects the untiled kernel.  The
  * result does not depend on it (fixed point: bitwise).  A tuning knob with no
- * reference counterpart; plans start with 64 (4D) or 256. */
+ * reference counterpart; plans start with 256. */
 int dkt_plan_set_tile(dkt_plan plan, int tile_leaves);
 
 /* Number of kernels this plan's matrix-vector products and solves have
@@ -274,6 +274,8 @@ int dkt_server_submit(dkt_server srv, int dim, int max_depth, const uint32_t *tr
 int dkt_server_wait(dkt_server srv, int64_t ticket, dkt_solve_report *report);
 /* Copies the solution (n_nodes values, DA node order) of a finished request. */
 int dkt_server_solution(dkt_server srv, int64_t ticket, double *x_host, int64_t capacity);
+/* The error message of a request that failed (empty when it did not). */
+int dkt_server_error(dkt_server srv, int64_t ticket, char *buf, int capacity);
 /* Drops a finished request's stored result. */
 int dkt_server_release(dkt_server srv, int64_t ticket);
 /* Finishes the admitted requests, drops the queued ones, joins the workers. */
