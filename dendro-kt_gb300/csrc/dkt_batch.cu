@@ -79,6 +79,8 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
     out.tl_p2l.alloc((size_t) std::max<int64_t>(nh, 1) * npe);
   }
   out.seg.assign(1, 0);
+  out.lseg.assign(1, 0);
+  std::vector<int32_t> mlo;
   int64_t bn = 0, bl = 0, bh = 0, bb = 0, bt = 0, bu = 0;
   for (const Plan *p : in) {
     const size_t ne = (size_t) p->n_leaf * npe, np_ = (size_t) p->n_hang * npe;
@@ -101,11 +103,16 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
       copy_to(out.tl_p2l.p + bh * npe, p->tl_p2l.p, np_, s);
     }
     check_launch("batch_combine");
+    for (int64_t t = 0; t < p->tl_n; t++) mlo.push_back((int32_t) out.seg.size() - 1);
     bn += p->n_nodes; bl += p->n_leaf; bh += p->n_hang; bb += p->n_bdry; bt += p->tl_n; bu += p->tl_sum_u;
     out.seg.push_back(bn);
+    out.lseg.push_back(bl);
   }
   if (a.tl_ready) {
     out.tl_T = a.tl_T; out.tl_n = nt; out.tl_sum_u = su; out.tl_umax = umax;
+    if (mlo.empty()) mlo.push_back(0);
+    out.tl_mlo.upload(mlo.data(), mlo.size(), s);
+    out.tl_mhi.upload(mlo.data(), mlo.size(), s);   // tiles of one plan never straddle meshes
   }
   DKT_CUDA(cudaStreamSynchronize(s));
   q1fx_setup(out, s);

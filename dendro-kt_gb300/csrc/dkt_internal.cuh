@@ -203,7 +203,12 @@ struct Plan {
   int64_t fallbacks = 0;
   // batches (dkt_batch.cu): node offset of every mesh, plus the end; empty
   // for a single mesh
-  std::vector<int64_t> seg;
+  std::vector<int64_t> seg, lseg;    // node and leaf offsets of the meshes
+  DBuf<int32_t> tl_mlo, tl_mhi;      // per tile: first and last mesh it covers (batches)
+  // While a batched solve captures its iterations: per-mesh converged flags
+  // (stride in ints); tiles whose meshes have all converged are skipped.
+  const int *skip_mesh = nullptr;
+  int skip_stride = 1;
   // stale-chain shape: longest run in groups and in entries
   int64_t st_max_run_groups = 0, st_max_run_ents = 0;
 

@@ -94,9 +94,15 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
 template <typename T>
 __global__ void __launch_bounds__(ST) k_dot(const T *__restrict__ a, const T *__restrict__ b,
                                            const int64_t *__restrict__ lo, const int64_t *__restrict__ hi,
-                                           double *__restrict__ part)
+                                           double *__restrict__ part, const int *__restrict__ skip = nullptr,
+                                           const int32_t *__restrict__ prob = nullptr, int stride = 1)
 {
   __shared__ double sh[ST / 32];
+  // chunks of converged meshes contribute nothing (their sums are not used)
+  if (skip && skip[(int64_t) prob[blockIdx.x] * stride]) {
+    if (threadIdx.x == 0) part[blockIdx.x] = 0.0;
+    return;
+  }
   double s = 0.0;
   for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) s += (double) a[i] * (double) b[i];
   s = block_sum(s, sh);
@@ -132,6 +138,10 @@ __global__ void __launch_bounds__(ST) k_update(T *__restrict__ x, T *__restrict_
                                               const CgScal *__restrict__ sc, double *__restrict__ part)
 {
   __shared__ double sh[ST / 32];
+  if (sc[prob[blockIdx.x]].done) {   // a converged mesh: frozen, its sums unused
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = 0.0; part[2 * blockIdx.x + 1] = 0.0; }
+    return;
+  }
   const double a = sc[prob[blockIdx.x]].alpha;
   const T at = (T) a;
   double srz = 0.0, srr = 0.0;
@@ -287,7 +297,8 @@ struct Cg {
   {
     const unsigned nb = (unsigned) ch.n;
     CgOp<T>::apply(pl, p.p, q.p, s);
-    k_dot<T><<<nb, ST, 0, s>>>(p.p, q.p, ch.lo.p, ch.hi.p, part.p);
+    k_dot<T><<<nb, ST, 0, s>>>(p.p, q.p, ch.lo.p, ch.hi.p, part.p, &sc.p[0].done, ch.prob.p,
+                               (int) (sizeof(CgScal) / sizeof(int)));
     k_fin_alpha<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p);
     k_update<T><<<nb, ST, 0, s>>>(x, r, z.p, p.p, q.p, dinv, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, part.p);
     k_fin_beta<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 1, n_done.p);
@@ -331,6 +342,9 @@ struct Cg {
       if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
       cudaGraph_t g = nullptr;
       const int64_t before = pl.n_launch;
+      // products inside the iterations skip the tiles of converged meshes
+      pl.skip_mesh = ch.P > 1 ? &sc.p[0].done : nullptr;
+      pl.skip_stride = (int) (sizeof(CgScal) / sizeof(int));
       DKT_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       try {
         for (int k = 0; k < CHUNK_IT; k++) iteration(x, r, dinv, s);
@@ -338,8 +352,10 @@ struct Cg {
         cudaStreamEndCapture(s, &g);
         if (g) cudaGraphDestroy(g);
         pl.n_launch = before;
+        pl.skip_mesh = nullptr;
         throw;
       }
+      pl.skip_mesh = nullptr;
       DKT_CUDA(cudaStreamEndCapture(s, &g));
       graph_count = pl.n_launch - before;
       pl.n_launch = before;

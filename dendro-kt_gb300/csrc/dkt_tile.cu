@@ -301,6 +301,17 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   k_tile_ranks<<<(unsigned) n_tile, T, 0, s>>>(pl.info.p, pl.hidx.p, pl.tl_lstart.p, pl.tl_hb.p);
   check_launch("tile_masks");
   DKT_CUDA(cudaStreamSynchronize(s));
+  if (pl.lseg.size() >= 2) {
+    // a re-tiled batch: the meshes each tile covers
+    std::vector<int32_t> lo(n_tile), hi(n_tile);
+    for (int64_t t = 0; t < n_tile; t++) {
+      const int64_t a = t * T, b = std::min<int64_t>((t + 1) * T, pl.n_leaf) - 1;
+      lo[t] = (int32_t) (std::upper_bound(pl.lseg.begin(), pl.lseg.end(), a) - pl.lseg.begin() - 1);
+      hi[t] = (int32_t) (std::upper_bound(pl.lseg.begin(), pl.lseg.end(), b) - pl.lseg.begin() - 1);
+    }
+    pl.tl_mlo.upload(lo.data(), lo.size(), s);
+    pl.tl_mhi.upload(hi.data(), hi.size(), s);
+  }
   pl.tl_T = T;
   pl.tl_n = n_tile;
   pl.tl_umax = umax;
@@ -401,13 +412,18 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
     const int *__restrict__ fe, int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
-    int conforming, int skip_stale)
+    int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
+    const int *__restrict__ skip_mesh, int skip_stride)
 {
   using V = typename AR::T;
   using F = typename AR::Factor;
   constexpr int NPE = 1 << DIM;
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t tile = blockIdx.x;
+  // a batched solve: tiles whose meshes have all converged are not needed
+  if (skip_mesh && skip_mesh[(int64_t) tile_mlo[tile] * skip_stride] &&
+      skip_mesh[(int64_t) tile_mhi[tile] * skip_stride])
+    return;
   const int64_t u0 = tile_off[tile];
   const int U = (int) (tile_off[tile + 1] - u0);
   const int64_t i = tile_ls[tile] + threadIdx.x;
@@ -566,7 +582,8 @@ static void launch_tiled(Plan &pl, const void *fm, const int *fe, const typename
   ensure_dyn_smem(kfn, smem);
   kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
                                            pl.tl_lstart.p, pl.tl_nodes.p, fm, fe, n_fac, x, y, hzoff, hztab, stv,
-                                           pl.conforming ? 1 : 0, skip_stale ? 1 : 0);
+                                           pl.conforming ? 1 : 0, skip_stale ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p,
+                                           pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride);
 }
 
 template <typename AR>
