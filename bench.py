@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--batch", type=int, default=512, help="problems in the batched 3D Poisson solve; 0 skips it")
     ap.add_argument("--batch-max-elements", type=float, default=1e6)
     ap.add_argument("--serve", type=int, default=48, help="requests in the served stream; 0 skips it")
-    ap.add_argument("--serve-max-elements", type=float, default=5e5)
+    ap.add_argument("--serve-max-elements", type=float, default=5e6)
     return ap.parse_args()
 
 

@@ -17,6 +17,7 @@
 // Scales: x is stored as xq = round(x * 2^sx) with |xq| <= 2^(60-dim); the
 // per-mode factors carry 2^c so that every contribution stays below
 // 2^(54-dim) and a node can absorb 256 of them; y = yq * 2^-(sx+c).
+#include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
 #include "dkt_q1.cuh"
@@ -182,36 +183,63 @@ __global__ void __launch_bounds__(256) k_matvec_q1(
   }
 }
 
-// max |x| (as the bit pattern of a non-negative double, so integer atomicMax orders it)
-__global__ void k_absmax(const double *__restrict__ x, int64_t n, unsigned long long *__restrict__ out)
+// max |x| (as the bit pattern of a non-negative double, so integer atomicMax
+// orders it): grid-stride loads four apart, a block reduction, one atomic per block.
+__global__ void __launch_bounds__(256) k_absmax(const double *__restrict__ x, int64_t n,
+                                                unsigned long long *__restrict__ out)
 {
+  __shared__ double sh[8];
   double m = 0.0;
-  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x)
-    m = fmax(m, fabs(x[i]));
+  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    const double a = fabs(x[i]), b = fabs(x[i + stride]), c = fabs(x[i + 2 * stride]), d = fabs(x[i + 3 * stride]);
+    m = fmax(m, fmax(fmax(a, b), fmax(c, d)));
+  }
+  for (; i < n; i += stride) m = fmax(m, fabs(x[i]));
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long) __double_as_longlong(m));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int) (blockDim.x >> 5); w++) m = fmax(m, sh[w]);
+    atomicMax(out, (unsigned long long) __double_as_longlong(m));
+  }
 }
 
-// xq = round(x * 2^sx), sx from max|x| (device scalar); boundary entries zeroed
-// when ids are given (feMatrix pre-matvec).
-__global__ void k_to_fixed(const double *__restrict__ x, long long *__restrict__ xq, int64_t n,
-                           const unsigned long long *__restrict__ amax, int *__restrict__ sx_out, int dim)
+// sx from max|x|: xq = round(x * 2^sx) keeps |xq| <= 2^(60-dim)
+__device__ __forceinline__ int fixed_exponent(const unsigned long long *amax, int dim)
 {
   const double m = __longlong_as_double((long long) *amax);
   int e = 0;
   if (m > 0.0) frexp(m, &e);   // m < 2^e
-  const int sx = (60 - dim) - e;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *sx_out = sx;
-  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x)
-    xq[i] = __double2ll_rn(ldexp(x[i], sx));
+  return (60 - dim) - e;
+}
+
+// x * 2^k as two exact power-of-two products (no intermediate overflow for
+// |k| <= 2046); equal to ldexp(x, k) for every finite x
+__device__ __forceinline__ double scale2(double x, int k)
+{
+  const int h = k / 2;
+  return (x * __longlong_as_double((long long) (1023 + h) << 52)) *
+         __longlong_as_double((long long) (1023 + (k - h)) << 52);
+}
+
+// xq = round(x * 2^sx), one element per thread
+__global__ void k_to_fixed(const double *__restrict__ x, long long *__restrict__ xq, int64_t n,
+                           const unsigned long long *__restrict__ amax, int *__restrict__ sx_out, int dim)
+{
+  const int sx = fixed_exponent(amax, dim);
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *sx_out = sx;
+  if (i < n) xq[i] = __double2ll_rn(scale2(x[i], sx));
 }
 
 __global__ void k_from_fixed(const long long *__restrict__ yq, double *__restrict__ y, int64_t n,
                              const int *__restrict__ sx, int c)
 {
   const int sh = -(*sx + c);
-  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x)
-    y[i] = ldexp((double) yq[i], sh);
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = scale2((double) yq[i], sh);
 }
 
 __global__ void k_zero_ids_ll(long long *__restrict__ v, const uint32_t *__restrict__ ids, int64_t nb)
@@ -404,8 +432,8 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
 {
   const int64_t n = pl.n_nodes;
   DKT_CUDA(cudaMemsetAsync(pl.fx_amax.p, 0, sizeof(unsigned long long), s));
-  k_absmax<<<608, 256, 0, s>>>(x, n, pl.fx_amax.p);
-  k_to_fixed<<<608, 256, 0, s>>>(x, pl.xq.p, n, pl.fx_amax.p, pl.fx_sx.p, pl.dim);
+  k_absmax<<<std::max<unsigned>(1u, std::min<unsigned>(grid_for(n, 1024), 152 * 8)), 256, 0, s>>>(x, n, pl.fx_amax.p);
+  k_to_fixed<<<grid_for(n), 256, 0, s>>>(x, pl.xq.p, n, pl.fx_amax.p, pl.fx_sx.p, pl.dim);
   check_launch("to_fixed");
   pl.n_launch += 2;
   if (bc && pl.n_bdry > 0) {
@@ -445,7 +473,7 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
       case 4: launch_q1fx_stale_leaves<4>(pl, s); break;
     }
   }
-  k_from_fixed<<<608, 256, 0, s>>>(pl.yq.p, y, n, pl.fx_sx.p, pl.fx_c);
+  k_from_fixed<<<grid_for(n), 256, 0, s>>>(pl.yq.p, y, n, pl.fx_sx.p, pl.fx_c);
   check_launch("from_fixed");
   pl.n_launch++;
   if (bc && pl.n_bdry > 0) {

@@ -213,7 +213,7 @@ __global__ void k_stale_fresh(int64_t n_ent, const int32_t *__restrict__ row, co
 // every term refers to the previous group, whose values are in shared
 // memory), then the block writes the chunk's values out.  The walk touches
 // shared memory only, so a step costs a few shared-memory latencies.
-constexpr int CH_E = 512;      // entries per chunk
+constexpr int CH_E = 256;      // entries per chunk
 constexpr int CH_G = 128;      // groups per chunk
 constexpr int CH_THREADS = 128;
 static_assert(CH_G == CH_THREADS, "one group test per thread");
@@ -317,7 +317,9 @@ void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
   if (!pl.st_ready || pl.st_n_runs == 0) return;
   const int64_t ne = pl.st_n_ent;
   const int npe = pl.npe;
-  const int ch_t = std::max(4096, npe * npe);
+  // small chunks keep the block's shared memory (~18 KB for Q1) low, so the
+  // chain coexists with the tiled kernel it overlaps
+  const int ch_t = std::max(1024, npe * npe);
   const size_t smem = (size_t) ch_t * 12 + (size_t) 2 * CH_E * 8 + (size_t) npe * 8 + (size_t) (CH_E + 1) * 4
                       + (size_t) (CH_G + 1) * 4 + 64;
   const unsigned blocks = (unsigned) pl.st_n_runs;

@@ -339,3 +339,26 @@ def test_device_sphere_shell_equals_host(dkt):
         dc, dl = dkt.sphere_shell_tree(dim, 10, level, ctr, 0.3, device=True)
         key = lambda c, l: sorted(map(tuple, np.concatenate([c.astype(np.int64), l[:, None].astype(np.int64)], 1)))
         assert len(hl) == len(dl) and key(hc, hl) == key(dc, dl), dim
+
+
+@pytest.mark.parametrize("dim,npts,md,order", [(2, 3000, 12, 1), (3, 6000, 10, 1), (3, 1500, 10, 2), (4, 800, 8, 1)])
+def test_hilbert_meshes_vs_oracle(dkt, dim, npts, md, order):
+    """Hilbert-ordered Gaussian meshes: device tree order, DA node order and
+    product against the oracle running the same (generated) curve tables."""
+    pts = dkt.gaussian_points(npts, dim, md, seed=11)
+    tc, tl = dkt.tree_from_points(pts, dim, md)
+    da = dkt.DA(tc, tl, dim, order=order, max_depth=md, curve=dkt.CURVE_HILBERT)
+    rot, ht = dkt.curve_tables(dkt.CURVE_HILBERT, dim)
+    orc.set_curve(dim, md, rot, ht)
+    try:
+        sc, sl = orc.tree_sort(tc, tl, dim)
+        c, lv = da.tree()
+        assert np.array_equal(c, sc) and np.array_equal(lv, sl)
+        ora = orc.DA(sc, sl, dim, order, 2)
+        nc, nl = da.nodes()
+        assert np.array_equal(nc, ora.node_coords) and np.array_equal(nl, ora.node_levels)
+        A = dkt.Matrix(da, op=dkt.OP_LAPMASS)   # the plan takes the DA's curve
+        x = dkt.uniform_pm1(12, da.n)
+        assert _rel(_gpu_mv(A, x), ora.matvec(x)) <= TOL
+    finally:
+        orc.set_curve(dim, md)
