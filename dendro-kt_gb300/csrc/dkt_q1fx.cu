@@ -448,7 +448,11 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
   const bool split = pl.tl_ready && pl.st_ready && pl.st_n_runs > 0 && pl.st_n_hleaf > 0;
   if (split) {
     if (!pl.st_stream) {
-      DKT_CUDA(cudaStreamCreateWithFlags(&pl.st_stream, cudaStreamNonBlocking));
+      // highest priority: the chain's few, long, latency-bound blocks start at
+      // once and the tiled kernel fills the rest of the machine around them
+      int lo = 0, hi = 0;
+      DKT_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      DKT_CUDA(cudaStreamCreateWithPriority(&pl.st_stream, cudaStreamNonBlocking, hi));
       DKT_CUDA(cudaEventCreateWithFlags(&pl.st_fork, cudaEventDisableTiming));
       DKT_CUDA(cudaEventCreateWithFlags(&pl.st_join, cudaEventDisableTiming));
     }
