@@ -183,45 +183,102 @@ __global__ void __launch_bounds__(256) k_matvec_q1(
   }
 }
 
-// max |x| (as the bit pattern of a non-negative double, so integer atomicMax
-// orders it): grid-stride loads four apart, a block reduction, one atomic per block.
+// The passes between FP64 and fixed point run on the integer pipes: GB300
+// executes FP64 (and FP64 conversions) at a small fraction of its integer
+// rate, enough to make these memory-bound passes compute-bound otherwise.
+
+// max |x|: the largest bit pattern of |x| (non-negative doubles order as
+// integers): grid-stride loads four apart, a block reduction, one atomic per block.
 __global__ void __launch_bounds__(256) k_absmax(const double *__restrict__ x, int64_t n,
                                                 unsigned long long *__restrict__ out)
 {
-  __shared__ double sh[8];
-  double m = 0.0;
+  __shared__ unsigned long long sh[8];
+  constexpr unsigned long long ABS = 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long *xb = reinterpret_cast<const unsigned long long *>(x);
+  unsigned long long m = 0;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   for (; i + 3 * stride < n; i += 4 * stride) {
-    const double a = fabs(x[i]), b = fabs(x[i + stride]), c = fabs(x[i + 2 * stride]), d = fabs(x[i + 3 * stride]);
-    m = fmax(m, fmax(fmax(a, b), fmax(c, d)));
+    const unsigned long long a = xb[i] & ABS, b = xb[i + stride] & ABS, c = xb[i + 2 * stride] & ABS,
+                             d = xb[i + 3 * stride] & ABS;
+    m = max(m, max(max(a, b), max(c, d)));
   }
-  for (; i < n; i += stride) m = fmax(m, fabs(x[i]));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  for (; i < n; i += stride) m = max(m, xb[i] & ABS);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < (int) (blockDim.x >> 5); w++) m = fmax(m, sh[w]);
-    atomicMax(out, (unsigned long long) __double_as_longlong(m));
+    for (int w = 1; w < (int) (blockDim.x >> 5); w++) m = max(m, sh[w]);
+    atomicMax(out, m);
   }
 }
 
 // sx from max|x|: xq = round(x * 2^sx) keeps |xq| <= 2^(60-dim)
 __device__ __forceinline__ int fixed_exponent(const unsigned long long *amax, int dim)
 {
-  const double m = __longlong_as_double((long long) *amax);
-  int e = 0;
-  if (m > 0.0) frexp(m, &e);   // m < 2^e
+  const unsigned long long b = *amax;
+  if (b == 0) return 60 - dim;
+  const int ef = (int) (b >> 52);                       // biased exponent (|x| finite)
+  const int e = ef == 0 ? -1010 - __clzll(b) : ef - 1022;   // max|x| < 2^e, as frexp
   return (60 - dim) - e;
 }
 
-// x * 2^k as two exact power-of-two products (no intermediate overflow for
-// |k| <= 2046); equal to ldexp(x, k) for every finite x
+// x * 2^k as two exact power-of-two products (|k| <= 2046); ldexp(x, k)
 __device__ __forceinline__ double scale2(double x, int k)
 {
   const int h = k / 2;
   return (x * __longlong_as_double((long long) (1023 + h) << 52)) *
          __longlong_as_double((long long) (1023 + (k - h)) << 52);
+}
+
+// round(x * 2^sx) to nearest even, in integer arithmetic (|result| < 2^63)
+__device__ __forceinline__ long long fixed_from_double(double x, int sx)
+{
+  const unsigned long long b = (unsigned long long) __double_as_longlong(x);
+  const int ef = (int) ((b >> 52) & 0x7FF);
+  unsigned long long m = b & ((1ull << 52) - 1);
+  int e;                                                // |x| = m * 2^e
+  if (ef == 0) e = -1074;
+  else { m |= 1ull << 52; e = ef - 1075; }
+  const int k = e + sx;
+  unsigned long long q;
+  if (m == 0 || k < -63) q = 0;
+  else if (k >= 0) q = m << k;
+  else {
+    const int r = -k;
+    q = m >> r;
+    const unsigned long long rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+    if (rem > half || (rem == half && (q & 1ull))) q++;
+  }
+  return (b >> 63) ? -(long long) q : (long long) q;
+}
+
+// (double) v * 2^sh: the int64 -> double rounding (to nearest even) and the
+// exponent, in integer arithmetic; results outside the normal range take
+// the FP64 path
+__device__ __forceinline__ double double_from_fixed(long long v, int sh)
+{
+  if (v == 0) return 0.0;
+  const bool neg = v < 0;
+  const unsigned long long a = neg ? 0ull - (unsigned long long) v : (unsigned long long) v;
+  const int msb = 63 - __clzll(a);
+  unsigned long long m;
+  int e = msb;
+  if (msb <= 52) {
+    m = a << (52 - msb);
+  } else {
+    const int r = msb - 52;
+    m = a >> r;
+    const unsigned long long rem = a & ((1ull << r) - 1), half = 1ull << (r - 1);
+    if (rem > half || (rem == half && (m & 1ull))) {
+      m++;
+      if (m == (1ull << 53)) { m >>= 1; e++; }
+    }
+  }
+  const int be = e + sh + 1023;
+  if (be <= 0 || be >= 2047) return scale2((double) v, sh);
+  return __longlong_as_double((long long) (((unsigned long long) neg << 63) | ((unsigned long long) be << 52) |
+                                           (m & ((1ull << 52) - 1))));
 }
 
 // xq = round(x * 2^sx), one element per thread
@@ -231,7 +288,7 @@ __global__ void k_to_fixed(const double *__restrict__ x, long long *__restrict__
   const int sx = fixed_exponent(amax, dim);
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) *sx_out = sx;
-  if (i < n) xq[i] = __double2ll_rn(scale2(x[i], sx));
+  if (i < n) xq[i] = fixed_from_double(x[i], sx);
 }
 
 __global__ void k_from_fixed(const long long *__restrict__ yq, double *__restrict__ y, int64_t n,
@@ -239,7 +296,7 @@ __global__ void k_from_fixed(const long long *__restrict__ yq, double *__restric
 {
   const int sh = -(*sx + c);
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = scale2((double) yq[i], sh);
+  if (i < n) y[i] = double_from_fixed(yq[i], sh);
 }
 
 __global__ void k_zero_ids_ll(long long *__restrict__ v, const uint32_t *__restrict__ ids, int64_t nb)
