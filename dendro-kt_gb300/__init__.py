@@ -16,7 +16,7 @@ _lib = None
 
 OK, E_ARG, E_CUDA, E_NOMEM, E_UNSUP, E_NOCONV, E_INTERNAL = 0, -1, -2, -3, -4, -5, -6
 CURVE_MORTON, CURVE_HILBERT = 0, 1
-OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM, OP_LAPLACE, OP_MASS = 0, 1, 2, 3, 4, 5
+OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM, OP_LAPLACE, OP_MASS, OP_HEATVEC = 0, 1, 2, 3, 4, 5, 6
 ARITH_AUTO, ARITH_FP64, ARITH_FIXED = 0, 1, 2
 TRAVERSAL_REFERENCE, TRAVERSAL_CONFORMING = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -68,6 +68,7 @@ def load(build_if_missing=True):
         "dkt_fematrix_matvec": ([P, P, P, ctypes.c_double, P], I),
         "dkt_fematrix_matvec_host": ([P, P, P, ctypes.c_double], I),
         "dkt_fematrix_matvec_noalloc": ([P, P, P, ctypes.c_double, P], I),
+        "dkt_fevector_compute_vec": ([P, P, P, ctypes.c_double, P], I),
         "dkt_diagonal": ([P, P, P], I),
         "dkt_cg_solve": ([P, P, P, I, ctypes.c_double, I, P, P, P], I),
         "dkt_pcg_solve": ([P, P, P, I, I, ctypes.c_double, I, P, P, P, P], I),
@@ -236,6 +237,10 @@ class Matrix:
     def matvec(self, x_dev, y_dev, scale=1.0, stream=None):
         """feMatrix::matVec on device tensors."""
         _check(load().dkt_fematrix_matvec(self._h, _p(x_dev), _p(y_dev), scale, _stream(stream)))
+
+    def compute_vec(self, in_dev, out_dev, scale=1.0, stream=None):
+        """feVector::computeVec on device tensors (operators OP_HEATVEC, OP_MASS, OP_CUSTOM)."""
+        _check(load().dkt_fevector_compute_vec(self._h, _p(in_dev), _p(out_dev), scale, _stream(stream)))
 
     def matvec_noalloc(self, x_dev, y_dev, scale=1.0, stream=None):
         """feMatrix::matVec that allocates no device memory (fixed 8 MiB scratch per device)."""

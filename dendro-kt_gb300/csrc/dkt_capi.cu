@@ -94,7 +94,7 @@ void set_curve(dkt::CurveHost &cv, int curve, int dim)
 
 void setup_operator(dkt::Plan &pl, int op, const double *tables, cudaStream_t s)
 {
-  if (op < 0 || op > 5) throw std::invalid_argument("unknown operator");
+  if (op < 0 || op > 6) throw std::invalid_argument("unknown operator");
   pl.op.kind = op;
   pl.op.npe = pl.npe;
   pl.op.nlev = pl.md + 1;
@@ -325,6 +325,18 @@ int dkt_fematrix_matvec(dkt_plan plan, const double *x_dev, double *y_dev, doubl
   if (!plan || !x_dev || !y_dev) return fail(DKT_E_ARG, "null argument");
   return guarded([&]() {
     dkt::fematrix_matvec(plan->pl, x_dev, y_dev, scale, (cudaStream_t) stream);
+    return DKT_OK;
+  });
+}
+
+int dkt_fevector_compute_vec(dkt_plan plan, const double *in_dev, double *out_dev, double scale, void *stream)
+{
+  if (!plan || !in_dev || !out_dev) return fail(DKT_E_ARG, "null argument");
+  const int k = plan->pl.op.kind;
+  if (k != dkt::OP_HEATVEC && k != dkt::OP_MASS && k != dkt::OP_CUSTOM)
+    return fail(DKT_E_ARG, "plan operator is not a vector (right-hand side) operator");
+  return guarded([&]() {
+    dkt::fematrix_matvec(plan->pl, in_dev, out_dev, scale, (cudaStream_t) stream);
     return DKT_OK;
   });
 }

@@ -134,6 +134,12 @@ void builtin_operator(int kind, int dim, int p, int md, std::vector<double> &A, 
     return;
   }
   tensor_matrix(re, dim, -1, B);   // mass
+  if (kind == 6) {   // HeatVec<3>: J_x J_y J_z (Q^T W Q)^(x)3, scale ignored
+    if (dim != 3) throw std::invalid_argument("the HeatVec operator is defined for dim 3");
+    uses_scale = false;
+    for (int l = 0; l <= md; l++) beta[l] = std::pow(0.5 * std::ldexp(1.0, -l), 3);
+    return;
+  }
   for (int l = 0; l <= md; l++) {
     const double J = 0.5 * std::ldexp(1.0, -l);
     alpha[l] = (kind == 5) ? 0.0 : std::pow(J, dim - 2);   // 5: mass only

@@ -132,9 +132,12 @@ struct DA {
 // Elemental operator K_L = alpha[L] * A + beta[L] * B (dense nPe x nPe, the
 // reference's lexicographic node order, x fastest), or one dense table per
 // level when kind == custom.
-enum OpKind { OP_IDENTITY = 0, OP_HEAT = 1, OP_LAPMASS = 2, OP_CUSTOM = 3, OP_LAPLACE = 4, OP_MASS = 5 };
+enum OpKind { OP_IDENTITY = 0, OP_HEAT = 1, OP_LAPMASS = 2, OP_CUSTOM = 3, OP_LAPLACE = 4, OP_MASS = 5, OP_HEATVEC = 6 };
 // operators whose feMatrix pre/post steps zero the domain-boundary entries
-__host__ __device__ inline bool op_has_bc(int k) { return k == OP_HEAT || k == OP_LAPMASS || k == OP_LAPLACE; }
+__host__ __device__ inline bool op_has_bc(int k)
+{
+  return k == OP_HEAT || k == OP_LAPMASS || k == OP_LAPLACE || k == OP_HEATVEC;
+}
 
 struct Operator {
   int kind = OP_LAPMASS;

@@ -47,10 +47,16 @@ extern "C" {
 #define DKT_OP_LAPMASS 2
 #define DKT_OP_CUSTOM 3
 /* Laplacian alone (J^(d-2) K_ref, Dirichlet zeroing as HeatMat) and mass
- * alone (J^d M_ref, no boundary step: the right-hand side b = M f of the
- * Poisson problems, the role of feVector::computeVec, FEM/include/feVector.h:122-168). */
+ * alone (J^d M_ref in any dim, no boundary step: the right-hand side b = M f
+ * of the Poisson problems, whose boundary rows the caller zeroes). */
 #define DKT_OP_LAPLACE 4
 #define DKT_OP_MASS 5
+/* HeatEq::HeatVec<3>::elementalComputeVec (FEM/examples/src/heatVec.cpp:30-78):
+ * the mass right-hand side J^3 M_ref, scale ignored, with the Dirichlet
+ * zeroing of input and output of pre/postComputeVec (:83-105); the operator
+ * that feVector::computeVec applies (FEM/include/feVector.h:122-168).  dim 3
+ * only, as in the reference (its 3D tensor kernels). */
+#define DKT_OP_HEATVEC 6
 
 typedef struct dkt_da_s *dkt_da;
 typedef struct dkt_plan_s *dkt_plan;
@@ -147,6 +153,14 @@ int dkt_fematrix_matvec_noalloc(dkt_plan plan, const double *x_dev, double *y_de
 
 /* Same with host arrays: copies in, computes, copies out, synchronises. */
 int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host, double scale);
+
+/* feVector<T,dim>::computeVec(in, out, scale) (FEM/include/feVector.h:122-168):
+ * preComputeVec on the input copy, fem::matvec with elementalComputeVec,
+ * postComputeVec on the output.  The plan's operator is the vector's
+ * elemental operator: DKT_OP_HEATVEC for HeatEq::HeatVec<3>, DKT_OP_MASS for
+ * the mass right-hand side in any dim (no boundary step), or DKT_OP_CUSTOM
+ * tables.  Device arrays; same traversal and result as dkt_fematrix_matvec. */
+int dkt_fevector_compute_vec(dkt_plan plan, const double *in_dev, double *out_dev, double scale, void *stream);
 
 /* Diagonal of the operator (for Jacobi preconditioning), on device. */
 int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream);

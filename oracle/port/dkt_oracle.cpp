@@ -613,6 +613,10 @@ void ikd_interp(unsigned dim, const RefEl &re, const double *in, double *out, un
 //   op 1: HeatMat<dim>::elementalMatVec, 3-axis stiffness with J = h/2
 //         (FEM/examples/src/heatMat.cpp:45-117)
 //   op 2: Laplacian + mass, J^(d-2) K_ref + J^d M_ref (restated operator)
+//   op 4 / op 5: its Laplacian / its mass term alone
+//   op 6: HeatVec<dim>::elementalComputeVec, J^d M_ref with the scale ignored
+//         (FEM/examples/src/heatVec.cpp:30-78), Dirichlet zeroing of input
+//         and output as pre/postComputeVec (:83-105)
 // ---------------------------------------------------------------------------
 void ele_op(int op, unsigned dim, const RefEl &re, const double *in, double *out, const double *coords, double scale)
 {
@@ -659,9 +663,10 @@ void ele_op(int op, unsigned dim, const RefEl &re, const double *in, double *out
     for (unsigned d = 0; d < dim; d++) { apply_axis(dim, M, (int) d == term ? re.D.data() : re.Q.data(), true, a.data(), b.data(), d); std::swap(a, b); }
     double f = term < 0 ? Jd : Jdm2;
     if (op == 4 && term < 0) f = 0.0;   // Laplacian only
-    if (op == 5 && term >= 0) f = 0.0;  // mass only
+    if ((op == 5 || op == 6) && term >= 0) f = 0.0;  // mass only
     for (unsigned idx = 0; idx < n; idx++) acc[idx] += f * a[idx];
   }
+  if (op == 6) scale = 1.0;   // HeatVec ignores the scale argument
   for (unsigned i = 0; i < n; i++) out[i] = scale * acc[i];
 }
 
@@ -1041,7 +1046,7 @@ int dkto_fematrix_matvec(void *hp, const double *x, double *y)
   OracleDA *h = (OracleDA *) hp;
   const size_t n = h->nodeL.size();
   std::vector<double> xin(x, x + n);
-  const bool bc = (h->op == 1 || h->op == 2 || h->op == 4);
+  const bool bc = (h->op == 1 || h->op == 2 || h->op == 4 || h->op == 6);
   if (bc) for (uint32_t b : h->bdry) xin[b] = 0.0;
   dkto_matvec_raw(hp, xin.data(), y);
   if (bc) for (uint32_t b : h->bdry) y[b] = 0.0;

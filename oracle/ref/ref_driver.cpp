@@ -11,10 +11,13 @@
 //       op 1: HeatEq::HeatMat<dim> (FEM/examples/src/heatMat.cpp:45-139)
 //       op 2: Laplacian + mass, a restatement built from the reference's
 //             RefElement 1D operators (the reference has no valid 4D operator)
+//       op 6: feVector::computeVec (FEM/include/feVector.h:122-168) of
+//             HeatEq::HeatVec<dim> (FEM/examples/src/heatVec.cpp:30-104), the
+//             mass right-hand side with boundary zeroing; a 3D operator
 //   * the raw fem::matvec output (FEM/include/matvec.h:231-240), no pre/post
 //   * the RefElement 1D matrices (FEM/src/refel.cpp:75-220)
 //
-// Binary formats are documented in oracle/ref/README.md.
+// The binary formats are the ones tests/golden/refio.py writes and reads.
 #include <mpi.h>
 #include "treeNode.h"
 #include "tsort.h"
@@ -25,6 +28,7 @@
 #include "matvec.h"
 #include "refel.h"
 #include "heatMat.h"
+#include "heatVec.h"
 
 #include <chrono>
 #include <cstdio>
@@ -215,14 +219,17 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
   IdentityMat<dim> idm(da, 1);
   HeatEq::HeatMat<dim> heat(da, 1);
   LapMassMat<dim> lm(da, 1);
+  HeatEq::HeatVec<dim> hv(da, 1);
   std::array<double, dim> lo, hi;
   lo.fill(0.0);
   hi.fill(1.0);
   Point<dim> pmin(lo), pmax(hi);   // problem domain [0,1]^dim
   heat.setProblemDimensions(pmin, pmax);
   lm.setProblemDimensions(pmin, pmax);
+  hv.setProblemDimensions(pmin, pmax);
   if (op == 0) mv = [&](const double *a, double *b) { idm.matVec(a, b, 1.0); };
   else if (op == 1) mv = [&](const double *a, double *b) { heat.matVec(a, b, 1.0); };
+  else if (op == 6) mv = [&](const double *a, double *b) { hv.computeVec(a, b, 1.0); };
   else mv = [&](const double *a, double *b) { lm.matVec(a, b, 1.0); };
 
   std::vector<double> times;
@@ -242,6 +249,7 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
     fem::EleOpT<double> eop;
     if (op == 0) eop = std::bind(&IdentityMat<dim>::elementalMatVec, &idm, _1, _2, _3, _4);
     else if (op == 1) eop = std::bind(&HeatEq::HeatMat<dim>::elementalMatVec, &heat, _1, _2, _3, _4);
+    else if (op == 6) eop = std::bind(&HeatEq::HeatVec<dim>::elementalComputeVec, &hv, _1, _2, _3, _4);
     else eop = std::bind(&LapMassMat<dim>::elementalMatVec, &lm, _1, _2, _3, _4);
     fem::matvec(xg.data(), yraw.data(), da->getTNCoords(), nTotal, *da->getTreePartFront(), *da->getTreePartBack(),
                 eop, 1.0, da->getReferenceElement());

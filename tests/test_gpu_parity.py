@@ -270,6 +270,32 @@ def test_laplace_and_mass_operators_vs_oracle(dkt, op):
         assert _rel(_gpu_mv(A, x), yr) <= TOL, mode
 
 
+HEATVEC = [p for p in GOLDEN if "_op6_" in os.path.basename(p)]
+
+
+@pytest.mark.parametrize("path", HEATVEC, ids=[os.path.basename(p)[:-4] for p in HEATVEC])
+def test_fevector_compute_vec_matches_reference(dkt, path):
+    """feVector::computeVec of HeatVec<3> through dkt_fevector_compute_vec:
+    the reference's right-hand side (input and output boundary zeroed, scale
+    ignored) within 1e-12, in both arithmetic paths."""
+    import torch
+    g = np.load(path)
+    dim, md, order = int(g["dim"]), int(g["md"]), int(g["order"])
+    curve = dkt.CURVE_HILBERT if os.path.basename(path).startswith("hilbert_") else dkt.CURVE_MORTON
+    da = dkt.DA(g["tree_coords"], g["tree_levels"], dim, order=order, max_depth=md, curve=curve, sorted_tree=True)
+    V = dkt.Matrix(da, op=dkt.OP_HEATVEC)
+    xd = torch.from_numpy(np.ascontiguousarray(g["x"])).cuda()
+    for mode in (dkt.ARITH_FP64, dkt.ARITH_AUTO):
+        V.set_arithmetic(mode)
+        yd = torch.empty_like(xd)
+        V.compute_vec(xd, yd, scale=3.0)   # HeatVec ignores the scale
+        torch.cuda.synchronize()
+        assert _rel(yd.cpu().numpy(), g["y"]) <= TOL, mode
+    L = dkt.Matrix(da, op=dkt.OP_LAPLACE)
+    with pytest.raises(RuntimeError):
+        L.compute_vec(xd, torch.empty_like(xd))
+
+
 @pytest.mark.parametrize("order", [1, 2])
 def test_conforming_traversal_vs_oracle(dkt, order):
     """Conforming traversal (parent nodes of any level on the parent lattice,
