@@ -125,6 +125,17 @@ def traffic(kernel, leaf_visits):
     return None
 
 
+def q2sf_flops(dim, leaves, hanging):
+    """FP64 flops (FMA = 2) of the sum-factorised Q2 kernel: per leaf the
+    forward and transposed 1D transforms (local axes 9 flops per 3-node line,
+    the shuffled last axis 5 per value) and the diagonal; per hanging leaf the
+    sparse child interpolation and its transpose (5 flops per line or value)."""
+    npe = 3 ** dim
+    per_leaf = 2 * ((dim - 1) * (npe // 3) * 9 + npe * 5) + npe
+    per_hang = 2 * ((dim - 1) * (npe // 3) * 5 + npe * 5)
+    return leaves * per_leaf + hanging * per_hang
+
+
 def algorithmic_bytes(stats, n_nodes, npe):
     """Algorithmic bytes of one product (the map layout of the reference
     traversal, whatever the kernel actually stores): x read and y written
@@ -252,7 +263,8 @@ def batch_trees(dkt, n_prob, lo, hi, md=10):
     """Batched workload: element targets log-uniform in [lo, hi] (numpy PCG64
     stream 12345); mesh k refined around the 1-4 Gaussian clusters (sd 0.05)
     of cluster_points(seed=k), the point count adjusted to land within 10%
-    of the target (two corrections at most).  Built on host threads."""
+    of the target (two corrections at most).  Trees are built on the device
+    (dkt_mesh_tree_from_points_device), from several host threads."""
     import concurrent.futures as cf
     rng = np.random.default_rng(12345)
     targets = np.exp(rng.uniform(np.log(lo), np.log(hi), n_prob)).astype(np.int64)
@@ -261,7 +273,7 @@ def batch_trees(dkt, n_prob, lo, hi, md=10):
         t = int(targets[k])
         n = max(4, t // 6)
         for _ in range(3):
-            c, l = dkt.tree_from_points(dkt.cluster_points(n, 3, md, seed=k), 3, md)
+            c, l = dkt.tree_from_points(dkt.cluster_points(n, 3, md, seed=k), 3, md, device=True)
             r = len(l) / t
             if 0.9 <= r <= 1.1:
                 break
@@ -309,7 +321,7 @@ def run_batch(a, dkt, dev):
     out = {"workload": "%d 3D Q1 Poisson problems, element targets log-uniform in [1e3, %.0e], 1-4 Gaussian "
                        "clusters (sd 0.05) each; %d elements, %d nodes in one block-diagonal plan"
                        % (a.batch, a.batch_max_elements, n_elem, B.n),
-           "setup_s": {"meshes_host": t_mesh, "plans": t_plan}, "tile": tile, "tile_product_ms": tile_ms}
+           "setup_s": {"meshes": t_mesh, "plans": t_plan}, "tile": tile, "tile_product_ms": tile_ms}
     stream = torch.cuda.current_stream(dev)
     for name, prec, arith in (("fp64_native", dkt.PREC_FP64, dkt.ARITH_FP64), ("fp64", dkt.PREC_FP64, dkt.ARITH_AUTO),
                               ("mixed", dkt.PREC_MIXED, dkt.ARITH_AUTO)):
@@ -356,7 +368,8 @@ def serve_requests(dkt, n_req, max_elem, rate=200.0, seed=4):
                 c, l = dkt.sphere_shell_tree(dim, md[dim], level, ctr, rad)
         else:
             n = max(4, int(target / (2.0 * dim)))
-            c, l = dkt.tree_from_points(dkt.cluster_points(n, dim, md[dim], seed=10000 + k), dim, md[dim])
+            c, l = dkt.tree_from_points(dkt.cluster_points(n, dim, md[dim], seed=10000 + k), dim, md[dim],
+                                        device=True)
         out.append((float(t[k]), dim, md[dim], c, l, 5000 + k))
     return out
 
@@ -471,11 +484,20 @@ def run_gpu(a, rank, world, local_rank):
         return
     peak, peak_kind = peaks()
     fixed = a.order == 1
-    kname = "k_matvec_q1t" if fixed else "k_matvec_leaf"
+    kname = "k_matvec_q1t" if fixed else "k_matvec_q2sf"
     dtype = "i64 (exact fixed point, f64 in/out)" if fixed else "f64"
     B = algorithmic_bytes(st, n, npe)
     k_avg_s = (k_ms / max(k_launches, 1)) / 1e3
     achieved = B / k_avg_s / 1e9
+    fp64 = None
+    if not fixed:
+        # the sum-factorised Q2 kernel is bound by the FP64 pipe: its FP64
+        # flops per launch (FMA = 2) against the FMA rate probed on this GPU
+        flops = q2sf_flops(4, st["leaves"], st["hanging_leaves"])
+        peak64 = dkt.probe_device()["fp64_fma_tflops"]
+        fp64 = {"achieved_tflops": flops / k_avg_s / 1e12, "peak_tflops": peak64,
+                "frac": flops / k_avg_s / 1e12 / peak64, "flops_per_launch": flops,
+                "peak_kind": "measured (FP64 FMA probe, this run)"}
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": t_max / a.steps, "higher_is_better": True, "scaling": "weak",
@@ -493,6 +515,8 @@ def run_gpu(a, rank, world, local_rank):
         "clocks": clk.summary(),
         "setup_s": {"mesh": t_mesh, "da": t_da, "plan": t_plan},
     }
+    if fp64 is not None:
+        out["fp64_pipe"] = fp64
     if a.solve_level > 0:
         out["solve"] = run_solves(a, dkt, dev)
     if a.batch > 0:

@@ -85,6 +85,7 @@ def load(build_if_missing=True):
         "dkt_plan_destroy": ([P], None),
         "dkt_mesh_gaussian_points": ([I64, I, I, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, P], I),
         "dkt_mesh_tree_from_points": ([P, I64, I, I, I64, P, P, P], I),
+        "dkt_mesh_tree_from_points_device": ([P, I64, I, I, I64, P, P, P], I),
         "dkt_mesh_moving_ball": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
         "dkt_free": ([P], None),
         "dkt_mesh_moving_ball_device": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
@@ -357,11 +358,13 @@ def _take_cells(n, c, lv, dim):
     return coords.reshape(-1, dim), levels
 
 
-def tree_from_points(points, dim, max_depth, max_pts=1):
+def tree_from_points(points, dim, max_depth, max_pts=1, device=False):
+    """Complete tree with at most max_pts points per leaf, 2:1 balanced
+    (device=True builds it on the GPU, False on the host; the trees are equal)."""
     pts = np.ascontiguousarray(points, dtype=np.uint32).reshape(-1, dim)
     n, c, lv = ctypes.c_int64(0), ctypes.c_void_p(), ctypes.c_void_p()
-    _check(load().dkt_mesh_tree_from_points(_p(pts), pts.shape[0], dim, max_depth, max_pts, ctypes.byref(n),
-                                            ctypes.byref(c), ctypes.byref(lv)))
+    fn = load().dkt_mesh_tree_from_points_device if device else load().dkt_mesh_tree_from_points
+    _check(fn(_p(pts), pts.shape[0], dim, max_depth, max_pts, ctypes.byref(n), ctypes.byref(c), ctypes.byref(lv)))
     return _take_cells(n, c, lv, dim)
 
 

@@ -16,7 +16,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libdkt_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["dkt_da.cu", "dkt_plan.cu", "dkt_matvec.cu", "dkt_cg.cu", "dkt_capi.cu", "dkt_probe.cu", "dkt_q1fx.cu", "dkt_stale.cu", "dkt_tree.cu", "dkt_solve.cu", "dkt_tile.cu", "dkt_batch.cu", "dkt_serve.cu"]
+CU = ["dkt_da.cu", "dkt_plan.cu", "dkt_matvec.cu", "dkt_cg.cu", "dkt_capi.cu", "dkt_probe.cu", "dkt_q1fx.cu", "dkt_stale.cu", "dkt_tree.cu", "dkt_solve.cu", "dkt_tile.cu", "dkt_batch.cu", "dkt_serve.cu", "dkt_q2sf.cu"]
 CPP = ["dkt_host.cpp"]
 
 

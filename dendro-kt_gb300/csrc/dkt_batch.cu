@@ -13,6 +13,7 @@
 namespace dkt {
 
 bool q1fx_setup(Plan &pl, cudaStream_t s);
+bool q2sf_setup(Plan &pl, cudaStream_t s);
 
 __global__ void k_offset_ids(const int32_t *__restrict__ in, int32_t *__restrict__ out, int64_t n, int32_t base)
 {
@@ -116,6 +117,7 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
   }
   DKT_CUDA(cudaStreamSynchronize(s));
   q1fx_setup(out, s);
+  q2sf_setup(out, s);
   out.tl_ready = a.tl_ready;
 }
 

@@ -22,11 +22,14 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 void diagonal(const Plan &pl, double *diag, cudaStream_t s);
 bool q1fx_setup(Plan &pl, cudaStream_t s);
+bool q2sf_setup(Plan &pl, cudaStream_t s);
 void tile_setup(Plan &pl, int T, cudaStream_t s);
 bool tile_size_supported(int dim, int T);
 inline int default_tile(int dim) { return 256; }
 void sphere_shell_device(int dim, int md, int level, double R, double w, const double *c, DBuf<uint64_t> &out,
                          int64_t &n_out, cudaStream_t s);
+void tree_from_points_device(const uint32_t *pts_host, int64_t n, int dim, int md, int64_t max_pts,
+                             DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s);
 void moving_ball_device(int md, int level, double R, double w, const double *c0, const double *c1,
                         DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s);
 void unpack_cells_to_host(const DBuf<uint64_t> &keys, int64_t n, int dim, int md, uint32_t *coords, uint8_t *levels,
@@ -216,6 +219,7 @@ static int plan_common(int dim, int order, int curve, int md, const uint32_t *no
     setup_operator(pl, op, tables, s);
     dkt::stale_setup(pl, ip, s);
     if (dkt::q1fx_setup(pl, s)) dkt::tile_setup(pl, dkt::default_tile(dim), s);
+    dkt::q2sf_setup(pl, s);
     if (bdry_dev) {
       pl.bdry.alloc(nb > 0 ? nb : 1);
       if (nb > 0) DKT_CUDA(cudaMemcpyAsync(pl.bdry.p, bdry_dev, nb * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
@@ -647,6 +651,29 @@ int dkt_mesh_sphere_shell_device(int dim, int max_depth, int level, double radiu
     if (!c || !l) { std::free(c); std::free(l); return fail(DKT_E_NOMEM, "host allocation failed"); }
     dkt::unpack_cells_to_host(keys, n, dim, max_depth, c, l, 0);
     *n_out = n;
+    *coords = c;
+    *levels = l;
+    return DKT_OK;
+  });
+}
+
+int dkt_mesh_tree_from_points_device(const uint32_t *pts, int64_t n, int dim, int max_depth, int64_t max_pts,
+                                     int64_t *n_out, uint32_t **coords, uint8_t **levels)
+{
+  if (!pts || !n_out || !coords || !levels || n <= 0 || dim < 2 || dim > 4 || max_pts < 1 || max_depth < 1 ||
+      dim * max_depth + 6 > 64)
+    return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    for (int64_t i = 0; i < n * dim; i++)
+      if (pts[i] >= (1u << max_depth)) throw std::invalid_argument("point outside the domain");
+    dkt::DBuf<uint64_t> keys;
+    int64_t nc = 0;
+    dkt::tree_from_points_device(pts, n, dim, max_depth, max_pts, keys, nc, 0);
+    uint32_t *c = (uint32_t *) std::malloc((size_t) nc * dim * sizeof(uint32_t) + 1);
+    uint8_t *l = (uint8_t *) std::malloc((size_t) nc + 1);
+    if (!c || !l) { std::free(c); std::free(l); return fail(DKT_E_NOMEM, "host allocation failed"); }
+    dkt::unpack_cells_to_host(keys, nc, dim, max_depth, c, l, 0);
+    *n_out = nc;
     *coords = c;
     *levels = l;
     return DKT_OK;

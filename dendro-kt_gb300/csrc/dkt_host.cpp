@@ -78,6 +78,88 @@ RefEl1D refel_1d(int p)
   return r;
 }
 
+// Simultaneous diagonalisation of the order-2 1D mass M1 = Q^T W Q and
+// stiffness K1 = D^T W D: a transform T with M1 = T^T T and K1 = T^T diag(lam) T.
+// Both matrices are centrosymmetric (symmetric nodes and quadrature), so the
+// pencil splits into an even 2x2 block on span{(1,0,1), (0,1,0)} and an odd
+// 1x1 block on (1,0,-1).  The even block is reduced by the Cholesky factor of
+// its mass and diagonalised by one Jacobi rotation.  Rows 0, 1 of T are even
+// (t00, t01, t00), (t10, t11, t10) and row 2 is odd (t20, 0, -t20); T is
+// returned row-major.  Computed in long double.
+bool q2_factors(double T[9], double lam[3], double pint[3])
+{
+  const RefEl1D re = refel_1d(2);
+  typedef long double R;
+  R M1[9], K1[9];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      R m = 0, k = 0;
+      for (int g = 0; g < 3; g++) {
+        m += (R) re.W[g] * re.Q[r * 3 + g] * re.Q[c * 3 + g];
+        k += (R) re.W[g] * re.D[r * 3 + g] * re.D[c * 3 + g];
+      }
+      M1[r * 3 + c] = m;
+      K1[r * 3 + c] = k;
+    }
+  const R s2 = std::sqrt((R) 0.5);
+  const R me00 = (M1[0] + M1[2] + M1[6] + M1[8]) / 2, me01 = (M1[1] + M1[7]) * s2, me11 = M1[4];
+  const R ke00 = (K1[0] + K1[2] + K1[6] + K1[8]) / 2, ke01 = (K1[1] + K1[7]) * s2, ke11 = K1[4];
+  const R mo = (M1[0] - M1[2] - M1[6] + M1[8]) / 2, ko = (K1[0] - K1[2] - K1[6] + K1[8]) / 2;
+  const R l11 = std::sqrt(me00), l21 = me01 / l11, l22 = std::sqrt(me11 - l21 * l21);
+  // Li = L^-1, C = Li Ke Li^T
+  const R i00 = 1 / l11, i10 = -l21 / (l11 * l22), i11 = 1 / l22;
+  const R c00 = i00 * i00 * ke00;
+  const R c01 = i00 * (i10 * ke00 + i11 * ke01);
+  const R c11 = i10 * i10 * ke00 + 2 * i10 * i11 * ke01 + i11 * i11 * ke11;
+  const R th = std::atan2(2 * c01, c00 - c11) / 2, c = std::cos(th), s = std::sin(th);
+  const R lam0 = c00 * c * c + 2 * c01 * c * s + c11 * s * s;
+  const R lam1 = c00 * s * s - 2 * c01 * c * s + c11 * c * c;
+  // Se = Li^T V, V = [[c, -s], [s, c]]: generalised eigenvectors in the even basis
+  const R se00 = i00 * c + i10 * s, se01 = -i00 * s + i10 * c;
+  const R se10 = i11 * s, se11 = i11 * c;
+  R S[9];   // columns: two even modes, one odd mode
+  S[0] = se00 * s2; S[3] = se10; S[6] = se00 * s2;
+  S[1] = se01 * s2; S[4] = se11; S[7] = se01 * s2;
+  S[2] = s2 / std::sqrt(mo); S[5] = 0; S[8] = -s2 / std::sqrt(mo);
+  // T = S^T M1 = S^-1 (S^T M1 S = I)
+  R Tl[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      R v = 0;
+      for (int k = 0; k < 3; k++) v += S[k * 3 + i] * M1[k * 3 + j];
+      Tl[i * 3 + j] = v;
+    }
+  const R t00 = (Tl[0] + Tl[2]) / 2, t10 = (Tl[3] + Tl[5]) / 2, t20 = (Tl[6] - Tl[8]) / 2;
+  const R Ts[9] = {t00, Tl[1], t00, t10, Tl[4], t10, t20, 0, -t20};
+  for (int i = 0; i < 9; i++) T[i] = (double) Ts[i];
+  lam[0] = (double) lam0;
+  lam[1] = (double) lam1;
+  lam[2] = (double) (ko / mo);
+  // check M1 = T^T T and K1 = T^T diag(lam) T
+  R err = 0, mx = 0;
+  for (int r = 0; r < 3; r++)
+    for (int cc = 0; cc < 3; cc++) {
+      R m = 0, k = 0;
+      for (int i = 0; i < 3; i++) {
+        m += Ts[i * 3 + r] * Ts[i * 3 + cc];
+        k += Ts[i * 3 + r] * (R) lam[i] * Ts[i * 3 + cc];
+      }
+      err = std::max(err, std::max(std::fabs(m - M1[r * 3 + cc]), std::fabs(k - K1[r * 3 + cc])));
+      mx = std::max(mx, std::max(std::fabs(M1[r * 3 + cc]), std::fabs(K1[r * 3 + cc])));
+    }
+  // child interpolation: forward row j of child 0 is ip0[k*3 + j] over k;
+  // rows 0 and 2 copy parent nodes 0 and 1, child 1 is the mirror image
+  const std::vector<double> &a = re.ip0, &b = re.ip1;
+  bool ok = err <= 1e-15L * mx;
+  ok = ok && a[0] == 1 && a[3] == 0 && a[6] == 0 && a[2] == 0 && a[5] == 1 && a[8] == 0;
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 3; k++) ok = ok && b[k * 3 + j] == a[(2 - k) * 3 + (2 - j)];
+  pint[0] = a[1];
+  pint[1] = a[4];
+  pint[2] = a[7];
+  return ok;
+}
+
 // Dense element matrix sum_g w_g * (prod_d B_d[c_d][g_d]) * (prod_d B_d[r_d][g_d])
 // over tensor Gauss points g, with B_d = D on axis `deriv` and Q elsewhere
 // (deriv < 0: mass).  Only axes < nax carry the quadrature; further axes (the

@@ -12,6 +12,10 @@ struct RefEl1D {
 RefEl1D refel_1d(int p);
 void builtin_operator(int kind, int dim, int p, int md, std::vector<double> &A, std::vector<double> &B,
                       std::vector<double> &alpha, std::vector<double> &beta, bool &uses_scale);
+// Order-2 factors: M1 = T^T T, K1 = T^T diag(lam) T (T row-major 3x3), and the
+// middle row (a, b, c) of the child-0 interpolation; false if the 1D operators
+// do not have the expected symmetric structure.
+bool q2_factors(double T[9], double lam[3], double pint[3]);
 
 struct Cell {
   uint32_t x[4];

@@ -184,6 +184,13 @@ struct Plan {
   DBuf<long long> fx_fm, xq, yq;
   DBuf<int> fx_fe, fx_sx;
   DBuf<unsigned long long> fx_amax;
+  // Sum-factorised order-2 kernel (dkt_q2sf.cu): 1D transform T (row-major),
+  // child-interpolation middle row, per-level diagonals, hanging-first order.
+  bool sf_ready = false, sf_split = false;
+  int64_t sf_n_main = 0;             // leaves of the main launch (all, or those reading no stale slot)
+  double sf_T[9] = {0}, sf_pint[3] = {0};
+  DBuf<double> sf_D;
+  DBuf<int32_t> sf_order;
   // binary32 variant of the same Q1 operators (inner solves).
   bool f32_ready = false;
   DBuf<float> f32_f, x32;

@@ -215,6 +215,7 @@ static void launch_leaf(Plan &pl, const double *x, double *y, double scale, cuda
 }
 
 void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cudaStream_t s);
+void q2sf_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
 
 // fem::matvec: y = 0, then the leaf kernel.
 void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
@@ -222,6 +223,7 @@ void matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
   if (pl.fx_ready && pl.arith != 1) { q1fx_matvec(pl, x, y, scale, false, s); return; }
   DKT_CUDA(cudaMemsetAsync(y, 0, pl.n_nodes * sizeof(double), s));
   if (pl.n_leaf == 0) return;
+  if (pl.sf_ready && pl.arith != 1) { q2sf_matvec(pl, x, y, scale, s); return; }
   stale_eval(pl, x, nullptr, s);
   switch (pl.dim * 10 + pl.order) {
     case 21: launch_leaf<2, 1>(pl, x, y, scale, s); break;

@@ -485,6 +485,19 @@ void scale_vector(double *v, int64_t n, double a, cudaStream_t s)
 
 // fem::matvec / feMatrix::matVec through the fixed-point path.  `bc` applies
 // the pre/post boundary zeroing.
+// The side stream of the stale-buffer chain and its fork/join events, made on
+// first use.  Highest priority: the chain's few, long, latency-bound blocks
+// start at once and the leaf kernel fills the rest of the machine around them.
+void ensure_side_stream(Plan &pl)
+{
+  if (pl.st_stream) return;
+  int lo = 0, hi = 0;
+  DKT_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  DKT_CUDA(cudaStreamCreateWithPriority(&pl.st_stream, cudaStreamNonBlocking, hi));
+  DKT_CUDA(cudaEventCreateWithFlags(&pl.st_fork, cudaEventDisableTiming));
+  DKT_CUDA(cudaEventCreateWithFlags(&pl.st_join, cudaEventDisableTiming));
+}
+
 void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cudaStream_t s)
 {
   const int64_t n = pl.n_nodes;
@@ -504,15 +517,7 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
   // follow once the chain has joined.
   const bool split = pl.tl_ready && pl.st_ready && pl.st_n_runs > 0 && pl.st_n_hleaf > 0;
   if (split) {
-    if (!pl.st_stream) {
-      // highest priority: the chain's few, long, latency-bound blocks start at
-      // once and the tiled kernel fills the rest of the machine around them
-      int lo = 0, hi = 0;
-      DKT_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-      DKT_CUDA(cudaStreamCreateWithPriority(&pl.st_stream, cudaStreamNonBlocking, hi));
-      DKT_CUDA(cudaEventCreateWithFlags(&pl.st_fork, cudaEventDisableTiming));
-      DKT_CUDA(cudaEventCreateWithFlags(&pl.st_join, cudaEventDisableTiming));
-    }
+    ensure_side_stream(pl);
     DKT_CUDA(cudaEventRecord(pl.st_fork, s));
     DKT_CUDA(cudaStreamWaitEvent(pl.st_stream, pl.st_fork, 0));
     stale_eval(pl, nullptr, pl.xq.p, pl.st_stream);

@@ -1,0 +1,409 @@
+// Sum-factorised leaf kernel for the order-2 built-in operators.
+//
+// Every Q2 built-in operator (HeatMat<3>, Laplacian + mass, Laplacian, mass,
+// HeatVec<3>) is a Kronecker sum of the 1D mass M1 and stiffness K1:
+//   K_L = alpha_L sum_t (M1 x .. x K1_t x .. x M1) + beta_L (M1 x .. x M1).
+// With M1 = T^T T and K1 = T^T diag(lam) T (q2_factors), this is
+//   K_L = (T x .. x T)^T diag(D_L) (T x .. x T),
+//   D_L[r] = alpha_L sum_t lam[digit_t(r)] + beta_L,
+// so the elemental product of fem::matvec (matvec.h:467-468) becomes a 1D
+// transform along every axis, a diagonal scaling and the transposed
+// transforms: 2 d 3^d (7/3) + 3^d FP64 operations instead of the 2 (3^d)^2 of
+// the dense contraction (4D: 1,593 against 13,122).  The child interpolation
+// of hanging leaves (IKD_Parent2Child / IKD_Child2Parent, refel.h:214-271) is
+// applied the same way with its exact sparsity (two of three rows copy a
+// parent node).  FP64 on this part runs at about 2 FMA per clock per SM, so
+// operation count is what bounds the kernel.
+//
+// Three threads work on one leaf: thread k holds the 3^(d-1) values whose
+// last-axis index is k.  Transforms along the other axes are local; the
+// last axis is applied with two warp shuffles per value.  A warp takes ten
+// leaves (lanes 30 and 31 idle).  Leaves run in an order with the hanging
+// leaves first (stable), so almost every warp is uniform in whether it runs
+// the interpolation.
+#include <algorithm>
+#include "dkt_host.h"
+#include "dkt_internal.cuh"
+
+namespace dkt {
+
+struct SfCoef {
+  // T rows (t00, t01, t00), (t10, t11, t10), (t20, 0, -t20)
+  double t00, t01, t10, t11, t20;
+  // middle row of the child-0 interpolation: y1 = pa x0 + pb x1 + pc x2
+  double pa, pb, pc;
+};
+
+template <int DIM>
+struct SfDim {
+  static constexpr int NV = DIM == 2 ? 3 : (DIM == 3 ? 9 : 27);   // values per thread
+  static constexpr int NPE = 3 * NV;
+};
+
+// Line operators on (a, b, c) along one axis, in place.
+__device__ __forceinline__ void line_t(double &a, double &b, double &c, const SfCoef &k)
+{
+  const double s = a + c, d = a - c;
+  const double e0 = fma(k.t01, b, k.t00 * s);
+  const double e1 = fma(k.t11, b, k.t10 * s);
+  a = e0;
+  b = e1;
+  c = k.t20 * d;
+}
+__device__ __forceinline__ void line_tt(double &a, double &b, double &c, const SfCoef &k)
+{
+  const double e = fma(k.t10, b, k.t00 * a), o = k.t20 * c, m = fma(k.t11, b, k.t01 * a);
+  a = e + o;
+  b = m;
+  c = e - o;
+}
+// parent -> child (forward interpolation), child bit cb along this axis
+__device__ __forceinline__ void line_p(double &a, double &b, double &c, const SfCoef &k, bool cb)
+{
+  const double y0 = cb ? b : a, y2 = cb ? c : b;
+  const double y1 = fma(k.pc, cb ? a : c, fma(k.pb, b, k.pa * (cb ? c : a)));
+  a = y0;
+  b = y1;
+  c = y2;
+}
+// child -> parent (transposed interpolation)
+__device__ __forceinline__ void line_pt(double &a, double &b, double &c, const SfCoef &k, bool cb)
+{
+  const double lo = fma(k.pa, b, cb ? c : a), mid = fma(k.pb, b, cb ? a : c), hi = k.pc * b;
+  a = cb ? hi : lo;
+  b = mid;
+  c = cb ? lo : hi;
+}
+
+// Row k of a 3x3 matrix G given row-major as g[9], as (own, next, next-next)
+// coefficients: out_k = cs w_k + c1 w_{k+1} + c2 w_{k+2} (indices mod 3).
+__device__ __forceinline__ void row_of(const double (&g)[9], int k, double &cs, double &c1, double &c2)
+{
+  cs = k == 0 ? g[0] : (k == 1 ? g[4] : g[8]);
+  c1 = k == 0 ? g[1] : (k == 1 ? g[5] : g[6]);
+  c2 = k == 0 ? g[2] : (k == 1 ? g[3] : g[7]);
+}
+
+// Apply along the local axes 0..DIM-2 with op(a, b, c).
+template <int DIM, typename Op>
+__device__ __forceinline__ void local_axes(double (&v)[SfDim<DIM>::NV], Op op)
+{
+  constexpr int NV = SfDim<DIM>::NV;
+#pragma unroll
+  for (int ax = 0; ax < DIM - 1; ax++) {
+    const int s = ax == 0 ? 1 : (ax == 1 ? 3 : 9);
+#pragma unroll
+    for (int j = 0; j < NV; j++)
+      if ((j / s) % 3 == 0) op(ax, v[j], v[j + s], v[j + 2 * s]);
+  }
+}
+// Apply along the last axis: every value mixes with the same slot of the two
+// sibling lanes.
+template <int DIM>
+__device__ __forceinline__ void last_axis(double (&v)[SfDim<DIM>::NV], double cs, double c1, double c2, int l1, int l2)
+{
+#pragma unroll
+  for (int j = 0; j < SfDim<DIM>::NV; j++) {
+    const double w1 = __shfl_sync(0xffffffffu, v[j], l1);
+    const double w2 = __shfl_sync(0xffffffffu, v[j], l2);
+    v[j] = fma(c2, w2, fma(c1, w1, cs * v[j]));
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_matvec_q2sf(
+    const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+    const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, const int32_t *__restrict__ order,
+    int64_t n_leaf, SfCoef cf, const double *__restrict__ Dtab, const double *__restrict__ x, double *__restrict__ y,
+    double scale, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
+    const double *__restrict__ stv, int conforming)
+{
+  constexpr int NV = SfDim<DIM>::NV, NPE = SfDim<DIM>::NPE;
+  const int lane = threadIdx.x & 31, slot = lane / 3, k = lane - 3 * slot;
+  const int64_t t = ((int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 10 + slot;
+  const bool valid = slot < 10 && t < n_leaf;
+  // sibling lanes of the same leaf; the idle lanes 30, 31 read themselves
+  const int l1 = slot < 10 ? 3 * slot + (k + 1) % 3 : lane;
+  const int l2 = slot < 10 ? 3 * slot + (k + 2) % 3 : lane;
+  const int64_t i = valid ? (int64_t) order[t] : 0;
+  const uint32_t inf = valid ? info[i] : 0u;
+  const int L = inf & 0xFFu;
+  const unsigned child = (inf >> 8) & 0xFFu;
+  const bool hang = valid && ((inf >> 16) & 1u);
+  const bool cb_last = (child >> (DIM - 1)) & 1u;
+
+  double u[NV];
+  const int32_t *er = e2n + i * NPE + k * NV;
+#pragma unroll
+  for (int j = 0; j < NV; j++) {
+    const int32_t nd = valid ? er[j] : -1;
+    u[j] = nd >= 0 ? x[nd] : 0.0;
+  }
+  const bool any_h = __any_sync(0xffffffffu, hang);
+  uint32_t fmk = 0;   // fill bits of this thread's ranks k*NV .. k*NV+NV-1
+  int64_t h = 0;
+  if (any_h) {
+    double v[NV];
+    if (hang) {
+      h = hidx[i];
+      const int b0 = k * NV, w = b0 >> 5, sh = b0 & 31;   // b0 + NV <= 81 < 96: words w, w+1 <= 2
+      const uint64_t two = (uint64_t) fill[h * 3 + w] | ((uint64_t) fill[h * 3 + w + 1] << 32);
+      fmk = (uint32_t) (two >> sh) & ((1u << NV) - 1u);
+      const int32_t hz = hzoff ? hzoff[h] : -1;   // slots read from the emulated static buffer
+      const int32_t *pr = p2n + h * NPE + k * NV;
+#pragma unroll
+      for (int j = 0; j < NV; j++) {
+        const int32_t pn = pr[j];
+        double val = 0.0;
+        if (pn >= 0) val = x[pn];
+        else if (hz >= 0) {
+          const int32_t id = hztab[(int64_t) hz * NPE + k * NV + j];
+          if (id >= 0) val = stv[id];
+        }
+        v[j] = val;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NV; j++) v[j] = 0.0;
+    }
+    local_axes<DIM>(v, [&](int ax, double &a, double &b, double &c) { line_p(a, b, c, cf, (child >> ax) & 1u); });
+    {
+      // row k of the child interpolation along the last axis
+      const double g[9] = {cb_last ? 0.0 : 1.0, cb_last ? 1.0 : 0.0, 0.0,
+                           cb_last ? cf.pc : cf.pa, cf.pb, cb_last ? cf.pa : cf.pc,
+                           0.0, cb_last ? 0.0 : 1.0, cb_last ? 1.0 : 0.0};
+      double cs, c1, c2;
+      row_of(g, k, cs, c1, c2);
+      last_axis<DIM>(v, cs, c1, c2, l1, l2);
+    }
+    if (hang) {
+#pragma unroll
+      for (int j = 0; j < NV; j++)
+        if (!((fmk >> j) & 1u)) u[j] = v[j];
+    }
+  }
+  // forward transform
+  local_axes<DIM>(u, [&](int, double &a, double &b, double &c) { line_t(a, b, c, cf); });
+  {
+    const double g[9] = {cf.t00, cf.t01, cf.t00, cf.t10, cf.t11, cf.t10, cf.t20, 0.0, -cf.t20};
+    double cs, c1, c2;
+    row_of(g, k, cs, c1, c2);
+    last_axis<DIM>(u, cs, c1, c2, l1, l2);
+  }
+  // diagonal of level L
+  const double *Dl = Dtab + (int64_t) L * NPE + k * NV;
+  if (scale == 1.0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) u[j] *= __ldg(Dl + j);
+  } else {
+#pragma unroll
+    for (int j = 0; j < NV; j++) u[j] *= scale * __ldg(Dl + j);
+  }
+  // transposed transform
+  {
+    const double g[9] = {cf.t00, cf.t10, cf.t20, cf.t01, cf.t11, 0.0, cf.t00, cf.t10, -cf.t20};
+    double cs, c1, c2;
+    row_of(g, k, cs, c1, c2);
+    last_axis<DIM>(u, cs, c1, c2, l1, l2);
+  }
+  local_axes<DIM>(u, [&](int, double &a, double &b, double &c) { line_tt(a, b, c, cf); });
+  if (valid) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      const int32_t nd = er[j];
+      if (nd >= 0) atomicAdd(y + nd, u[j]);
+    }
+  }
+  if (any_h) {
+    // zero the filled ranks, interpolate back to the parent (matvec.h:482-522)
+#pragma unroll
+    for (int j = 0; j < NV; j++)
+      if (!hang || ((fmk >> j) & 1u)) u[j] = 0.0;
+    local_axes<DIM>(u, [&](int ax, double &a, double &b, double &c) { line_pt(a, b, c, cf, (child >> ax) & 1u); });
+    {
+      // row k of the transposed interpolation along the last axis
+      const double g[9] = {cb_last ? 0.0 : 1.0, cb_last ? cf.pc : cf.pa, 0.0,
+                           cb_last ? 1.0 : 0.0, cf.pb, cb_last ? 0.0 : 1.0,
+                           0.0, cb_last ? cf.pa : cf.pc, cb_last ? 1.0 : 0.0};
+      double cs, c1, c2;
+      row_of(g, k, cs, c1, c2);
+      last_axis<DIM>(u, cs, c1, c2, l1, l2);
+    }
+    if (hang) {
+      const int32_t *pr = p2n + h * NPE + k * NV;
+#pragma unroll
+      for (int j = 0; j < NV; j++) {
+        const int32_t pn = pr[j];
+        // the reference masks parent slot q by the leaf's fill bit q
+        if (pn >= 0 && (conforming || !((fmk >> j) & 1u))) atomicAdd(y + pn, u[j]);
+      }
+    }
+  }
+}
+
+// Leaf classes of the main launch: 0 hanging, 1 not hanging, 2 left out
+// (reads stale slots, done after the chain when the product is split).
+__global__ void k_leaf_class(const uint32_t *__restrict__ info, uint32_t *__restrict__ f0, uint32_t *__restrict__ f1,
+                             int64_t n, int drop_stale)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t v = info[i];
+  const bool out = drop_stale && ((v >> 27) & 1u);
+  f0[i] = (!out && ((v >> 16) & 1u)) ? 1u : 0u;
+  f1[i] = (!out && !((v >> 16) & 1u)) ? 1u : 0u;
+}
+// Stable order with the hanging leaves first: the scan of class 0, then n_h +
+// the scan of class 1.
+__global__ void k_order_hanging_first(const uint32_t *__restrict__ f0, const uint32_t *__restrict__ p0,
+                                      const uint32_t *__restrict__ f1, const uint32_t *__restrict__ p1, int64_t n,
+                                      int64_t n_h, int32_t *__restrict__ order)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (f0[i]) order[p0[i]] = (int32_t) i;
+  else if (f1[i]) order[n_h + (int64_t) p1[i]] = (int32_t) i;
+}
+
+// Plan-time setup: the order-2 factors, the per-level diagonals D_L and the
+// leaf order.  Returns false (dense kernel) for other orders, the identity
+// and custom operators, or if the 1D operators lack the expected structure.
+bool q2sf_setup(Plan &pl, cudaStream_t s)
+{
+  pl.sf_ready = false;
+  const int k = pl.op.kind;
+  if (pl.order != 2 || k == OP_IDENTITY || k == OP_CUSTOM || pl.n_leaf == 0) return false;
+  double T[9], lam[3], pint[3];
+  if (!q2_factors(T, lam, pint)) return false;
+  const int dim = pl.dim, npe = pl.npe, nlev = pl.md + 1;
+  // D_L[r] = alpha_L sum_t lam[digit_t(r)] + beta_L; checked against the dense
+  // tables of the plan's operator on one level
+  std::vector<double> D((size_t) nlev * npe);
+  for (int l = 0; l < nlev; l++)
+    for (int r = 0; r < npe; r++) {
+      double sl = 0.0;
+      int rr = r;
+      for (int d = 0; d < dim; d++) { sl += lam[rr % 3]; rr /= 3; }
+      D[(size_t) l * npe + r] = pl.op.alpha[l] * sl + pl.op.beta[l];
+    }
+  {
+    // (T x..x T)^T diag(D_0 unit) (T x..x T) against A and B separately
+    std::vector<double> TT((size_t) npe * npe);
+    for (int r = 0; r < npe; r++)
+      for (int c = 0; c < npe; c++) {
+        double v = 1.0;
+        int rr = r, cc = c;
+        for (int d = 0; d < dim; d++) { v *= T[(rr % 3) * 3 + (cc % 3)]; rr /= 3; cc /= 3; }
+        TT[(size_t) r * npe + c] = v;
+      }
+    double err = 0.0, mx = 0.0;
+    for (int term = 0; term < 2; term++) {
+      const std::vector<double> &coef = term == 0 ? pl.op.alpha : pl.op.beta;
+      if (std::all_of(coef.begin(), coef.end(), [](double c) { return c == 0.0; })) continue;   // term unused
+      const std::vector<double> &ref = term == 0 ? pl.op.A : pl.op.B;
+      for (int r = 0; r < npe; r++)
+        for (int c = 0; c < npe; c++) {
+          double v = 0.0;
+          for (int m = 0; m < npe; m++) {
+            double dm = 1.0;
+            if (term == 0) {
+              dm = 0.0;
+              int mm = m;
+              for (int d = 0; d < dim; d++) { dm += lam[mm % 3]; mm /= 3; }
+            }
+            v += TT[(size_t) m * npe + r] * dm * TT[(size_t) m * npe + c];
+          }
+          const double want = ref[(size_t) r * npe + c];
+          err = std::max(err, std::fabs(v - want));
+          mx = std::max(mx, std::fabs(want));
+        }
+    }
+    if (!(err <= 1e-13 * mx)) return false;
+  }
+  pl.sf_D.upload(D.data(), D.size(), s);
+  std::copy(T, T + 9, pl.sf_T);
+  std::copy(pint, pint + 3, pl.sf_pint);
+  // With stale parent reads the chain runs on a side stream during the main
+  // launch, which leaves out the leaves that read its values.
+  pl.sf_split = pl.st_ready && pl.st_n_runs > 0 && pl.st_n_hleaf > 0;
+  DBuf<uint32_t> f0(pl.n_leaf), p0(pl.n_leaf), f1(pl.n_leaf), p1(pl.n_leaf);
+  k_leaf_class<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.info.p, f0.p, f1.p, pl.n_leaf, pl.sf_split ? 1 : 0);
+  const int64_t nh = (int64_t) exclusive_scan_total<uint32_t>(f0.p, p0.p, pl.n_leaf, s);
+  const int64_t nn = (int64_t) exclusive_scan_total<uint32_t>(f1.p, p1.p, pl.n_leaf, s);
+  pl.sf_n_main = nh + nn;
+  if (pl.sf_n_main + (pl.sf_split ? pl.st_n_hleaf : 0) != pl.n_leaf) throw std::runtime_error("q2sf leaf classes");
+  pl.sf_order.alloc(std::max<int64_t>(pl.sf_n_main, 1));
+  k_order_hanging_first<<<grid_for(pl.n_leaf), 256, 0, s>>>(f0.p, p0.p, f1.p, p1.p, pl.n_leaf, nh, pl.sf_order.p);
+  check_launch("q2sf_order");
+  DKT_CUDA(cudaStreamSynchronize(s));
+  pl.sf_ready = true;
+  return true;
+}
+
+template <int DIM>
+static void launch_sf(Plan &pl, const int32_t *order, int64_t n, const double *x, double *y, double scale,
+                      cudaStream_t s)
+{
+  if (n == 0) return;
+  SfCoef cf;
+  cf.t00 = pl.sf_T[0]; cf.t01 = pl.sf_T[1]; cf.t10 = pl.sf_T[3]; cf.t11 = pl.sf_T[4]; cf.t20 = pl.sf_T[6];
+  cf.pa = pl.sf_pint[0]; cf.pb = pl.sf_pint[1]; cf.pc = pl.sf_pint[2];
+  const int64_t per_block = 4 * 10;   // 4 warps of 10 leaves
+  const unsigned blocks = (unsigned) ((n + per_block - 1) / per_block);
+  k_matvec_q2sf<DIM><<<blocks, 128, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, order,
+                                            n, cf, pl.sf_D.p, x, y, pl.op.uses_scale ? scale : 1.0,
+                                            pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_v.p,
+                                            pl.conforming ? 1 : 0);
+  check_launch("matvec_q2sf");
+}
+
+static void launch_sf_dim(Plan &pl, const int32_t *order, int64_t n, const double *x, double *y, double scale,
+                          cudaStream_t s)
+{
+  switch (pl.dim) {
+    case 2: launch_sf<2>(pl, order, n, x, y, scale, s); break;
+    case 3: launch_sf<3>(pl, order, n, x, y, scale, s); break;
+    case 4: launch_sf<4>(pl, order, n, x, y, scale, s); break;
+    default: throw std::runtime_error("unsupported dim");
+  }
+  if (n > 0) pl.n_launch++;
+}
+
+void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s);
+void ensure_side_stream(Plan &pl);
+
+// fem::matvec with the sum-factorised kernel; y has been zeroed.  With stale
+// parent reads, the static-buffer chain runs on the high-priority side stream
+// while the main launch does every leaf that does not read its values; those
+// leaves follow once the chain has joined.  Only the main launch is timed.
+void q2sf_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
+{
+  if (pl.sf_split) {
+    ensure_side_stream(pl);
+    DKT_CUDA(cudaEventRecord(pl.st_fork, s));
+    DKT_CUDA(cudaStreamWaitEvent(pl.st_stream, pl.st_fork, 0));
+    stale_eval(pl, x, nullptr, pl.st_stream);
+    DKT_CUDA(cudaEventRecord(pl.st_join, pl.st_stream));
+  } else {
+    stale_eval(pl, x, nullptr, s);
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (pl.timing) {
+    DKT_CUDA(cudaEventCreate(&e0));
+    DKT_CUDA(cudaEventCreate(&e1));
+    DKT_CUDA(cudaEventRecord(e0, s));
+  }
+  launch_sf_dim(pl, pl.sf_order.p, pl.sf_n_main, x, y, scale, s);
+  if (pl.timing) {
+    DKT_CUDA(cudaEventRecord(e1, s));
+    pl.ev.push_back(e0);
+    pl.ev.push_back(e1);
+    pl.timed_launches++;
+  }
+  if (pl.sf_split) {
+    DKT_CUDA(cudaStreamWaitEvent(s, pl.st_join, 0));
+    launch_sf_dim(pl, pl.st_hleaves.p, pl.st_n_hleaf, x, y, scale, s);
+  }
+}
+
+}  // namespace dkt

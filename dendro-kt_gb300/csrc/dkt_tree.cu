@@ -349,6 +349,67 @@ void moving_ball_device(int md, int level, double R, double w, const double *c0,
   }, out, n_out, s);
 }
 
+// Points -> complete tree with at most max_pts points per leaf (the root is
+// always split), then 2:1 balanced: SFC_Tree::locTreeBalancing on one rank
+// (src/tsort.cpp:826-854).  The points' full-resolution interleaved Morton
+// keys are sorted once; a cell's points are the key range of its prefix, so
+// each refinement test is two binary searches.
+__device__ inline uint64_t morton_full_key(const uint32_t *a, int dim, int md)
+{
+  uint64_t k = 0;
+  for (int bit = md - 1; bit >= 0; bit--)
+    for (int d = dim - 1; d >= 0; d--) k = (k << 1) | ((a[d] >> bit) & 1u);
+  return k;
+}
+__global__ void k_point_keys(const uint32_t *__restrict__ pts, int64_t n, int dim, int md, uint64_t *__restrict__ keys)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t a[MAX_DIM];
+  for (int d = 0; d < dim; d++) a[d] = pts[i * dim + d];
+  keys[i] = morton_full_key(a, dim, md);
+}
+__device__ inline int64_t first_not_below(const uint64_t *__restrict__ v, int64_t n, uint64_t key)
+{
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (v[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+__global__ void k_count_test(const uint64_t *__restrict__ cells, int64_t n, int dim, int md,
+                             const uint64_t *__restrict__ pk, int64_t np, int64_t max_pts, uint32_t *__restrict__ refine)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t a[MAX_DIM];
+  int lev;
+  tdecode(cells[i], dim, md, a, lev);
+  if (lev == 0) { refine[i] = 1u; return; }
+  if (lev >= md) { refine[i] = 0u; return; }
+  const uint64_t lo = morton_full_key(a, dim, md);
+  const int shift = dim * (md - lev);   // < 64: lev >= 1 and dim * md <= 58
+  const int64_t b = first_not_below(pk, np, lo);
+  const int64_t e = first_not_below(pk, np, lo + (1ull << shift));
+  refine[i] = (e - b > max_pts) ? 1u : 0u;
+}
+
+void tree_from_points_device(const uint32_t *pts_host, int64_t n, int dim, int md, int64_t max_pts,
+                             DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s)
+{
+  if (dim < 2 || dim > MAX_DIM || n <= 0 || max_pts < 1) throw std::invalid_argument("tree from points: bad argument");
+  DBuf<uint32_t> pts;
+  pts.upload(pts_host, (size_t) n * dim, s);
+  DBuf<uint64_t> pk(n);
+  k_point_keys<<<grid_for(n), 256, 0, s>>>(pts.p, n, dim, md, pk.p);
+  check_launch("point_keys");
+  radix_sort_pairs<uint64_t, uint32_t>(pk.p, nullptr, (size_t) n, dim * md, s);
+  refine_device(dim, md, [&](const uint64_t *cells, int64_t nc, uint32_t *flag) {
+    k_count_test<<<grid_for(nc), 256, 0, s>>>(cells, nc, dim, md, pk.p, n, max_pts, flag);
+  }, out, n_out, s);
+}
+
 __global__ void k_unpack_cells(const uint64_t *__restrict__ k, uint32_t *__restrict__ x, uint8_t *__restrict__ lev,
                                int64_t n, int dim, int md)
 {

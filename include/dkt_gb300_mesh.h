@@ -25,6 +25,11 @@ int dkt_mesh_gaussian_points(int64_t n, int dim, int max_depth, double mean, dou
  * all 3^dim - 1 neighbours; cells are returned unsorted (dkt_da_create sorts). */
 int dkt_mesh_tree_from_points(const uint32_t *pts, int64_t n, int dim, int max_depth, int64_t max_pts,
                               int64_t *n_out, uint32_t **coords, uint8_t **levels);
+/* Same tree, built on the current device: the points' Morton keys are sorted
+ * once, cells are refined level by level (a cell's point count is a key
+ * range), then balanced as above; cells returned sorted by level. */
+int dkt_mesh_tree_from_points_device(const uint32_t *pts, int64_t n, int dim, int max_depth, int64_t max_pts,
+                                     int64_t *n_out, uint32_t **coords, uint8_t **levels);
 
 /* dim 4 (x,y,z,t): every cell whose box meets the shell
  * | |(x,y,z) - c(t)| - radius | <= halfwidth, c(t) = c0 + (c1 - c0) t, is refined
@@ -37,12 +42,6 @@ int dkt_mesh_moving_ball(int max_depth, int level, double radius, double halfwid
 int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double halfwidth, const double *c0,
                                 const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels);
 
-/* Sphere-shell refinement in dim 2..4, built on the device: every cell of
- * level < `level` whose box meets | ||x - centre|| - radius | <= halfwidth is
- * split (exact box distance interval), then the tree is 2:1 balanced.  The
- * workload generator of the served request stream (refinement on a random
- * sphere); no reference counterpart beyond SFC_Tree::locTreeBalancing
- * (src/tsort.cpp:826-854) for the balance.  Arrays are freed with dkt_free. */
 /* Rotation tables of a space-filling curve, the data that _InitializeHcurve
  * (src/KDhcurvedata.cpp:23-57) loads: per orientation, the Morton children
  * in curve order then the curve rank of every Morton child (rot, 2^(dim+1)
@@ -53,6 +52,12 @@ int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double 
  * Buffers: rot >= 192*32 bytes, ht >= 192*16 ints for dim 4. */
 int dkt_curve_tables(int curve, int dim, int8_t *rot, int32_t *ht, int *nrot);
 
+/* Sphere-shell refinement in dim 2..4, built on the device: every cell of
+ * level < `level` whose box meets | ||x - centre|| - radius | <= halfwidth is
+ * split (exact box distance interval), then the tree is 2:1 balanced.  The
+ * workload generator of the served request stream (refinement on a random
+ * sphere); no reference counterpart beyond SFC_Tree::locTreeBalancing
+ * (src/tsort.cpp:826-854) for the balance.  Arrays are freed with dkt_free. */
 int dkt_mesh_sphere_shell(int dim, int max_depth, int level, double radius, double halfwidth, const double *centre,
                           int64_t *n_out, uint32_t **coords, uint8_t **levels);   /* host build, same tree */
 int dkt_mesh_sphere_shell_device(int dim, int max_depth, int level, double radius, double halfwidth,

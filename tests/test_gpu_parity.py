@@ -56,8 +56,9 @@ def test_golden_da_and_matvec(dkt, path):
     assert np.array_equal(da.boundary_ids(), g["bdry"])
     A = dkt.Matrix(da, op=op)
     assert A.stats()["stale_slots"] == 0
-    modes = [dkt.ARITH_FP64, dkt.ARITH_AUTO] if order == 1 else [dkt.ARITH_AUTO]
-    for mode in modes:   # native FP64 kernel and, for Q1, the exact fixed-point kernel
+    # dense native-FP64 kernel, then AUTO: the exact fixed-point kernel (Q1)
+    # or the sum-factorised FP64 kernel (Q2 built-in operators)
+    for mode in (dkt.ARITH_FP64, dkt.ARITH_AUTO):
         A.set_arithmetic(mode)
         assert _rel(_gpu_mv(A, g["x"]), g["y"]) <= TOL, mode
         assert _rel(_gpu_mv(A, g["x"], raw=True), g["y_raw"]) <= TOL, mode
@@ -96,9 +97,8 @@ def test_gaussian_meshes_vs_oracle(dkt, dim, n, md, order, op):
     x = dkt.uniform_pm1(1, da.n)
     yr = ora.matvec(x)
     assert _rel(_gpu_mv(A, x), yr) <= TOL
-    if order == 1:
-        A.set_arithmetic(dkt.ARITH_FP64)
-        assert _rel(_gpu_mv(A, x), yr) <= TOL
+    A.set_arithmetic(dkt.ARITH_FP64)
+    assert _rel(_gpu_mv(A, x), yr) <= TOL
     st, ost = A.stats(), ora.stats()
     assert st["leaves"] == ost["leaves"] and st["hanging_leaves"] == ost["hanging_leaves"]
     assert st["stale_slots"] == 0 and ost["stale_reads"] == 0
@@ -116,7 +116,10 @@ def test_moving_ball_4d_vs_oracle(dkt, order):
     assert np.array_equal(nc, ora.node_coords) and np.array_equal(nl, ora.node_levels)
     A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
     x = dkt.uniform_pm1(2, da.n)
-    assert _rel(_gpu_mv(A, x), ora.matvec(x)) <= TOL
+    yr = ora.matvec(x)
+    for mode in (dkt.ARITH_FP64, dkt.ARITH_AUTO):
+        A.set_arithmetic(mode)
+        assert _rel(_gpu_mv(A, x), yr) <= TOL, mode
     assert A.stats()["leaves"] == ora.stats()["leaves"]
 
 
@@ -126,6 +129,19 @@ def test_device_moving_ball_equals_host(dkt):
         dc, dl = dkt.moving_ball_tree(max_depth=8, level=level, device=True)
         key = lambda c, l: sorted(map(tuple, np.concatenate([c.astype(np.int64), l[:, None].astype(np.int64)], 1)))
         assert len(hl) == len(dl) and key(hc, hl) == key(dc, dl)
+
+
+@pytest.mark.parametrize("dim,n,md,max_pts", [(2, 3000, 12, 1), (3, 20000, 10, 1), (3, 5000, 10, 7), (4, 800, 8, 1)])
+def test_device_tree_from_points_equals_host(dkt, dim, n, md, max_pts):
+    """locTreeBalancing on the device equals the host build (and therefore the
+    reference, which the host build is checked against in the golden tests);
+    repeated points included."""
+    pts = dkt.gaussian_points(n, dim, md, seed=9)
+    pts = np.concatenate([pts, pts[: n // 10]])
+    hc, hl = dkt.tree_from_points(pts, dim, md, max_pts=max_pts)
+    dc, dl = dkt.tree_from_points(pts, dim, md, max_pts=max_pts, device=True)
+    key = lambda c, l: sorted(map(tuple, np.concatenate([c.astype(np.int64), l[:, None].astype(np.int64)], 1)))
+    assert len(hl) == len(dl) and key(hc, hl) == key(dc, dl)
 
 
 def test_moving_ball_static_buffer_emulation(dkt):
@@ -149,6 +165,25 @@ def test_moving_ball_static_buffer_emulation(dkt):
         for mode in (dkt.ARITH_FP64, dkt.ARITH_AUTO):
             A.set_arithmetic(mode)
             assert _rel(_gpu_mv(A, x), yr) <= TOL, (seed, mode)
+
+
+def test_moving_ball_static_buffer_emulation_q2(dkt):
+    """Level-5 moving ball at order 2: 20,352 stale parent-slot reads per
+    product, reproduced by both the dense and the sum-factorised kernel."""
+    md, level = 10, 5
+    tc, tl = dkt.moving_ball_tree(max_depth=md, level=level, device=True)
+    da = dkt.DA(tc, tl, 4, order=2, max_depth=md)
+    orc.set_curve(4, md)
+    orc.set_stale_mode(0)
+    sc, sl = da.tree()
+    ora = orc.DA(sc, sl, 4, 2, 2)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    x = dkt.uniform_pm1(2, da.n)
+    yr = ora.matvec(x)
+    assert ora.stats()["stale_reads"] == A.stats()["stale_slots"] > 0
+    for mode in (dkt.ARITH_FP64, dkt.ARITH_AUTO):
+        A.set_arithmetic(mode)
+        assert _rel(_gpu_mv(A, x), yr) <= TOL, mode
 
 
 @pytest.mark.parametrize("dim,L", [(2, 4), (3, 3), (4, 2)])
