@@ -171,6 +171,13 @@ struct Plan {
   bool st_ready = false;
   int64_t st_start = 0, st_n_ent = 0, st_n_runs = 0;
   DBuf<int32_t> st_row, st_idx, st_runs, st_hzoff, st_hztab, st_srow, st_sidx, st_gstart;
+  // order 2: per group the child number and the need / take slot masks
+  // ([G][6]: needed slots, slots taken from the previous group), walked as a
+  // tensor-product interpolation instead of per-entry term lists
+  bool st_tp = false;
+  double st_pint[3] = {0, 0, 0};
+  DBuf<int32_t> st_gchild;
+  DBuf<uint32_t> st_gmask;
   DBuf<double> st_w, st_v, st_sw, st_f;
   DBuf<long long> st_vq;
   DBuf<int32_t> st_hleaves;          // leaves that read stale slots (info bit 27)

@@ -8,8 +8,11 @@
 //   D_L[r] = alpha_L sum_t lam[digit_t(r)] + beta_L,
 // so the elemental product of fem::matvec (matvec.h:467-468) becomes a 1D
 // transform along every axis, a diagonal scaling and the transposed
-// transforms: 2 d 3^d (7/3) + 3^d FP64 operations instead of the 2 (3^d)^2 of
-// the dense contraction (4D: 1,593 against 13,122).  The child interpolation
+// transforms: about 2 d 3^d (4/3) + 3^d FP64 operations instead of the
+// 2 (3^d)^2 of the dense contraction (4D: 1,053 against 13,122).  The
+// transform is used in its unit-diagonal form U = diag(1/T_kk) T, rows
+// (1, u01, 1), (u10, 1, u10), (-1, 0, 1), whose line products take four
+// operations; the row scales move into D.  The child interpolation
 // of hanging leaves (IKD_Parent2Child / IKD_Child2Parent, refel.h:214-271) is
 // applied the same way with its exact sparsity (two of three rows copy a
 // parent node).  FP64 on this part runs at about 2 FMA per clock per SM, so
@@ -28,8 +31,8 @@
 namespace dkt {
 
 struct SfCoef {
-  // T rows (t00, t01, t00), (t10, t11, t10), (t20, 0, -t20)
-  double t00, t01, t10, t11, t20;
+  // unit-diagonal transform U = diag(1/T_kk) T, rows (1, u01, 1), (u10, 1, u10), (-1, 0, 1)
+  double u01, u10;
   // middle row of the child-0 interpolation: y1 = pa x0 + pb x1 + pc x2
   double pa, pb, pc;
 };
@@ -41,21 +44,22 @@ struct SfDim {
 };
 
 // Line operators on (a, b, c) along one axis, in place.
+// U: 4 operations per line
 __device__ __forceinline__ void line_t(double &a, double &b, double &c, const SfCoef &k)
 {
-  const double s = a + c, d = a - c;
-  const double e0 = fma(k.t01, b, k.t00 * s);
-  const double e1 = fma(k.t11, b, k.t10 * s);
+  const double s = a + c;
+  const double e0 = fma(k.u01, b, s), e1 = fma(k.u10, s, b), o = c - a;
   a = e0;
   b = e1;
-  c = k.t20 * d;
+  c = o;
 }
+// U^T: 4 operations per line
 __device__ __forceinline__ void line_tt(double &a, double &b, double &c, const SfCoef &k)
 {
-  const double e = fma(k.t10, b, k.t00 * a), o = k.t20 * c, m = fma(k.t11, b, k.t01 * a);
-  a = e + o;
+  const double e = fma(k.u10, b, a), m = fma(k.u01, a, b);
+  a = e - c;
   b = m;
-  c = e - o;
+  c = e + c;
 }
 // parent -> child (forward interpolation), child bit cb along this axis
 __device__ __forceinline__ void line_p(double &a, double &b, double &c, const SfCoef &k, bool cb)
@@ -98,7 +102,17 @@ __device__ __forceinline__ void local_axes(double (&v)[SfDim<DIM>::NV], Op op)
   }
 }
 // Apply along the last axis: every value mixes with the same slot of the two
-// sibling lanes.
+// sibling lanes.  last_axis_unit: the lane's own coefficient is 1.
+template <int DIM>
+__device__ __forceinline__ void last_axis_unit(double (&v)[SfDim<DIM>::NV], double c1, double c2, int l1, int l2)
+{
+#pragma unroll
+  for (int j = 0; j < SfDim<DIM>::NV; j++) {
+    const double w1 = __shfl_sync(0xffffffffu, v[j], l1);
+    const double w2 = __shfl_sync(0xffffffffu, v[j], l2);
+    v[j] = fma(c2, w2, fma(c1, w1, v[j]));
+  }
+}
 template <int DIM>
 __device__ __forceinline__ void last_axis(double (&v)[SfDim<DIM>::NV], double cs, double c1, double c2, int l1, int l2)
 {
@@ -185,10 +199,10 @@ __global__ void __launch_bounds__(128) k_matvec_q2sf(
   // forward transform
   local_axes<DIM>(u, [&](int, double &a, double &b, double &c) { line_t(a, b, c, cf); });
   {
-    const double g[9] = {cf.t00, cf.t01, cf.t00, cf.t10, cf.t11, cf.t10, cf.t20, 0.0, -cf.t20};
+    const double g[9] = {1.0, cf.u01, 1.0, cf.u10, 1.0, cf.u10, -1.0, 0.0, 1.0};
     double cs, c1, c2;
     row_of(g, k, cs, c1, c2);
-    last_axis<DIM>(u, cs, c1, c2, l1, l2);
+    last_axis_unit<DIM>(u, c1, c2, l1, l2);
   }
   // diagonal of level L
   const double *Dl = Dtab + (int64_t) L * NPE + k * NV;
@@ -201,10 +215,10 @@ __global__ void __launch_bounds__(128) k_matvec_q2sf(
   }
   // transposed transform
   {
-    const double g[9] = {cf.t00, cf.t10, cf.t20, cf.t01, cf.t11, 0.0, cf.t00, cf.t10, -cf.t20};
+    const double g[9] = {1.0, cf.u10, -1.0, cf.u01, 1.0, 0.0, 1.0, cf.u10, 1.0};
     double cs, c1, c2;
     row_of(g, k, cs, c1, c2);
-    last_axis<DIM>(u, cs, c1, c2, l1, l2);
+    last_axis_unit<DIM>(u, c1, c2, l1, l2);
   }
   local_axes<DIM>(u, [&](int, double &a, double &b, double &c) { line_tt(a, b, c, cf); });
   if (valid) {
@@ -276,15 +290,21 @@ bool q2sf_setup(Plan &pl, cudaStream_t s)
   double T[9], lam[3], pint[3];
   if (!q2_factors(T, lam, pint)) return false;
   const int dim = pl.dim, npe = pl.npe, nlev = pl.md + 1;
-  // D_L[r] = alpha_L sum_t lam[digit_t(r)] + beta_L; checked against the dense
-  // tables of the plan's operator on one level
+  // D_L[r] = alpha_L sum_t lam[digit_t(r)] + beta_L, times prod_t T_kk^2 for
+  // the kernel's unit-diagonal transform U = diag(1/T_kk) T (so that
+  // (x T)^T diag(D) (x T) = (x U)^T diag(D prod T_kk^2) (x U)).  T and lam are
+  // checked against the dense tables of the plan's operator below.
   std::vector<double> D((size_t) nlev * npe);
   for (int l = 0; l < nlev; l++)
     for (int r = 0; r < npe; r++) {
-      double sl = 0.0;
+      long double sl = 0.0L, f = 1.0L;
       int rr = r;
-      for (int d = 0; d < dim; d++) { sl += lam[rr % 3]; rr /= 3; }
-      D[(size_t) l * npe + r] = pl.op.alpha[l] * sl + pl.op.beta[l];
+      for (int d = 0; d < dim; d++) {
+        sl += lam[rr % 3];
+        f *= (long double) T[(rr % 3) * 4] * T[(rr % 3) * 4];
+        rr /= 3;
+      }
+      D[(size_t) l * npe + r] = (double) (((long double) pl.op.alpha[l] * sl + pl.op.beta[l]) * f);
     }
   {
     // (T x..x T)^T diag(D_0 unit) (T x..x T) against A and B separately
@@ -346,7 +366,8 @@ static void launch_sf(Plan &pl, const int32_t *order, int64_t n, const double *x
 {
   if (n == 0) return;
   SfCoef cf;
-  cf.t00 = pl.sf_T[0]; cf.t01 = pl.sf_T[1]; cf.t10 = pl.sf_T[3]; cf.t11 = pl.sf_T[4]; cf.t20 = pl.sf_T[6];
+  cf.u01 = pl.sf_T[1] / pl.sf_T[0];
+  cf.u10 = pl.sf_T[3] / pl.sf_T[4];
   cf.pa = pl.sf_pint[0]; cf.pb = pl.sf_pint[1]; cf.pc = pl.sf_pint[2];
   const int64_t per_block = 4 * 10;   // 4 warps of 10 leaves
   const unsigned blocks = (unsigned) ((n + per_block - 1) / per_block);

@@ -100,6 +100,8 @@ void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s)
   std::vector<double> fw, sw;
   std::vector<int32_t> gstart;     // entry offset of every group, plus the end
   std::vector<int32_t> runs;       // pairs [first group, end group)
+  std::vector<int32_t> gchild;     // order 2: child number of every group
+  std::vector<uint32_t> gmask;     // order 2: need[3], take[3] of every group
   int32_t n_ent = 0;
   int64_t prev_g = -2;
   for (int64_t g = 0; g < H; g++) {
@@ -112,6 +114,15 @@ void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s)
     prev_g = g;
     gstart.push_back(n_ent);
     ent_base[g] = n_ent;
+    gchild.push_back(child[g]);
+    {
+      uint32_t take[3] = {0u, 0u, 0u};
+      if (g > 0)
+        for (int q2 = 0; q2 < npe; q2++)
+          if (stale(g, q2) && ((need[g - 1][q2 >> 5] >> (q2 & 31)) & 1u)) take[q2 >> 5] |= 1u << (q2 & 31);
+      for (int w = 0; w < 3; w++) gmask.push_back(need[g][w]);
+      for (int w = 0; w < 3; w++) gmask.push_back(take[w]);
+    }
     for (int q = 0; q < npe; q++) {
       if (!((need[g][q >> 5] >> (q & 31)) & 1u)) continue;
       n_ent++;
@@ -168,6 +179,24 @@ void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s)
   pl.st_sidx.upload(sidx.data(), sidx.size(), s);
   pl.st_sw.upload(sw.data(), sw.size(), s);
   pl.st_gstart.upload(gstart.data(), gstart.size(), s);
+  // Order 2 walks each group as P_c applied axis by axis to the previous
+  // group's values: valid when the child interpolation copies parent nodes 0
+  // and 1 in its outer rows and the second child is the mirror image.
+  pl.st_tp = false;
+  if (M == 3 && !gchild.empty()) {
+    const double *a = ip.data(), *b = ip.data() + 9;
+    bool ok = a[0] == 1 && a[3] == 0 && a[6] == 0 && a[2] == 0 && a[5] == 1 && a[8] == 0;
+    for (int j = 0; j < 3; j++)
+      for (int k = 0; k < 3; k++) ok = ok && b[k * 3 + j] == a[(2 - k) * 3 + (2 - j)];
+    if (ok) {
+      pl.st_tp = true;
+      pl.st_pint[0] = a[1];
+      pl.st_pint[1] = a[4];
+      pl.st_pint[2] = a[7];
+      pl.st_gchild.upload(gchild.data(), gchild.size(), s);
+      pl.st_gmask.upload(gmask.data(), gmask.size(), s);
+    }
+  }
   pl.st_runs.upload(runs.data(), runs.size(), s);
   pl.st_f.alloc(std::max<int64_t>(n_ent, 1));
   pl.st_hzoff.upload(hz_off.data(), hz_off.size(), s);
@@ -312,6 +341,98 @@ __global__ void __launch_bounds__(CH_THREADS) k_stale_chain(
   }
 }
 
+// Order-2 chained part.  A group's stale terms are the child interpolation
+// P_c (x) .. (x) P_c applied to the previous group's values, so instead of
+// per-entry term lists the walk applies P_c axis by axis: the previous
+// group's values go to the slots it takes (all other slots zero), one lane
+// per line of three slots applies the 1D interpolation along each axis, and
+// every needed slot's result plus the entry's fresh part is the entry's
+// value.  One block per run; chunks of consecutive groups (their child
+// numbers, slot masks and fresh parts) are staged in shared memory by the
+// whole block and walked by warp 0.
+constexpr int TP_G = 128;        // groups per chunk
+constexpr int TP_E = 4096;       // entries per chunk
+constexpr int TP_THREADS = 128;
+static_assert(TP_G == TP_THREADS, "one group test per thread");
+
+// parent -> child along one axis (child bit cb): the outer rows copy parent
+// nodes, the middle row is (pa, pb, pc) (mirrored for the second child)
+__device__ __forceinline__ void ip_line(double &a, double &b, double &c, double pa, double pb, double pc, bool cb)
+{
+  const double y0 = cb ? b : a, y2 = cb ? c : b;
+  const double y1 = fma(pc, cb ? a : c, fma(pb, b, pa * (cb ? c : a)));
+  a = y0;
+  b = y1;
+  c = y2;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(TP_THREADS) k_stale_chain_tp(
+    const int32_t *__restrict__ runs, int64_t n_runs, const int32_t *__restrict__ gstart,
+    const int32_t *__restrict__ gchild, const uint32_t *__restrict__ gmask, const double *__restrict__ f,
+    double *__restrict__ v, double pa, double pb, double pc)
+{
+  constexpr int NPE = DIM == 2 ? 9 : (DIM == 3 ? 27 : 81), NL = NPE / 3;
+  __shared__ double fS[TP_E];
+  __shared__ double m[NPE], prevS[NPE];
+  __shared__ uint32_t mS[TP_G * 6];
+  __shared__ int32_t cS[TP_G], gS[TP_G + 1];
+  const int64_t run = blockIdx.x;
+  if (run >= n_runs) return;
+  const int32_t g_end = runs[2 * run + 1];
+  int32_t g0 = runs[2 * run];
+  while (g0 < g_end) {
+    const int32_t e0 = gstart[g0];
+    // chunk: the groups [g0, g0 + cg) whose entries fit (monotone test)
+    const int32_t gt = g0 + (int32_t) threadIdx.x;
+    const int ok = (gt < g_end && gstart[gt + 1] - e0 <= TP_E) ? 1 : 0;
+    const int cg_raw = __syncthreads_count(ok);
+    const int cg = cg_raw > 0 ? cg_raw : 1;   // a group has at most NPE < TP_E entries
+    const int32_t e1 = gstart[g0 + cg];
+    for (int k = threadIdx.x; k <= cg; k += TP_THREADS) gS[k] = gstart[g0 + k] - e0;
+    for (int k = threadIdx.x; k < cg; k += TP_THREADS) cS[k] = gchild[g0 + k];
+    for (int k = threadIdx.x; k < cg * 6; k += TP_THREADS) mS[k] = gmask[(int64_t) g0 * 6 + k];
+    for (int32_t e = threadIdx.x; e < e1 - e0; e += TP_THREADS) fS[e] = f[e0 + e];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      for (int j = 0; j < cg; j++) {
+        const uint32_t *mk = mS + j * 6;   // need[3], take[3]
+        const unsigned ch = (unsigned) cS[j];
+        for (int q = lane; q < NPE; q += 32) m[q] = ((mk[3 + (q >> 5)] >> (q & 31)) & 1u) ? prevS[q] : 0.0;
+        __syncwarp();
+#pragma unroll
+        for (int ax = 0; ax < DIM; ax++) {
+          const int s = ax == 0 ? 1 : (ax == 1 ? 3 : (ax == 2 ? 9 : 27));
+          if (lane < NL) {
+            const int base = (lane % s) + (lane / s) * 3 * s;
+            double a = m[base], b = m[base + s], c = m[base + 2 * s];
+            ip_line(a, b, c, pa, pb, pc, (ch >> ax) & 1u);
+            m[base] = a;
+            m[base + s] = b;
+            m[base + 2 * s] = c;
+          }
+          __syncwarp();
+        }
+        const int ge = gS[j];
+        for (int q = lane; q < NPE; q += 32) {
+          const uint32_t w = mk[q >> 5];
+          if ((w >> (q & 31)) & 1u) {
+            int r = __popc(w & ((1u << (q & 31)) - 1u));   // rank among the needed slots
+            for (int ww = 0; ww < (q >> 5); ww++) r += __popc(mk[ww]);
+            const double val = fS[ge + r] + m[q];
+            v[e0 + ge + r] = val;
+            prevS[q] = val;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    g0 += cg;
+  }
+}
+
 void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
 {
   if (!pl.st_ready || pl.st_n_runs == 0) return;
@@ -323,6 +444,26 @@ void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
   const size_t smem = (size_t) ch_t * 12 + (size_t) 2 * CH_E * 8 + (size_t) npe * 8 + (size_t) (CH_E + 1) * 4
                       + (size_t) (CH_G + 1) * 4 + 64;
   const unsigned blocks = (unsigned) pl.st_n_runs;
+  if (pl.st_tp) {
+    if (xq) throw std::runtime_error("stale_eval: the order-2 walk has no fixed-point variant");
+    k_stale_fresh<false><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, x, nullptr,
+                                                            pl.st_f.p);
+    const double pa = pl.st_pint[0], pb = pl.st_pint[1], pc = pl.st_pint[2];
+    switch (pl.dim) {
+      case 2: k_stale_chain_tp<2><<<blocks, TP_THREADS, 0, s>>>(pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p,
+                                                                pl.st_gchild.p, pl.st_gmask.p, pl.st_f.p, pl.st_v.p,
+                                                                pa, pb, pc); break;
+      case 3: k_stale_chain_tp<3><<<blocks, TP_THREADS, 0, s>>>(pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p,
+                                                                pl.st_gchild.p, pl.st_gmask.p, pl.st_f.p, pl.st_v.p,
+                                                                pa, pb, pc); break;
+      default: k_stale_chain_tp<4><<<blocks, TP_THREADS, 0, s>>>(pl.st_runs.p, pl.st_n_runs, pl.st_gstart.p,
+                                                                 pl.st_gchild.p, pl.st_gmask.p, pl.st_f.p, pl.st_v.p,
+                                                                 pa, pb, pc); break;
+    }
+    check_launch("stale_eval_tp");
+    pl.n_launch += 2;
+    return;
+  }
   if (xq) {
     k_stale_fresh<true><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, nullptr, xq,
                                                            pl.st_f.p);
