@@ -49,6 +49,8 @@ def parse():
                     help="moving-ball level of the Poisson solves (FP64 vs mixed PCG); 0 skips them")
     ap.add_argument("--batch", type=int, default=512, help="problems in the batched 3D Poisson solve; 0 skips it")
     ap.add_argument("--batch-max-elements", type=float, default=1e6)
+    ap.add_argument("--q2-level", type=int, default=6,
+                    help="moving-ball level of the Q2 product section (0 skips it)")
     ap.add_argument("--serve", type=int, default=48, help="requests in the served stream; 0 skips it")
     ap.add_argument("--serve-max-elements", type=float, default=5e6)
     return ap.parse_args()
@@ -414,6 +416,49 @@ def run_serve(a, dkt):
     return out
 
 
+def run_q2(a, dkt, dev):
+    """The Q2 half of the moving-ball matvec: Laplacian+mass at order 2 on
+    the same mesh family (reference traversal, stale reads included), with
+    the sum-factorised FP64 kernel; inputs resident, CUDA events on the
+    launching stream."""
+    import torch
+    t0 = time.perf_counter()
+    tc, tl = moving_ball(dkt, a.q2_level, device=True)
+    da = dkt.DA(tc, tl, 4, order=2, max_depth=MD)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    t_setup = time.perf_counter() - t0
+    st = A.stats()
+    xd = torch.from_numpy(dkt.uniform_pm1(2, da.n)).to(dev)
+    yd = torch.empty_like(xd)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(a.warmup, 3)):
+        A.matvec(xd, yd, stream=stream)
+    steps = max(5, min(a.steps, 20))
+    torch.cuda.synchronize(dev)
+    A.kernel_timing(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        A.matvec(xd, yd, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = ev0.elapsed_time(ev1) / steps
+    k_ms, k_launches = A.kernel_timing(False)
+    k_avg_s = (k_ms / max(k_launches, 1)) / 1e3
+    flops = q2sf_flops(4, st["leaves"], st["hanging_leaves"])
+    peak64 = dkt.probe_device()["fp64_fma_tflops"]
+    return {"workload": "moving-ball spacetime matvec, dim 4, Q2 Laplacian+mass, FP64, level %d, max_depth %d"
+                        % (a.q2_level, MD),
+            "elements": int(da.n_elem), "nodes": int(da.n), "leaf_visits": st["leaves"],
+            "hanging_leaves": st["hanging_leaves"], "stale_slots": st["stale_slots"],
+            "elem_matvecs_per_s": da.n_elem / (ms / 1e3), "ms_per_step": ms, "steps": steps,
+            "kernel": "k_matvec_q2sf", "kernel_ms": k_avg_s * 1e3,
+            "fp64_pipe": {"achieved_tflops": flops / k_avg_s / 1e12, "peak_tflops": peak64,
+                          "frac": flops / k_avg_s / 1e12 / peak64, "flops_per_launch": flops,
+                          "peak_kind": "measured (FP64 FMA probe, this run)"},
+            "setup_s": t_setup}
+
+
 def run_gpu(a, rank, world, local_rank):
     import torch
     import __graft_entry__ as ge
@@ -517,6 +562,8 @@ def run_gpu(a, rank, world, local_rank):
     }
     if fp64 is not None:
         out["fp64_pipe"] = fp64
+    if a.q2_level > 0 and a.order == 1:
+        out["q2"] = run_q2(a, dkt, dev)
     if a.solve_level > 0:
         out["solve"] = run_solves(a, dkt, dev)
     if a.batch > 0:

@@ -86,6 +86,8 @@ def load(build_if_missing=True):
         "dkt_mesh_gaussian_points": ([I64, I, I, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, P], I),
         "dkt_mesh_tree_from_points": ([P, I64, I, I, I64, P, P, P], I),
         "dkt_mesh_tree_from_points_device": ([P, I64, I, I, I64, P, P, P], I),
+        "dkt_mesh_function2octree": ([P, P, I, I, I, I, ctypes.c_double, I, P, P, P], I),
+        "dkt_write_vtu": ([ctypes.c_char_p, I, I, P, P, I64, P, ctypes.c_char_p], I),
         "dkt_mesh_moving_ball": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
         "dkt_free": ([P], None),
         "dkt_mesh_moving_ball_device": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
@@ -366,6 +368,49 @@ def tree_from_points(points, dim, max_depth, max_pts=1, device=False):
     fn = load().dkt_mesh_tree_from_points_device if device else load().dkt_mesh_tree_from_points
     _check(fn(_p(pts), pts.shape[0], dim, max_depth, max_pts, ctypes.byref(n), ctypes.byref(c), ctypes.byref(lv)))
     return _take_cells(n, c, lv, dim)
+
+
+_FIELD_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int64, ctypes.c_int,
+                             ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p)
+
+
+def function2octree(func, n_vars, dim, max_depth, order=1, interp_tol=1e-3, balance=True):
+    """ot::function2Octree (balance=False) or the tree of ot::DA(func, ...)
+    (balance=True), built on the GPU.  func(x) takes points x [n, dim] in
+    [0, 1]^dim and returns the fields' values [n, n_vars]; it is called on
+    batches of points."""
+    err = []
+
+    def cb(xp, n, d, outp, nv, _user):
+        try:
+            x = np.ctypeslib.as_array(xp, shape=(n, d))
+            out = np.ctypeslib.as_array(outp, shape=(n, nv))
+            out[...] = np.asarray(func(x), dtype=np.float64).reshape(n, nv)
+            return 0
+        except Exception as e:   # reported after the call
+            err.append(e)
+            return 1
+
+    fn = _FIELD_FN(cb)
+    n, c, lv = ctypes.c_int64(0), ctypes.c_void_p(), ctypes.c_void_p()
+    rc = load().dkt_mesh_function2octree(ctypes.cast(fn, ctypes.c_void_p), None, int(n_vars), int(dim),
+                                         int(max_depth), int(order), float(interp_tol), 1 if balance else 0,
+                                         ctypes.byref(n), ctypes.byref(c), ctypes.byref(lv))
+    if err:
+        raise err[0]
+    _check(rc)
+    return _take_cells(n, c, lv, dim)
+
+
+def write_vtu(path, coords, levels, dim, max_depth, cell_values=None, name="value"):
+    """io::vtk::oct2vtu: write the tree (dim 2 or 3) as a VTU file."""
+    c = np.ascontiguousarray(coords, dtype=np.uint32).reshape(-1, dim)
+    lv = np.ascontiguousarray(levels, dtype=np.uint8)
+    cv = None if cell_values is None else np.ascontiguousarray(cell_values, dtype=np.float64)
+    if cv is not None and cv.size != lv.size:
+        raise ValueError("one cell value per cell")
+    _check(load().dkt_write_vtu(os.fsencode(path), int(dim), int(max_depth), _p(c), _p(lv), lv.size,
+                                None if cv is None else _p(cv), name.encode()))
 
 
 def curve_tables(curve, dim):

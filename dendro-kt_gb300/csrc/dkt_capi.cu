@@ -30,6 +30,8 @@ void sphere_shell_device(int dim, int md, int level, double R, double w, const d
                          int64_t &n_out, cudaStream_t s);
 void tree_from_points_device(const uint32_t *pts_host, int64_t n, int dim, int md, int64_t max_pts,
                              DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s);
+void function2octree_device(FieldFn fn, void *user, int n_vars, int dim, int md, int p, double tol, bool balance,
+                            DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s);
 void moving_ball_device(int md, int level, double R, double w, const double *c0, const double *c1,
                         DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s);
 void unpack_cells_to_host(const DBuf<uint64_t> &keys, int64_t n, int dim, int md, uint32_t *coords, uint8_t *levels,
@@ -676,6 +678,39 @@ int dkt_mesh_tree_from_points_device(const uint32_t *pts, int64_t n, int dim, in
     *n_out = nc;
     *coords = c;
     *levels = l;
+    return DKT_OK;
+  });
+}
+
+int dkt_mesh_function2octree(dkt_field_fn fn, void *user, int n_vars, int dim, int max_depth, int order,
+                             double interp_tol, int balance, int64_t *n_out, uint32_t **coords, uint8_t **levels)
+{
+  if (!fn || !n_out || !coords || !levels || n_vars < 1 || n_vars > 64 || dim < 2 || dim > 4 || order < 1 ||
+      order > 2 || max_depth < 1 || dim * max_depth + 6 > 64 || !(interp_tol >= 0))
+    return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    dkt::DBuf<uint64_t> keys;
+    int64_t nc = 0;
+    dkt::function2octree_device(fn, user, n_vars, dim, max_depth, order, interp_tol, balance != 0, keys, nc, 0);
+    uint32_t *c = (uint32_t *) std::malloc((size_t) nc * dim * sizeof(uint32_t) + 1);
+    uint8_t *l = (uint8_t *) std::malloc((size_t) nc + 1);
+    if (!c || !l) { std::free(c); std::free(l); return fail(DKT_E_NOMEM, "host allocation failed"); }
+    dkt::unpack_cells_to_host(keys, nc, dim, max_depth, c, l, 0);
+    *n_out = nc;
+    *coords = c;
+    *levels = l;
+    return DKT_OK;
+  });
+}
+
+int dkt_write_vtu(const char *path, int dim, int max_depth, const uint32_t *coords, const uint8_t *levels,
+                  int64_t n_cells, const double *cell_values, const char *cell_values_name)
+{
+  if (!path || (n_cells > 0 && (!coords || !levels)) || n_cells < 0 || (dim != 2 && dim != 3) || max_depth < 1 ||
+      max_depth > 30)
+    return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    dkt::write_vtu(path, dim, max_depth, coords, levels, n_cells, cell_values, cell_values_name);
     return DKT_OK;
   });
 }

@@ -12,11 +12,14 @@
 //    (src/tsort.cpp:566-854), organised by level sets instead of recursive
 //    bucketing.
 //  * the moving-ball spacetime mesh (dim 4).
+//  * VTU output of a tree (io::vtk::oct2vtu).
 #include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <stdexcept>
 #include <unordered_set>
 #include <vector>
@@ -578,6 +581,92 @@ std::vector<Cell> sphere_shell_tree(int dim, int md, int level, double R, double
   std::vector<Cell> leaves;
   shell_refine(root, dim, md, level, R, w, ctr, leaves);
   return balance(leaves, dim, md);
+}
+
+// ---------------------------------------------------------------------------
+// VTU output of an octree: io::vtk::oct2vtu (IO/vtk/include/oct2vtk.h:272-273,
+// IO/vtk/src/oct2vtk.cpp:1530-1760).  One cell per octant with its own 2^dim
+// corner points (integer lattice coordinates, UInt32, z = 0 in 2D), VTK
+// hexahedra in 3D and quads in 2D, inline base64 "binary" data arrays with a
+// UInt32 byte-count header; optionally one Float64 value per cell.
+// ---------------------------------------------------------------------------
+namespace {
+std::string base64(const std::vector<uint8_t> &in)
+{
+  static const char *tab = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
+  std::string out;
+  out.reserve((in.size() + 2) / 3 * 4);
+  size_t i = 0;
+  for (; i + 2 < in.size(); i += 3) {
+    const uint32_t v = (uint32_t) in[i] << 16 | (uint32_t) in[i + 1] << 8 | in[i + 2];
+    out += tab[v >> 18]; out += tab[(v >> 12) & 63]; out += tab[(v >> 6) & 63]; out += tab[v & 63];
+  }
+  if (i < in.size()) {
+    const uint32_t v = (uint32_t) in[i] << 16 | (i + 1 < in.size() ? (uint32_t) in[i + 1] << 8 : 0u);
+    out += tab[v >> 18]; out += tab[(v >> 12) & 63];
+    out += i + 1 < in.size() ? tab[(v >> 6) & 63] : '=';
+    out += '=';
+  }
+  return out;
+}
+template <typename T>
+std::string vtu_block(const std::vector<T> &v)
+{
+  const uint32_t nbytes = (uint32_t) (v.size() * sizeof(T));
+  std::vector<uint8_t> raw(4 + (size_t) nbytes);
+  for (int b = 0; b < 4; b++) raw[b] = (uint8_t) (nbytes >> (8 * b));   // little endian
+  if (nbytes) std::memcpy(raw.data() + 4, v.data(), nbytes);
+  return base64(raw);
+}
+}  // namespace
+
+void write_vtu(const char *path, int dim, int md, const uint32_t *coords, const uint8_t *levels, int64_t n,
+               const double *cell_values, const char *cell_values_name)
+{
+  if (dim != 2 && dim != 3) throw std::invalid_argument("VTU output is defined for dim 2 and 3");
+  if (n < 0 || (uint64_t) n * (1u << dim) > 0xFFFFFFFFull / 12) throw std::invalid_argument("too many cells for one VTU piece");
+  const int nv = 1 << dim;
+  std::vector<uint32_t> pts((size_t) n * nv * 3);
+  std::vector<int64_t> conn((size_t) n * nv), offs(n);
+  std::vector<uint8_t> types(n, (uint8_t) (dim == 3 ? 12 : 9));   // VTK_HEXAHEDRON, VTK_QUAD
+  // corner order of the VTK cell types: counter-clockwise in each z-layer
+  static const int ci[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+  for (int64_t e = 0; e < n; e++) {
+    if ((int) levels[e] > md) throw std::invalid_argument("cell level exceeds max_depth");
+    const uint32_t len = 1u << (md - levels[e]);
+    for (int k = 0; k < nv; k++)
+      for (int d = 0; d < 3; d++)
+        pts[((size_t) e * nv + k) * 3 + d] = d < dim ? coords[e * dim + d] + (((k >> d) & 1) ? len : 0u) : 0u;
+    for (int k = 0; k < nv; k++) conn[(size_t) e * nv + k] = e * nv + ci[k];
+    offs[e] = (int64_t) (e + 1) * nv;
+  }
+  std::FILE *fp = std::fopen(path, "w");
+  if (!fp) throw std::runtime_error(std::string("cannot open ") + path);
+  std::fprintf(fp, "<?xml version=\"1.0\"?>\n");
+  std::fprintf(fp, "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\" header_type=\"UInt32\">\n");
+  std::fprintf(fp, "  <UnstructuredGrid>\n");
+  std::fprintf(fp, "    <Piece NumberOfPoints=\"%lld\" NumberOfCells=\"%lld\">\n", (long long) n * nv, (long long) n);
+  std::fprintf(fp, "      <Points>\n");
+  std::fprintf(fp, "        <DataArray type=\"UInt32\" Name=\"Position\" NumberOfComponents=\"3\" format=\"binary\">\n");
+  std::fprintf(fp, "          %s\n        </DataArray>\n      </Points>\n", vtu_block(pts).c_str());
+  std::fprintf(fp, "      <Cells>\n");
+  std::fprintf(fp, "        <DataArray type=\"Int64\" Name=\"connectivity\" format=\"binary\">\n");
+  std::fprintf(fp, "          %s\n        </DataArray>\n", vtu_block(conn).c_str());
+  std::fprintf(fp, "        <DataArray type=\"Int64\" Name=\"offsets\" format=\"binary\">\n");
+  std::fprintf(fp, "          %s\n        </DataArray>\n", vtu_block(offs).c_str());
+  std::fprintf(fp, "        <DataArray type=\"UInt8\" Name=\"types\" format=\"binary\">\n");
+  std::fprintf(fp, "          %s\n        </DataArray>\n      </Cells>\n", vtu_block(types).c_str());
+  if (cell_values) {
+    std::vector<double> cv(cell_values, cell_values + n);
+    std::fprintf(fp, "      <CellData Scalars=\"%s\">\n", cell_values_name ? cell_values_name : "value");
+    std::fprintf(fp, "        <DataArray type=\"Float64\" Name=\"%s\" format=\"binary\">\n",
+                 cell_values_name ? cell_values_name : "value");
+    std::fprintf(fp, "          %s\n        </DataArray>\n      </CellData>\n", vtu_block(cv).c_str());
+  }
+  std::fprintf(fp, "    </Piece>\n  </UnstructuredGrid>\n</VTKFile>\n");
+  const bool bad = std::ferror(fp) != 0;
+  std::fclose(fp);
+  if (bad) throw std::runtime_error(std::string("write error on ") + path);
 }
 
 }  // namespace dkt

@@ -17,6 +17,10 @@ void builtin_operator(int kind, int dim, int p, int md, std::vector<double> &A, 
 // do not have the expected symmetric structure.
 bool q2_factors(double T[9], double lam[3], double pint[3]);
 
+// Field evaluation on a batch of points: x [n][dim] in the unit cube,
+// out [n][n_vars]; nonzero return = failure.
+typedef int (*FieldFn)(const double *x, int64_t n, int dim, double *out, int n_vars, void *user);
+
 struct Cell {
   uint32_t x[4];
   int lev;
@@ -29,5 +33,8 @@ std::vector<Cell> sphere_shell_tree(int dim, int md, int level, double R, double
 // Morton children in curve order then the curve rank of every Morton child
 // (rot), and the orientation of every Morton child (ht).
 void hilbert_tables(int dim, std::vector<int8_t> &rot, std::vector<int32_t> &ht, int &nrot);
+// VTU file of a tree (dim 2 or 3), optionally with one value per cell.
+void write_vtu(const char *path, int dim, int md, const uint32_t *coords, const uint8_t *levels, int64_t n,
+               const double *cell_values, const char *cell_values_name);
 
 }  // namespace dkt

@@ -7,6 +7,7 @@
 // every set operation is a radix sort + unique + binary search.
 #include <cmath>
 #include <vector>
+#include "dkt_host.h"
 #include "dkt_internal.cuh"
 
 namespace dkt {
@@ -287,7 +288,8 @@ __global__ void k_shell_test(const uint64_t *__restrict__ cells, int64_t n, int 
 
 // Level-by-level refinement driven by a refine-flag kernel, then 2:1 balance.
 template <typename TestFn>
-static void refine_device(int dim, int md, TestFn test, DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s)
+static void refine_device(int dim, int md, TestFn test, DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s,
+                          bool balance = true)
 {
   DBuf<uint64_t> frontier(1);
   const uint32_t z[MAX_DIM] = {0, 0, 0, 0};
@@ -319,7 +321,7 @@ static void refine_device(int dim, int md, TestFn test, DBuf<uint64_t> &out, int
     frontier = std::move(next);
     nf = nr * nc;
   }
-  balance_device(leaves, nl, dim, md, s);
+  if (balance) balance_device(leaves, nl, dim, md, s);
   out = std::move(leaves);
   n_out = nl;
 }
@@ -408,6 +410,122 @@ void tree_from_points_device(const uint32_t *pts_host, int64_t n, int dim, int m
   refine_device(dim, md, [&](const uint64_t *cells, int64_t nc, uint32_t *flag) {
     k_count_test<<<grid_for(nc), 256, 0, s>>>(cells, nc, dim, md, pk.p, n, max_pts, flag);
   }, out, n_out, s);
+}
+
+// ot::function2Octree (include/octUtils.h:180-417) on the device.  From the
+// root's children, level by level up to max_depth, a cell is split when
+// interpolating any field from its element nodes (order p) to the element
+// nodes of one of its children (IKD_Parent2Child) misses the field's values
+// there by more than interp_tol (max norm).  The fields are evaluated by the
+// caller on the host, on batches of points: per cell the parent's (p+1)^d
+// element nodes, then each child's, in Morton child order, coordinates
+// (anchor + len*i/p) / 2^max_depth as the reference forms them.  With
+// balance the tree is then 2:1 balanced, as ot::DA<dim>::DA(func, ...)
+// does (include/oda.tcc:67-88).
+__global__ void k_fill_u32(uint32_t *__restrict__ f, int64_t n, uint32_t v)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) f[i] = v;
+}
+__global__ void k_f2o_points(const uint64_t *__restrict__ cells, int64_t nc, int dim, int md, int p, int npe,
+                             double *__restrict__ pts)
+{
+  const int64_t idx = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int per = ((1 << dim) + 1) * npe;
+  if (idx >= nc * per) return;
+  const int64_t cell = idx / per;
+  const int rem = (int) (idx - cell * per), blk = rem / npe, node = rem - blk * npe;
+  uint32_t a[MAX_DIM];
+  int lev;
+  tdecode(cells[cell], dim, md, a, lev);
+  uint32_t len = 1u << (md - lev);
+  if (blk > 0) {
+    len >>= 1;
+    for (int d = 0; d < dim; d++) a[d] += (((blk - 1) >> d) & 1) ? len : 0u;
+  }
+  const double scale = 1.0 / (double) (1u << md);
+  int r = node;
+  for (int d = 0; d < dim; d++) {
+    const uint32_t i = (uint32_t) (r % (p + 1));
+    r /= p + 1;
+    const uint32_t c = (uint32_t) ((uint64_t) len * i / (uint32_t) p) + a[d];
+    pts[idx * dim + d] = scale * (double) c;
+  }
+}
+__global__ void k_f2o_test(int64_t nc, int dim, int p, int npe, const double *__restrict__ vals, int n_vars,
+                           const double *__restrict__ ip, double tol, uint32_t *__restrict__ flag)
+{
+  const int64_t cell = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= nc) return;
+  const int M = p + 1, nch = 1 << dim;
+  const double *base = vals + cell * (int64_t) (nch + 1) * npe * n_vars;
+  uint32_t split = 0u;
+  double a[81], b[81];
+  for (int c = 0; c < nch && !split; c++) {
+    for (int var = 0; var < n_vars && !split; var++) {
+      for (int k = 0; k < npe; k++) a[k] = base[(int64_t) k * n_vars + var];
+      // parent -> child c along each axis, the last axis first
+      for (int ax = dim - 1; ax >= 0; ax--) {
+        const double *A = ip + ((c >> ax) & 1) * M * M;
+        int stride = 1;
+        for (int t = 0; t < ax; t++) stride *= M;
+        for (int idx = 0; idx < npe; idx++) {
+          const int j = (idx / stride) % M, b0 = idx - j * stride;
+          double s = __dmul_rn(A[j], a[b0]);
+          for (int k = 1; k < M; k++) s = __dadd_rn(s, __dmul_rn(A[k * M + j], a[b0 + k * stride]));
+          b[idx] = s;
+        }
+        for (int idx = 0; idx < npe; idx++) a[idx] = b[idx];
+      }
+      const double *cv = base + (int64_t) (1 + c) * npe * n_vars;
+      double err = 0.0;
+      for (int k = 0; k < npe; k++) err = fmax(err, fabs(__dsub_rn(cv[(int64_t) k * n_vars + var], a[k])));
+      if (err > tol) split = 1u;
+    }
+  }
+  flag[cell] = split;
+}
+
+void function2octree_device(FieldFn fn, void *user, int n_vars, int dim, int md, int p, double tol, bool balance,
+                            DBuf<uint64_t> &out, int64_t &n_out, cudaStream_t s)
+{
+  if (dim < 2 || dim > MAX_DIM || p < 1 || p > 2 || n_vars < 1 || !fn || md < 1 || dim * md + 6 > 64)
+    throw std::invalid_argument("function2octree: bad argument");
+  const RefEl1D re = refel_1d(p);
+  std::vector<double> iph(re.ip0);
+  iph.insert(iph.end(), re.ip1.begin(), re.ip1.end());
+  DBuf<double> ip;
+  ip.upload(iph.data(), iph.size(), s);
+  int npe = 1;
+  for (int d = 0; d < dim; d++) npe *= p + 1;
+  const int per = ((1 << dim) + 1) * npe;
+  const int64_t batch = std::max<int64_t>(1, (int64_t(1) << 22) / per);   // about 4 M points per callback
+  refine_device(dim, md, [&](const uint64_t *cells, int64_t n, uint32_t *flag) {
+    uint64_t k0 = 0;
+    DKT_CUDA(cudaMemcpyAsync(&k0, cells, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    DKT_CUDA(cudaStreamSynchronize(s));
+    const int lev = (int) (k0 >> (dim * md));   // a frontier holds one level
+    if (lev == 0 || lev >= md) {
+      k_fill_u32<<<grid_for(n), 256, 0, s>>>(flag, n, lev == 0 ? 1u : 0u);
+      return;
+    }
+    const int64_t nb_max = std::min<int64_t>(batch, n);
+    DBuf<double> pts((size_t) nb_max * per * dim), vals((size_t) nb_max * per * n_vars);
+    std::vector<double> hp((size_t) nb_max * per * dim), hv((size_t) nb_max * per * n_vars);
+    for (int64_t c0 = 0; c0 < n; c0 += nb_max) {
+      const int64_t nb = std::min<int64_t>(nb_max, n - c0), np = nb * per;
+      k_f2o_points<<<grid_for(np), 256, 0, s>>>(cells + c0, nb, dim, md, p, npe, pts.p);
+      check_launch("f2o_points");
+      DKT_CUDA(cudaMemcpyAsync(hp.data(), pts.p, np * dim * sizeof(double), cudaMemcpyDeviceToHost, s));
+      DKT_CUDA(cudaStreamSynchronize(s));
+      if (fn(hp.data(), np, dim, hv.data(), n_vars, user) != 0)
+        throw std::runtime_error("function2octree: the field callback reported an error");
+      DKT_CUDA(cudaMemcpyAsync(vals.p, hv.data(), np * n_vars * sizeof(double), cudaMemcpyHostToDevice, s));
+      k_f2o_test<<<grid_for(nb, 128), 128, 0, s>>>(nb, dim, p, npe, vals.p, n_vars, ip.p, tol, flag + c0);
+      check_launch("f2o_test");
+      DKT_CUDA(cudaStreamSynchronize(s));
+    }
+  }, out, n_out, s, balance);
 }
 
 __global__ void k_unpack_cells(const uint64_t *__restrict__ k, uint32_t *__restrict__ x, uint8_t *__restrict__ lev,

@@ -42,6 +42,21 @@ int dkt_mesh_moving_ball(int max_depth, int level, double radius, double halfwid
 int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double halfwidth, const double *c0,
                                 const double *c1, int64_t *n_out, uint32_t **coords, uint8_t **levels);
 
+/* ot::function2Octree (include/octUtils.h:180-417) and, with balance = 1,
+ * the tree of ot::DA<dim>::DA(func, dofSz, comm, order, interp_tol)
+ * (include/oda.tcc:67-88), built on the current device.  From the root's
+ * children, level by level up to max_depth, a cell is split when
+ * interpolating any of the n_vars fields from its element nodes (order 1 or
+ * 2) to the element nodes of one of its children misses the field's values
+ * there by more than interp_tol (max norm).  The fields are evaluated by `fn`
+ * on the host, on batches of points (about 4 M per call): x [n][dim] with
+ * coordinates in [0, 1], out [n][n_vars]; a nonzero return aborts with
+ * DKT_E_INTERNAL.  With balance = 1 the tree is then 2:1 balanced.  Arrays
+ * are freed with dkt_free. */
+typedef int (*dkt_field_fn)(const double *x, int64_t n, int dim, double *out, int n_vars, void *user);
+int dkt_mesh_function2octree(dkt_field_fn fn, void *user, int n_vars, int dim, int max_depth, int order,
+                             double interp_tol, int balance, int64_t *n_out, uint32_t **coords, uint8_t **levels);
+
 /* Rotation tables of a space-filling curve, the data that _InitializeHcurve
  * (src/KDhcurvedata.cpp:23-57) loads: per orientation, the Morton children
  * in curve order then the curve rank of every Morton child (rot, 2^(dim+1)
@@ -62,6 +77,15 @@ int dkt_mesh_sphere_shell(int dim, int max_depth, int level, double radius, doub
                           int64_t *n_out, uint32_t **coords, uint8_t **levels);   /* host build, same tree */
 int dkt_mesh_sphere_shell_device(int dim, int max_depth, int level, double radius, double halfwidth,
                                  const double *centre, int64_t *n_out, uint32_t **coords, uint8_t **levels);
+
+/* io::vtk::oct2vtu (IO/vtk/include/oct2vtk.h:272-273): the tree as a VTK XML
+ * unstructured grid, one hexahedron (3D) or quad (2D) per cell with its own
+ * corner points in integer lattice coordinates (UInt32, 0..2^max_depth),
+ * inline base64 binary arrays.  cell_values (one double per cell, named
+ * cell_values_name) may be NULL.  dim 2 or 3, as the reference (VTK has no 4D
+ * cells; DKT_E_ARG for other dims). */
+int dkt_write_vtu(const char *path, int dim, int max_depth, const uint32_t *coords, const uint8_t *levels,
+                  int64_t n_cells, const double *cell_values, const char *cell_values_name);
 
 void dkt_free(void *p);
 

@@ -3,7 +3,10 @@
 // Test infrastructure only.  Compiled (by oracle/ref/Makefile) against the
 // unmodified Dendro-KT sources, a single-rank MPI stand-in and two LAPACK
 // routines; writes everything the parity tests pin:
-//   * the balanced tree      SFC_Tree::locTreeBalancing   (src/tsort.cpp:826-854)
+//   * the balanced tree      SFC_Tree::locTreeBalancing   (src/tsort.cpp:826-854),
+//     or (input kind 3) the tree of ot::DA<dim>::DA(func, ...) (include/oda.tcc:67-88):
+//     function2Octree (include/octUtils.h:180-417) of the two test fields
+//     below, then distTreeBalancing with one point per region
 //   * the DA node list       ot::DA::construct            (src/oda.cpp:52-151)
 //   * boundary node ids      (src/oda.cpp:145-150)
 //   * feMatrix::matVec output (FEM/include/feMatrix.h:189-259) for
@@ -159,6 +162,21 @@ class LapMassMat : public feMatrix<LapMassMat<dim>, dim> {
   }
 };
 
+// The two test fields of input kind 3: 1 / (eps + |x - c|^2), summed left to
+// right so that other implementations reproduce the values bit for bit.
+void test_fields(const double *x, double *out, unsigned dim)
+{
+  static const double c0[4] = {0.3, 0.6, 0.45, 0.5}, c1[4] = {0.7, 0.25, 0.55, 0.4};
+  double s0 = 0.01, s1 = 0.02;
+  for (unsigned d = 0; d < dim; d++) {
+    const double a = x[d] - c0[d], b = x[d] - c1[d];
+    s0 = s0 + a * a;
+    s1 = s1 + b * b;
+  }
+  out[0] = 1.0 / s0;
+  out[1] = 1.0 / s1;
+}
+
 double now_s()
 {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -179,10 +197,18 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
   const uint64_t nxIn = in.get<uint64_t>();
   std::vector<double> xIn(nxIn);
   in.arr(xIn.data(), nxIn);
+  const double interpTol = inputKind == 3 ? in.get<double>() : 0.0;
 
   std::vector<TN> tree;
   double t0 = now_s();
-  if (inputKind == 0) {
+  if (inputKind == 3) {
+    std::function<void(const double *, double *)> fx = [](const double *x, double *o) { test_fields(x, o, dim); };
+    const unsigned varIndex[2] = {0, 1};
+    std::vector<TN> complete;
+    ot::function2Octree<unsigned int, dim>(fx, 2, varIndex, 2, complete, maxDepth, interpTol, 0.3, order,
+                                           MPI_COMM_WORLD);
+    ot::SFC_Tree<unsigned int, dim>::distTreeBalancing(complete, tree, 1, 0.3, MPI_COMM_WORLD);
+  } else if (inputKind == 0) {
     std::vector<TN> pts;
     pts.reserve(n);
     for (uint64_t i = 0; i < n; i++) {

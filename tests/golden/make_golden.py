@@ -28,11 +28,12 @@ def build_ref():
     subprocess.run(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j2"], check=True)
 
 
-def run_ref(curve, dim, md, order, op, coords, levels, kind, seed, x=None):
+def run_ref(curve, dim, md, order, op, coords, levels, kind, seed, x=None, interp_tol=None):
     exe = os.path.join(REF_DIR, "ref_driver_" + curve)
     inp = os.path.join("/tmp", "dkt_golden_in.bin")
     out = os.path.join("/tmp", "dkt_golden_out.bin")
-    refio.write_input(inp, dim, md, order, op, coords, levels, input_kind=kind, seed=seed, x=x)
+    refio.write_input(inp, dim, md, order, op, coords, levels, input_kind=kind, seed=seed, x=x,
+                      interp_tol=interp_tol)
     subprocess.run([exe, inp, out], check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return refio.read_output(out, dim)
 
@@ -63,6 +64,10 @@ def cases():
         # RefElement::getElementSz() is 0 and HeatVec's Jacobian 1/(0/sz) is inf.
         out.append((f"{curve}_d3_p1_op6_gauss300", curve, 3, 8, 1, 6, ("gauss", 300)))
         out.append((f"{curve}_d3_p1_op6_ex1L4", curve, 3, 6, 1, 6, ("ex1", 4)))
+    # ot::DA<dim>::DA(func, ...): function2Octree of the two test fields of the
+    # driver (1 / (eps + |x - c|^2)), then 2:1 balance
+    for dim, md, order, tol in ((2, 8, 1, 0.2), (3, 7, 1, 1.0), (3, 7, 2, 1.0), (4, 6, 1, 4.0)):
+        out.append((f"morton_d{dim}_p{order}_op2_f2o", "morton", dim, md, order, 2, ("f2o", tol)))
     return out
 
 
@@ -71,7 +76,11 @@ def main(only=()):
     for name, curve, dim, md, order, op, (src, arg) in cases():
         if only and not any(o in name for o in only):
             continue
-        if src.startswith("gauss"):
+        if src == "f2o":
+            empty = np.zeros((0, dim), np.uint32)
+            r = run_ref(curve, dim, md, order, op, empty, np.zeros(0, np.uint8), 3, seed=1, interp_tol=arg)
+            inputs = dict(in_kind=3, in_coords=empty, in_levels=np.zeros(0, np.uint8), interp_tol=arg)
+        elif src.startswith("gauss"):
             gmd = md - 1 if src == "gauss_shift" else md
             pts = trees.gaussian_points(arg, dim, gmd, seed=0)
             if src == "gauss_shift":

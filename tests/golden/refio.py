@@ -9,7 +9,7 @@ import numpy as np
 
 
 def write_input(path, dim, max_depth, order, op, coords, levels=None, input_kind=0,
-                n_calls=1, seed=1, x=None):
+                n_calls=1, seed=1, x=None, interp_tol=None):
     coords = np.ascontiguousarray(coords, dtype=np.uint32).reshape(-1, dim)
     with open(path, "wb") as f:
         f.write(b"DKTI")
@@ -25,6 +25,8 @@ def write_input(path, dim, max_depth, order, op, coords, levels=None, input_kind
             x = np.ascontiguousarray(x, dtype=np.float64)
             f.write(struct.pack("<Q", x.size))
             f.write(x.tobytes())
+        if input_kind == 3:
+            f.write(struct.pack("<d", interp_tol))
 
 
 def read_output(path, dim):

@@ -81,3 +81,54 @@ def test_moving_ball_is_balanced(dkt):
     vol = np.sum((2.0 ** -sl.astype(np.float64)) ** dim)
     assert abs(vol - 1.0) < 1e-12
     assert sl.max() == 4
+
+
+def _vtu_arrays(path):
+    import base64
+    import xml.etree.ElementTree as ET
+    types = {"UInt32": np.uint32, "Int64": np.int64, "UInt8": np.uint8, "Float64": np.float64}
+    out = {}
+    for da in ET.parse(path).getroot().iter("DataArray"):
+        raw = base64.b64decode(da.text.strip())
+        nbytes = int(np.frombuffer(raw[:4], np.uint32)[0])
+        assert nbytes == len(raw) - 4
+        out[da.get("Name")] = np.frombuffer(raw[4:], types[da.get("type")])
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_write_vtu_roundtrip(dkt, tmp_path, dim):
+    """oct2vtu: every cell's corners, VTK corner order, cell types and cell
+    values come back from the file."""
+    md = 6
+    pts = dkt.gaussian_points(200, dim, md, seed=3)
+    c, l = dkt.tree_from_points(pts, dim, md)
+    path = str(tmp_path / "tree.vtu")
+    dkt.write_vtu(path, c, l, dim, md, cell_values=l.astype(np.float64), name="level")
+    a = _vtu_arrays(path)
+    nv = 1 << dim
+    P = a["Position"].reshape(-1, 3)
+    assert P.shape[0] == len(l) * nv
+    conn = a["connectivity"].reshape(-1, nv)
+    assert np.array_equal(a["offsets"], nv * np.arange(1, len(l) + 1))
+    assert np.all(a["types"] == (12 if dim == 3 else 9))
+    assert np.array_equal(a["level"], l.astype(np.float64))
+    lens = (1 << (md - l.astype(np.int64)))
+    first = P[conn[:, 0]][:, :dim].astype(np.int64)
+    assert np.array_equal(first, c.astype(np.int64))
+    # counter-clockwise around the bottom face: +x, then +y, then -x
+    assert np.array_equal(P[conn[:, 1]][:, 0].astype(np.int64) - first[:, 0], lens)
+    assert np.array_equal(P[conn[:, 2]][:, 1].astype(np.int64) - first[:, 1], lens)
+    assert np.array_equal(P[conn[:, 3]][:, 0].astype(np.int64), first[:, 0])
+    if dim == 3:
+        assert np.array_equal(P[conn[:, 4]][:, 2].astype(np.int64) - first[:, 2], lens)
+    else:
+        assert np.all(P[:, 2] == 0)
+
+
+def test_write_vtu_rejects_4d(dkt, tmp_path):
+    L = dkt.load()
+    c = np.zeros((1, 4), np.uint32)
+    l = np.zeros(1, np.uint8)
+    rc = L.dkt_write_vtu(str(tmp_path / "x.vtu").encode(), 4, 5, c.ctypes.data, l.ctypes.data, 1, None, b"v")
+    assert rc == dkt.E_ARG
