@@ -197,13 +197,27 @@ __global__ void __launch_bounds__(256) k_absmax(const double *__restrict__ x, in
   const unsigned long long *xb = reinterpret_cast<const unsigned long long *>(x);
   unsigned long long m = 0;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
-  int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + 3 * stride < n; i += 4 * stride) {
-    const unsigned long long a = xb[i] & ABS, b = xb[i + stride] & ABS, c = xb[i + 2 * stride] & ABS,
-                             d = xb[i + 3 * stride] & ABS;
-    m = max(m, max(max(a, b), max(c, d)));
+  const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if ((reinterpret_cast<uintptr_t>(x) & 15u) == 0) {
+    // 16-byte loads over the pairs, four in flight
+    const ulonglong2 *x2 = reinterpret_cast<const ulonglong2 *>(x);
+    const int64_t n2 = n >> 1;
+    int64_t i = tid;
+    for (; i + 3 * stride < n2; i += 4 * stride) {
+      const ulonglong2 a = __ldg(x2 + i), b = __ldg(x2 + i + stride), c = __ldg(x2 + i + 2 * stride),
+                       d = __ldg(x2 + i + 3 * stride);
+      m = max(m, max(max(a.x & ABS, a.y & ABS), max(b.x & ABS, b.y & ABS)));
+      m = max(m, max(max(c.x & ABS, c.y & ABS), max(d.x & ABS, d.y & ABS)));
+    }
+    for (; i < n2; i += stride) {
+      const ulonglong2 a = __ldg(x2 + i);
+      m = max(m, max(a.x & ABS, a.y & ABS));
+    }
+    if (tid == 0 && (n & 1)) m = max(m, xb[n - 1] & ABS);
+  } else {
+    // an 8-byte-aligned view (e.g. an offset slice): scalar loads
+    for (int64_t i = tid; i < n; i += stride) m = max(m, xb[i] & ABS);
   }
-  for (; i < n; i += stride) m = max(m, xb[i] & ABS);
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
   __syncthreads();

@@ -146,6 +146,15 @@ void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s)
   }
   if (!runs.empty()) runs.push_back((int32_t) gstart.size());
   gstart.push_back(n_ent);
+  {
+    // longest runs first: the chain kernels hand runs out in this order
+    std::vector<std::pair<int32_t, int32_t>> rp;
+    for (size_t k = 0; k + 1 < runs.size(); k += 2) rp.emplace_back(runs[k], runs[k + 1]);
+    std::stable_sort(rp.begin(), rp.end(), [&](const std::pair<int32_t, int32_t> &a, const std::pair<int32_t, int32_t> &b) {
+      return gstart[a.second] - gstart[a.first] > gstart[b.second] - gstart[b.first];
+    });
+    for (size_t k = 0; k < rp.size(); k++) { runs[2 * k] = rp[k].first; runs[2 * k + 1] = rp[k].second; }
+  }
   // per hazard leaf: entry id of (h-1, q) for each slot it reads stale
   std::vector<int32_t> hz_off(H, -1), hz_tab;
   for (int64_t h = 0; h < H; h++) {
@@ -261,8 +270,7 @@ __global__ void __launch_bounds__(CH_THREADS) k_stale_chain(
   int32_t *iS = reinterpret_cast<int32_t *>(carry + max_grp);   // [ch_t]
   int32_t *rS = iS + ch_t;                                  // [CH_E + 1]
   int32_t *gS = rS + CH_E + 1;                              // [CH_G + 1]
-  const int64_t run = blockIdx.x;
-  if (run >= n_runs) return;
+  for (int64_t run = blockIdx.x; run < n_runs; run += gridDim.x) {
   const int32_t g_end = runs[2 * run + 1];
   int32_t g0 = runs[2 * run];
   int32_t carry_base = 0;   // entry id of carry[0]
@@ -339,6 +347,7 @@ __global__ void __launch_bounds__(CH_THREADS) k_stale_chain(
     __syncthreads();
     g0 += cg;
   }
+  }
 }
 
 // Order-2 chained part.  A group's stale terms are the child interpolation
@@ -377,8 +386,7 @@ __global__ void __launch_bounds__(TP_THREADS) k_stale_chain_tp(
   __shared__ double m[NPE], prevS[NPE];
   __shared__ uint32_t mS[TP_G * 6];
   __shared__ int32_t cS[TP_G], gS[TP_G + 1];
-  const int64_t run = blockIdx.x;
-  if (run >= n_runs) return;
+  for (int64_t run = blockIdx.x; run < n_runs; run += gridDim.x) {
   const int32_t g_end = runs[2 * run + 1];
   int32_t g0 = runs[2 * run];
   while (g0 < g_end) {
@@ -431,6 +439,21 @@ __global__ void __launch_bounds__(TP_THREADS) k_stale_chain_tp(
     __syncthreads();
     g0 += cg;
   }
+  }
+}
+
+// Blocks of a chain launch: one per SM at most, each taking runs in turn from
+// the list (longest first).  One block per run would fill the SMs' block
+// slots with short-lived chain blocks at the start of the product and hold
+// back the leaf kernel it overlaps (level-8 moving ball: 3.93 ms for the
+// leaf kernel beside a one-block-per-run chain, 3.80 ms beside this one;
+// 3.60 ms alone).
+static unsigned chain_blocks(int64_t n_runs)
+{
+  int dev = 0, sms = 0;
+  DKT_CUDA(cudaGetDevice(&dev));
+  DKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  return (unsigned) std::max<int64_t>(1, std::min<int64_t>(n_runs, (int64_t) std::max(sms, 1)));
 }
 
 void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
@@ -443,7 +466,7 @@ void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)
   const int ch_t = std::max(1024, npe * npe);
   const size_t smem = (size_t) ch_t * 12 + (size_t) 2 * CH_E * 8 + (size_t) npe * 8 + (size_t) (CH_E + 1) * 4
                       + (size_t) (CH_G + 1) * 4 + 64;
-  const unsigned blocks = (unsigned) pl.st_n_runs;
+  const unsigned blocks = chain_blocks(pl.st_n_runs);
   if (pl.st_tp) {
     if (xq) throw std::runtime_error("stale_eval: the order-2 walk has no fixed-point variant");
     k_stale_fresh<false><<<grid_for(ne, 256), 256, 0, s>>>(ne, pl.st_row.p, pl.st_idx.p, pl.st_w.p, x, nullptr,

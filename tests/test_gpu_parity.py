@@ -466,3 +466,22 @@ def test_function2octree_complete_and_errors(dkt):
         raise ValueError("field failed")
     with pytest.raises(ValueError):
         dkt.function2octree(bad, 1, dim, md, interp_tol=1.0)
+
+
+def test_offset_views_as_vectors(dkt):
+    """Input and output vectors that are 8-byte but not 16-byte aligned views
+    (slices of a larger buffer) give the same product as aligned copies."""
+    import torch
+    md, level = 10, 4
+    tc, tl = dkt.moving_ball_tree(max_depth=md, level=level, device=True)
+    da = dkt.DA(tc, tl, 4, order=1, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    x = torch.from_numpy(dkt.uniform_pm1(2, da.n)).cuda()
+    y = torch.empty_like(x)
+    A.matvec(x, y)
+    xb = torch.zeros(da.n + 1, dtype=torch.float64, device="cuda")
+    yb = torch.zeros(da.n + 1, dtype=torch.float64, device="cuda")
+    xb[1:] = x
+    A.matvec(xb[1:], yb[1:])
+    torch.cuda.synchronize()
+    assert torch.equal(yb[1:], y)
