@@ -129,12 +129,12 @@ def traffic(kernel, leaf_visits):
 
 def q2sf_flops(dim, leaves, hanging):
     """FP64 flops (FMA = 2) of the sum-factorised Q2 kernel: per leaf the
-    forward and transposed 1D transforms (local axes 9 flops per 3-node line,
-    the shuffled last axis 5 per value) and the diagonal; per hanging leaf the
-    sparse child interpolation and its transpose (5 flops per line or value)."""
+    forward and transposed 1D transforms (6 flops per 3-node line, every axis
+    applied where it is local to a thread) and the diagonal; per hanging leaf
+    the sparse child interpolation and its transpose (5 flops per line)."""
     npe = 3 ** dim
-    per_leaf = 2 * ((dim - 1) * (npe // 3) * 9 + npe * 5) + npe
-    per_hang = 2 * ((dim - 1) * (npe // 3) * 5 + npe * 5)
+    per_leaf = 2 * dim * (npe // 3) * 6 + npe
+    per_hang = 2 * dim * (npe // 3) * 5
     return leaves * per_leaf + hanging * per_hang
 
 

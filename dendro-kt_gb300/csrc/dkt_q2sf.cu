@@ -8,8 +8,8 @@
 //   D_L[r] = alpha_L sum_t lam[digit_t(r)] + beta_L,
 // so the elemental product of fem::matvec (matvec.h:467-468) becomes a 1D
 // transform along every axis, a diagonal scaling and the transposed
-// transforms: about 2 d 3^d (4/3) + 3^d FP64 operations instead of the
-// 2 (3^d)^2 of the dense contraction (4D: 1,053 against 13,122).  The
+// transforms: 2 d 3^(d-1) 4 + 3^d FP64 operations instead of the 2 (3^d)^2
+// of the dense contraction (4D: 945 against 13,122).  The
 // transform is used in its unit-diagonal form U = diag(1/T_kk) T, rows
 // (1, u01, 1), (u10, 1, u10), (-1, 0, 1), whose line products take four
 // operations; the row scales move into D.  The child interpolation
@@ -18,10 +18,12 @@
 // parent node).  FP64 on this part runs at about 2 FMA per clock per SM, so
 // operation count is what bounds the kernel.
 //
-// Three threads work on one leaf: thread k holds the 3^(d-1) values whose
-// last-axis index is k.  Transforms along the other axes are local; the
-// last axis is applied with two warp shuffles per value.  A warp takes ten
-// leaves (lanes 30 and 31 idle).  Leaves run in an order with the hanging
+// Three threads work on one leaf, each holding 3^(d-1) of its values, in one
+// of two layouts (split by the last-axis index or by the first-axis index);
+// every 1D operator runs in the layout where its axis is local to a thread,
+// and the values change layout through shared memory (two exchanges per
+// leaf, four for a hanging leaf).  A warp takes ten leaves (lanes 30 and 31
+// idle).  Leaves run in an order with the hanging
 // leaves first (stable), so almost every warp is uniform in whether it runs
 // the interpolation.
 #include <algorithm>
@@ -79,53 +81,76 @@ __device__ __forceinline__ void line_pt(double &a, double &b, double &c, const S
   c = cb ? lo : hi;
 }
 
-// Row k of a 3x3 matrix G given row-major as g[9], as (own, next, next-next)
-// coefficients: out_k = cs w_k + c1 w_{k+1} + c2 w_{k+2} (indices mod 3).
-__device__ __forceinline__ void row_of(const double (&g)[9], int k, double &cs, double &c1, double &c2)
+// Two layouts of a leaf's 3^d values over its three threads.  Layout A:
+// thread k holds the ranks k*NV + j, j < NV (last-axis digit k), so axes
+// 0..d-2 are local; layout B: thread k holds the ranks k + 3 j (first-axis
+// digit k), so axes 1..d-1 are local.  Every 1D operator is applied where
+// its axis is local; the values change layout through a per-leaf buffer in
+// shared memory.
+template <int DIM, int AX, typename Op>
+__device__ __forceinline__ void axis_a(double (&v)[SfDim<DIM>::NV], Op op)
 {
-  cs = k == 0 ? g[0] : (k == 1 ? g[4] : g[8]);
-  c1 = k == 0 ? g[1] : (k == 1 ? g[5] : g[6]);
-  c2 = k == 0 ? g[2] : (k == 1 ? g[3] : g[7]);
+  static_assert(AX >= 0 && AX <= DIM - 2, "axis not local in layout A");
+  constexpr int s = AX == 0 ? 1 : (AX == 1 ? 3 : 9);
+#pragma unroll
+  for (int j = 0; j < SfDim<DIM>::NV; j++)
+    if ((j / s) % 3 == 0) op(AX, v[j], v[j + s], v[j + 2 * s]);
 }
-
-// Apply along the local axes 0..DIM-2 with op(a, b, c).
+template <int DIM, int AX, typename Op>
+__device__ __forceinline__ void axis_b(double (&v)[SfDim<DIM>::NV], Op op)
+{
+  static_assert(AX >= 1 && AX <= DIM - 1, "axis not local in layout B");
+  constexpr int s = AX == 1 ? 1 : (AX == 2 ? 3 : 9);
+#pragma unroll
+  for (int j = 0; j < SfDim<DIM>::NV; j++)
+    if ((j / s) % 3 == 0) op(AX, v[j], v[j + s], v[j + 2 * s]);
+}
 template <int DIM, typename Op>
-__device__ __forceinline__ void local_axes(double (&v)[SfDim<DIM>::NV], Op op)
+__device__ __forceinline__ void axes_a_all(double (&v)[SfDim<DIM>::NV], Op op)
 {
-  constexpr int NV = SfDim<DIM>::NV;
-#pragma unroll
-  for (int ax = 0; ax < DIM - 1; ax++) {
-    const int s = ax == 0 ? 1 : (ax == 1 ? 3 : 9);
-#pragma unroll
-    for (int j = 0; j < NV; j++)
-      if ((j / s) % 3 == 0) op(ax, v[j], v[j + s], v[j + 2 * s]);
-  }
+  axis_a<DIM, 0>(v, op);
+  if constexpr (DIM >= 3) axis_a<DIM, 1>(v, op);
+  if constexpr (DIM >= 4) axis_a<DIM, 2>(v, op);
 }
-// Apply along the last axis: every value mixes with the same slot of the two
-// sibling lanes.  last_axis_unit: the lane's own coefficient is 1.
-template <int DIM>
-__device__ __forceinline__ void last_axis_unit(double (&v)[SfDim<DIM>::NV], double c1, double c2, int l1, int l2)
+template <int DIM, typename Op>
+__device__ __forceinline__ void axes_b_all(double (&v)[SfDim<DIM>::NV], Op op)
 {
-#pragma unroll
-  for (int j = 0; j < SfDim<DIM>::NV; j++) {
-    const double w1 = __shfl_sync(0xffffffffu, v[j], l1);
-    const double w2 = __shfl_sync(0xffffffffu, v[j], l2);
-    v[j] = fma(c2, w2, fma(c1, w1, v[j]));
-  }
+  axis_b<DIM, 1>(v, op);
+  if constexpr (DIM >= 3) axis_b<DIM, 2>(v, op);
+  if constexpr (DIM >= 4) axis_b<DIM, 3>(v, op);
 }
-template <int DIM>
-__device__ __forceinline__ void last_axis(double (&v)[SfDim<DIM>::NV], double cs, double c1, double c2, int l1, int l2)
+// A -> B and B -> A through the leaf's buffer; idle lanes only synchronise.
+template <int NV>
+__device__ __forceinline__ void to_b(double (&v)[NV], double *buf, int k, bool act)
 {
+  if (act) {
 #pragma unroll
-  for (int j = 0; j < SfDim<DIM>::NV; j++) {
-    const double w1 = __shfl_sync(0xffffffffu, v[j], l1);
-    const double w2 = __shfl_sync(0xffffffffu, v[j], l2);
-    v[j] = fma(c2, w2, fma(c1, w1, cs * v[j]));
+    for (int j = 0; j < NV; j++) buf[k * NV + j] = v[j];
   }
+  __syncwarp();
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) v[j] = buf[k + 3 * j];
+  }
+  __syncwarp();
+}
+template <int NV>
+__device__ __forceinline__ void to_a(double (&v)[NV], double *buf, int k, bool act)
+{
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) buf[k + 3 * j] = v[j];
+  }
+  __syncwarp();
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) v[j] = buf[k * NV + j];
+  }
+  __syncwarp();
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(128) k_matvec_q2sf(
+__global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
     const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, const int32_t *__restrict__ order,
     int64_t n_leaf, SfCoef cf, const double *__restrict__ Dtab, const double *__restrict__ x, double *__restrict__ y,
@@ -133,36 +158,45 @@ __global__ void __launch_bounds__(128) k_matvec_q2sf(
     const double *__restrict__ stv, int conforming)
 {
   constexpr int NV = SfDim<DIM>::NV, NPE = SfDim<DIM>::NPE;
+  __shared__ double sbuf[4 * 10 * NPE];   // one buffer per leaf of the block (blockDim 128)
   const int lane = threadIdx.x & 31, slot = lane / 3, k = lane - 3 * slot;
-  const int64_t t = ((int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 10 + slot;
-  const bool valid = slot < 10 && t < n_leaf;
-  // sibling lanes of the same leaf; the idle lanes 30, 31 read themselves
-  const int l1 = slot < 10 ? 3 * slot + (k + 1) % 3 : lane;
-  const int l2 = slot < 10 ? 3 * slot + (k + 2) % 3 : lane;
+  const int warp = threadIdx.x >> 5;
+  const int64_t t = ((int64_t) blockIdx.x * 4 + warp) * 10 + slot;
+  const bool act = slot < 10;                 // lanes 30, 31 are idle
+  const bool valid = act && t < n_leaf;
+  double *buf = sbuf + (warp * 10 + (act ? slot : 0)) * NPE;
   const int64_t i = valid ? (int64_t) order[t] : 0;
   const uint32_t inf = valid ? info[i] : 0u;
   const int L = inf & 0xFFu;
   const unsigned child = (inf >> 8) & 0xFFu;
   const bool hang = valid && ((inf >> 16) & 1u);
-  const bool cb_last = (child >> (DIM - 1)) & 1u;
 
+  // own values in layout B
   double u[NV];
-  const int32_t *er = e2n + i * NPE + k * NV;
+  const int32_t *er = e2n + i * NPE;
 #pragma unroll
   for (int j = 0; j < NV; j++) {
-    const int32_t nd = valid ? er[j] : -1;
+    const int32_t nd = valid ? er[k + 3 * j] : -1;
     u[j] = nd >= 0 ? x[nd] : 0.0;
   }
   const bool any_h = __any_sync(0xffffffffu, hang);
-  uint32_t fmk = 0;   // fill bits of this thread's ranks k*NV .. k*NV+NV-1
+  uint32_t fA = 0, fB = 0;   // fill bits of the thread's ranks in layout A and in layout B
   int64_t h = 0;
   if (any_h) {
     double v[NV];
     if (hang) {
       h = hidx[i];
-      const int b0 = k * NV, w = b0 >> 5, sh = b0 & 31;   // b0 + NV <= 81 < 96: words w, w+1 <= 2
-      const uint64_t two = (uint64_t) fill[h * 3 + w] | ((uint64_t) fill[h * 3 + w + 1] << 32);
-      fmk = (uint32_t) (two >> sh) & ((1u << NV) - 1u);
+      const uint32_t w0 = fill[h * 3], w1 = fill[h * 3 + 1], w2 = fill[h * 3 + 2];
+      const int b0 = k * NV, sh = b0 & 31;   // ranks b0 .. b0+NV-1 lie in words b0>>5 and b0>>5 + 1
+      const uint64_t two = (b0 >> 5) == 0 ? ((uint64_t) w0 | ((uint64_t) w1 << 32))
+                                          : ((uint64_t) w1 | ((uint64_t) w2 << 32));
+      fA = (uint32_t) (two >> sh) & ((1u << NV) - 1u);
+#pragma unroll
+      for (int j = 0; j < NV; j++) {
+        const int r = k + 3 * j;
+        const uint32_t w = r < 32 ? w0 : (r < 64 ? w1 : w2);
+        fB |= ((w >> (r & 31)) & 1u) << j;
+      }
       const int32_t hz = hzoff ? hzoff[h] : -1;   // slots read from the emulated static buffer
       const int32_t *pr = p2n + h * NPE + k * NV;
 #pragma unroll
@@ -180,31 +214,23 @@ __global__ void __launch_bounds__(128) k_matvec_q2sf(
 #pragma unroll
       for (int j = 0; j < NV; j++) v[j] = 0.0;
     }
-    local_axes<DIM>(v, [&](int ax, double &a, double &b, double &c) { line_p(a, b, c, cf, (child >> ax) & 1u); });
-    {
-      // row k of the child interpolation along the last axis
-      const double g[9] = {cb_last ? 0.0 : 1.0, cb_last ? 1.0 : 0.0, 0.0,
-                           cb_last ? cf.pc : cf.pa, cf.pb, cb_last ? cf.pa : cf.pc,
-                           0.0, cb_last ? 0.0 : 1.0, cb_last ? 1.0 : 0.0};
-      double cs, c1, c2;
-      row_of(g, k, cs, c1, c2);
-      last_axis<DIM>(v, cs, c1, c2, l1, l2);
-    }
+    // parent -> child: axes 0..d-2 in layout A, the last axis in layout B
+    auto ip = [&](int ax, double &a, double &b, double &c) { line_p(a, b, c, cf, (child >> ax) & 1u); };
+    axes_a_all<DIM>(v, ip);
+    to_b<NV>(v, buf, k, act);
+    axis_b<DIM, DIM - 1>(v, ip);
     if (hang) {
 #pragma unroll
       for (int j = 0; j < NV; j++)
-        if (!((fmk >> j) & 1u)) u[j] = v[j];
+        if (!((fB >> j) & 1u)) u[j] = v[j];
     }
   }
-  // forward transform
-  local_axes<DIM>(u, [&](int, double &a, double &b, double &c) { line_t(a, b, c, cf); });
-  {
-    const double g[9] = {1.0, cf.u01, 1.0, cf.u10, 1.0, cf.u10, -1.0, 0.0, 1.0};
-    double cs, c1, c2;
-    row_of(g, k, cs, c1, c2);
-    last_axis_unit<DIM>(u, c1, c2, l1, l2);
-  }
-  // diagonal of level L
+  // forward transform: axes 1..d-1 in B, axis 0 in A
+  auto tf = [&](int, double &a, double &b, double &c) { line_t(a, b, c, cf); };
+  axes_b_all<DIM>(u, tf);
+  to_a<NV>(u, buf, k, act);
+  axis_a<DIM, 0>(u, tf);
+  // diagonal of level L (layout A: ranks k*NV + j)
   const double *Dl = Dtab + (int64_t) L * NPE + k * NV;
   if (scale == 1.0) {
 #pragma unroll
@@ -213,43 +239,35 @@ __global__ void __launch_bounds__(128) k_matvec_q2sf(
 #pragma unroll
     for (int j = 0; j < NV; j++) u[j] *= scale * __ldg(Dl + j);
   }
-  // transposed transform
-  {
-    const double g[9] = {1.0, cf.u10, -1.0, cf.u01, 1.0, 0.0, 1.0, cf.u10, 1.0};
-    double cs, c1, c2;
-    row_of(g, k, cs, c1, c2);
-    last_axis_unit<DIM>(u, c1, c2, l1, l2);
-  }
-  local_axes<DIM>(u, [&](int, double &a, double &b, double &c) { line_tt(a, b, c, cf); });
+  // transposed transform: axes 0..d-2 in A, the last axis in B
+  auto tt = [&](int, double &a, double &b, double &c) { line_tt(a, b, c, cf); };
+  axes_a_all<DIM>(u, tt);
+  to_b<NV>(u, buf, k, act);
+  axis_b<DIM, DIM - 1>(u, tt);
   if (valid) {
 #pragma unroll
     for (int j = 0; j < NV; j++) {
-      const int32_t nd = er[j];
+      const int32_t nd = er[k + 3 * j];
       if (nd >= 0) atomicAdd(y + nd, u[j]);
     }
   }
   if (any_h) {
-    // zero the filled ranks, interpolate back to the parent (matvec.h:482-522)
+    // zero the filled ranks, interpolate back to the parent (matvec.h:482-522):
+    // axes 1..d-1 in B, axis 0 in A
 #pragma unroll
     for (int j = 0; j < NV; j++)
-      if (!hang || ((fmk >> j) & 1u)) u[j] = 0.0;
-    local_axes<DIM>(u, [&](int ax, double &a, double &b, double &c) { line_pt(a, b, c, cf, (child >> ax) & 1u); });
-    {
-      // row k of the transposed interpolation along the last axis
-      const double g[9] = {cb_last ? 0.0 : 1.0, cb_last ? cf.pc : cf.pa, 0.0,
-                           cb_last ? 1.0 : 0.0, cf.pb, cb_last ? 0.0 : 1.0,
-                           0.0, cb_last ? cf.pa : cf.pc, cb_last ? 1.0 : 0.0};
-      double cs, c1, c2;
-      row_of(g, k, cs, c1, c2);
-      last_axis<DIM>(u, cs, c1, c2, l1, l2);
-    }
+      if (!hang || ((fB >> j) & 1u)) u[j] = 0.0;
+    auto pt = [&](int ax, double &a, double &b, double &c) { line_pt(a, b, c, cf, (child >> ax) & 1u); };
+    axes_b_all<DIM>(u, pt);
+    to_a<NV>(u, buf, k, act);
+    axis_a<DIM, 0>(u, pt);
     if (hang) {
       const int32_t *pr = p2n + h * NPE + k * NV;
 #pragma unroll
       for (int j = 0; j < NV; j++) {
         const int32_t pn = pr[j];
         // the reference masks parent slot q by the leaf's fill bit q
-        if (pn >= 0 && (conforming || !((fmk >> j) & 1u))) atomicAdd(y + pn, u[j]);
+        if (pn >= 0 && (conforming || !((fA >> j) & 1u))) atomicAdd(y + pn, u[j]);
       }
     }
   }
