@@ -468,7 +468,7 @@ int dkt_pcg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int precisi
   if (!plan || !b_dev || !x_dev || max_iter < 0 || !(tol > 0) || precision < 0 || precision > 1)
     return fail(DKT_E_ARG, "bad argument");
   if (precision == 1 && !plan->pl.f32_ready)
-    return fail(DKT_E_UNSUP, "mixed precision needs a Q1 built-in operator without stale parent reads");
+    return fail(DKT_E_UNSUP, "mixed precision needs a Q1 or Q2 built-in operator without stale parent reads");
   return guarded([&]() {
     return dkt::pcg_solve(plan->pl, b_dev, x_dev, precision, max_iter, tol, jacobi != 0, iters, refinements,
                           relres, (cudaStream_t) stream);
@@ -479,7 +479,7 @@ int dkt_matvec_f32(dkt_plan plan, const float *x_dev, float *y_dev, void *stream
 {
   if (!plan || !x_dev || !y_dev) return fail(DKT_E_ARG, "null argument");
   if (!plan->pl.f32_ready)
-    return fail(DKT_E_UNSUP, "binary32 product needs a Q1 built-in operator without stale parent reads");
+    return fail(DKT_E_UNSUP, "binary32 product needs a Q1 or Q2 built-in operator without stale parent reads");
   return guarded([&]() {
     const bool bc = dkt::op_has_bc(plan->pl.op.kind);
     dkt::q1f32_apply(plan->pl, x_dev, y_dev, bc, bc, (cudaStream_t) stream);

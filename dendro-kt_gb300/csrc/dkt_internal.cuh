@@ -197,6 +197,7 @@ struct Plan {
   int64_t sf_n_main = 0;             // leaves of the main launch (all, or those reading no stale slot)
   double sf_T[9] = {0}, sf_pint[3] = {0};
   DBuf<double> sf_D;
+  DBuf<float> sf_D32;
   DBuf<int32_t> sf_order;
   // binary32 variant of the same Q1 operators (inner solves).
   bool f32_ready = false;

@@ -456,12 +456,16 @@ __global__ void k_zero_ids_f(float *__restrict__ v, const uint32_t *__restrict__
   if (i < nb) v[ids[i]] = 0.0f;
 }
 
-// Binary32 product with the Q1 operator of the plan.  bc_in / bc_out zero the
+// Binary32 product with the built-in operator of the plan (Q1 here, Q2 in
+// dkt_q2sf.cu).  bc_in / bc_out zero the
 // domain-boundary entries of the input (through a scratch copy) and of the
 // output, as feMatrix::matVec does for the operators with boundary steps.
+void q2sf_f32(Plan &pl, const float *x, float *y, cudaStream_t s);
+
 void q1f32_apply(Plan &pl, const float *x, float *y, bool bc_in, bool bc_out, cudaStream_t s)
 {
-  if (!pl.f32_ready) throw std::runtime_error("binary32 product needs a Q1 built-in operator without stale parent reads");
+  if (!pl.f32_ready)
+    throw std::runtime_error("binary32 product needs a Q1 or Q2 built-in operator without stale parent reads");
   const int64_t n = pl.n_nodes;
   if (bc_in && pl.n_bdry > 0) {
     if (pl.x32.n < (size_t) n) pl.x32.alloc(n);
@@ -471,12 +475,16 @@ void q1f32_apply(Plan &pl, const float *x, float *y, bool bc_in, bool bc_out, cu
     pl.n_launch++;
     x = pl.x32.p;
   }
-  DKT_CUDA(cudaMemsetAsync(y, 0, n * sizeof(float), s));
-  switch (pl.dim) {
-    case 2: launch_q1f32<2>(pl, x, y, s); break;
-    case 3: launch_q1f32<3>(pl, x, y, s); break;
-    case 4: launch_q1f32<4>(pl, x, y, s); break;
-    default: throw std::runtime_error("unsupported dim");
+  if (pl.order == 2) {
+    q2sf_f32(pl, x, y, s);
+  } else {
+    DKT_CUDA(cudaMemsetAsync(y, 0, n * sizeof(float), s));
+    switch (pl.dim) {
+      case 2: launch_q1f32<2>(pl, x, y, s); break;
+      case 3: launch_q1f32<3>(pl, x, y, s); break;
+      case 4: launch_q1f32<4>(pl, x, y, s); break;
+      default: throw std::runtime_error("unsupported dim");
+    }
   }
   if (bc_out && pl.n_bdry > 0) {
     k_zero_ids_f<<<grid_for(pl.n_bdry), 256, 0, s>>>(y, pl.bdry.p, pl.n_bdry);

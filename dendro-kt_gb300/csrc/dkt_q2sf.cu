@@ -27,16 +27,18 @@
 // leaves first (stable), so almost every warp is uniform in whether it runs
 // the interpolation.
 #include <algorithm>
+#include <type_traits>
 #include "dkt_host.h"
 #include "dkt_internal.cuh"
 
 namespace dkt {
 
+template <typename V>
 struct SfCoef {
   // unit-diagonal transform U = diag(1/T_kk) T, rows (1, u01, 1), (u10, 1, u10), (-1, 0, 1)
-  double u01, u10;
+  V u01, u10;
   // middle row of the child-0 interpolation: y1 = pa x0 + pb x1 + pc x2
-  double pa, pb, pc;
+  V pa, pb, pc;
 };
 
 template <int DIM>
@@ -47,35 +49,39 @@ struct SfDim {
 
 // Line operators on (a, b, c) along one axis, in place.
 // U: 4 operations per line
-__device__ __forceinline__ void line_t(double &a, double &b, double &c, const SfCoef &k)
+template <typename V>
+__device__ __forceinline__ void line_t(V &a, V &b, V &c, const SfCoef<V> &k)
 {
-  const double s = a + c;
-  const double e0 = fma(k.u01, b, s), e1 = fma(k.u10, s, b), o = c - a;
+  const V s = a + c;
+  const V e0 = fma(k.u01, b, s), e1 = fma(k.u10, s, b), o = c - a;
   a = e0;
   b = e1;
   c = o;
 }
 // U^T: 4 operations per line
-__device__ __forceinline__ void line_tt(double &a, double &b, double &c, const SfCoef &k)
+template <typename V>
+__device__ __forceinline__ void line_tt(V &a, V &b, V &c, const SfCoef<V> &k)
 {
-  const double e = fma(k.u10, b, a), m = fma(k.u01, a, b);
+  const V e = fma(k.u10, b, a), m = fma(k.u01, a, b);
   a = e - c;
   b = m;
   c = e + c;
 }
 // parent -> child (forward interpolation), child bit cb along this axis
-__device__ __forceinline__ void line_p(double &a, double &b, double &c, const SfCoef &k, bool cb)
+template <typename V>
+__device__ __forceinline__ void line_p(V &a, V &b, V &c, const SfCoef<V> &k, bool cb)
 {
-  const double y0 = cb ? b : a, y2 = cb ? c : b;
-  const double y1 = fma(k.pc, cb ? a : c, fma(k.pb, b, k.pa * (cb ? c : a)));
+  const V y0 = cb ? b : a, y2 = cb ? c : b;
+  const V y1 = fma(k.pc, cb ? a : c, fma(k.pb, b, k.pa * (cb ? c : a)));
   a = y0;
   b = y1;
   c = y2;
 }
 // child -> parent (transposed interpolation)
-__device__ __forceinline__ void line_pt(double &a, double &b, double &c, const SfCoef &k, bool cb)
+template <typename V>
+__device__ __forceinline__ void line_pt(V &a, V &b, V &c, const SfCoef<V> &k, bool cb)
 {
-  const double lo = fma(k.pa, b, cb ? c : a), mid = fma(k.pb, b, cb ? a : c), hi = k.pc * b;
+  const V lo = fma(k.pa, b, cb ? c : a), mid = fma(k.pb, b, cb ? a : c), hi = k.pc * b;
   a = cb ? hi : lo;
   b = mid;
   c = cb ? lo : hi;
@@ -87,8 +93,8 @@ __device__ __forceinline__ void line_pt(double &a, double &b, double &c, const S
 // digit k), so axes 1..d-1 are local.  Every 1D operator is applied where
 // its axis is local; the values change layout through a per-leaf buffer in
 // shared memory.
-template <int DIM, int AX, typename Op>
-__device__ __forceinline__ void axis_a(double (&v)[SfDim<DIM>::NV], Op op)
+template <int DIM, int AX, typename V, typename Op>
+__device__ __forceinline__ void axis_a(V (&v)[SfDim<DIM>::NV], Op op)
 {
   static_assert(AX >= 0 && AX <= DIM - 2, "axis not local in layout A");
   constexpr int s = AX == 0 ? 1 : (AX == 1 ? 3 : 9);
@@ -96,8 +102,8 @@ __device__ __forceinline__ void axis_a(double (&v)[SfDim<DIM>::NV], Op op)
   for (int j = 0; j < SfDim<DIM>::NV; j++)
     if ((j / s) % 3 == 0) op(AX, v[j], v[j + s], v[j + 2 * s]);
 }
-template <int DIM, int AX, typename Op>
-__device__ __forceinline__ void axis_b(double (&v)[SfDim<DIM>::NV], Op op)
+template <int DIM, int AX, typename V, typename Op>
+__device__ __forceinline__ void axis_b(V (&v)[SfDim<DIM>::NV], Op op)
 {
   static_assert(AX >= 1 && AX <= DIM - 1, "axis not local in layout B");
   constexpr int s = AX == 1 ? 1 : (AX == 2 ? 3 : 9);
@@ -105,23 +111,23 @@ __device__ __forceinline__ void axis_b(double (&v)[SfDim<DIM>::NV], Op op)
   for (int j = 0; j < SfDim<DIM>::NV; j++)
     if ((j / s) % 3 == 0) op(AX, v[j], v[j + s], v[j + 2 * s]);
 }
-template <int DIM, typename Op>
-__device__ __forceinline__ void axes_a_all(double (&v)[SfDim<DIM>::NV], Op op)
+template <int DIM, typename V, typename Op>
+__device__ __forceinline__ void axes_a_all(V (&v)[SfDim<DIM>::NV], Op op)
 {
   axis_a<DIM, 0>(v, op);
   if constexpr (DIM >= 3) axis_a<DIM, 1>(v, op);
   if constexpr (DIM >= 4) axis_a<DIM, 2>(v, op);
 }
-template <int DIM, typename Op>
-__device__ __forceinline__ void axes_b_all(double (&v)[SfDim<DIM>::NV], Op op)
+template <int DIM, typename V, typename Op>
+__device__ __forceinline__ void axes_b_all(V (&v)[SfDim<DIM>::NV], Op op)
 {
   axis_b<DIM, 1>(v, op);
   if constexpr (DIM >= 3) axis_b<DIM, 2>(v, op);
   if constexpr (DIM >= 4) axis_b<DIM, 3>(v, op);
 }
 // A -> B and B -> A through the leaf's buffer; idle lanes only synchronise.
-template <int NV>
-__device__ __forceinline__ void to_b(double (&v)[NV], double *buf, int k, bool act)
+template <int NV, typename V>
+__device__ __forceinline__ void to_b(V (&v)[NV], V *buf, int k, bool act)
 {
   if (act) {
 #pragma unroll
@@ -134,8 +140,8 @@ __device__ __forceinline__ void to_b(double (&v)[NV], double *buf, int k, bool a
   }
   __syncwarp();
 }
-template <int NV>
-__device__ __forceinline__ void to_a(double (&v)[NV], double *buf, int k, bool act)
+template <int NV, typename V>
+__device__ __forceinline__ void to_a(V (&v)[NV], V *buf, int k, bool act)
 {
   if (act) {
 #pragma unroll
@@ -149,22 +155,24 @@ __device__ __forceinline__ void to_a(double (&v)[NV], double *buf, int k, bool a
   __syncwarp();
 }
 
-template <int DIM>
+// V = double: the FP64 product; V = float: the binary32 product (inner
+// operator of the mixed-precision solver; plans without stale reads).
+template <int DIM, typename V>
 __global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
     const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, const int32_t *__restrict__ order,
-    int64_t n_leaf, SfCoef cf, const double *__restrict__ Dtab, const double *__restrict__ x, double *__restrict__ y,
-    double scale, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
+    int64_t n_leaf, SfCoef<V> cf, const V *__restrict__ Dtab, const V *__restrict__ x, V *__restrict__ y,
+    V scale, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
     const double *__restrict__ stv, int conforming)
 {
   constexpr int NV = SfDim<DIM>::NV, NPE = SfDim<DIM>::NPE;
-  __shared__ double sbuf[4 * 10 * NPE];   // one buffer per leaf of the block (blockDim 128)
+  __shared__ V sbuf[4 * 10 * NPE];   // one buffer per leaf of the block (blockDim 128)
   const int lane = threadIdx.x & 31, slot = lane / 3, k = lane - 3 * slot;
   const int warp = threadIdx.x >> 5;
   const int64_t t = ((int64_t) blockIdx.x * 4 + warp) * 10 + slot;
   const bool act = slot < 10;                 // lanes 30, 31 are idle
   const bool valid = act && t < n_leaf;
-  double *buf = sbuf + (warp * 10 + (act ? slot : 0)) * NPE;
+  V *buf = sbuf + (warp * 10 + (act ? slot : 0)) * NPE;
   const int64_t i = valid ? (int64_t) order[t] : 0;
   const uint32_t inf = valid ? info[i] : 0u;
   const int L = inf & 0xFFu;
@@ -172,18 +180,18 @@ __global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
   const bool hang = valid && ((inf >> 16) & 1u);
 
   // own values in layout B
-  double u[NV];
+  V u[NV];
   const int32_t *er = e2n + i * NPE;
 #pragma unroll
   for (int j = 0; j < NV; j++) {
     const int32_t nd = valid ? er[k + 3 * j] : -1;
-    u[j] = nd >= 0 ? x[nd] : 0.0;
+    u[j] = nd >= 0 ? x[nd] : V(0);
   }
   const bool any_h = __any_sync(0xffffffffu, hang);
   uint32_t fA = 0, fB = 0;   // fill bits of the thread's ranks in layout A and in layout B
   int64_t h = 0;
   if (any_h) {
-    double v[NV];
+    V v[NV];
     if (hang) {
       h = hidx[i];
       const uint32_t w0 = fill[h * 3], w1 = fill[h * 3 + 1], w2 = fill[h * 3 + 2];
@@ -202,20 +210,20 @@ __global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
 #pragma unroll
       for (int j = 0; j < NV; j++) {
         const int32_t pn = pr[j];
-        double val = 0.0;
+        V val = V(0);
         if (pn >= 0) val = x[pn];
         else if (hz >= 0) {
           const int32_t id = hztab[(int64_t) hz * NPE + k * NV + j];
-          if (id >= 0) val = stv[id];
+          if (id >= 0) val = (V) stv[id];
         }
         v[j] = val;
       }
     } else {
 #pragma unroll
-      for (int j = 0; j < NV; j++) v[j] = 0.0;
+      for (int j = 0; j < NV; j++) v[j] = V(0);
     }
     // parent -> child: axes 0..d-2 in layout A, the last axis in layout B
-    auto ip = [&](int ax, double &a, double &b, double &c) { line_p(a, b, c, cf, (child >> ax) & 1u); };
+    auto ip = [&](int ax, V &a, V &b, V &c) { line_p(a, b, c, cf, (child >> ax) & 1u); };
     axes_a_all<DIM>(v, ip);
     to_b<NV>(v, buf, k, act);
     axis_b<DIM, DIM - 1>(v, ip);
@@ -226,13 +234,13 @@ __global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
     }
   }
   // forward transform: axes 1..d-1 in B, axis 0 in A
-  auto tf = [&](int, double &a, double &b, double &c) { line_t(a, b, c, cf); };
+  auto tf = [&](int, V &a, V &b, V &c) { line_t(a, b, c, cf); };
   axes_b_all<DIM>(u, tf);
   to_a<NV>(u, buf, k, act);
   axis_a<DIM, 0>(u, tf);
   // diagonal of level L (layout A: ranks k*NV + j)
-  const double *Dl = Dtab + (int64_t) L * NPE + k * NV;
-  if (scale == 1.0) {
+  const V *Dl = Dtab + (int64_t) L * NPE + k * NV;
+  if (scale == V(1)) {
 #pragma unroll
     for (int j = 0; j < NV; j++) u[j] *= __ldg(Dl + j);
   } else {
@@ -240,7 +248,7 @@ __global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
     for (int j = 0; j < NV; j++) u[j] *= scale * __ldg(Dl + j);
   }
   // transposed transform: axes 0..d-2 in A, the last axis in B
-  auto tt = [&](int, double &a, double &b, double &c) { line_tt(a, b, c, cf); };
+  auto tt = [&](int, V &a, V &b, V &c) { line_tt(a, b, c, cf); };
   axes_a_all<DIM>(u, tt);
   to_b<NV>(u, buf, k, act);
   axis_b<DIM, DIM - 1>(u, tt);
@@ -256,8 +264,8 @@ __global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
     // axes 1..d-1 in B, axis 0 in A
 #pragma unroll
     for (int j = 0; j < NV; j++)
-      if (!hang || ((fB >> j) & 1u)) u[j] = 0.0;
-    auto pt = [&](int ax, double &a, double &b, double &c) { line_pt(a, b, c, cf, (child >> ax) & 1u); };
+      if (!hang || ((fB >> j) & 1u)) u[j] = V(0);
+    auto pt = [&](int ax, V &a, V &b, V &c) { line_pt(a, b, c, cf, (child >> ax) & 1u); };
     axes_b_all<DIM>(u, pt);
     to_a<NV>(u, buf, k, act);
     axis_a<DIM, 0>(u, pt);
@@ -359,6 +367,10 @@ bool q2sf_setup(Plan &pl, cudaStream_t s)
     if (!(err <= 1e-13 * mx)) return false;
   }
   pl.sf_D.upload(D.data(), D.size(), s);
+  {
+    std::vector<float> D32(D.begin(), D.end());
+    pl.sf_D32.upload(D32.data(), D32.size(), s);
+  }
   std::copy(T, T + 9, pl.sf_T);
   std::copy(pint, pint + 3, pl.sf_pint);
   // With stale parent reads the chain runs on a side stream during the main
@@ -375,37 +387,52 @@ bool q2sf_setup(Plan &pl, cudaStream_t s)
   check_launch("q2sf_order");
   DKT_CUDA(cudaStreamSynchronize(s));
   pl.sf_ready = true;
+  // the binary32 product (inner operator of the mixed solver) needs no stale reads
+  pl.f32_ready = !pl.st_ready || pl.st_n_runs == 0;
   return true;
 }
 
-template <int DIM>
-static void launch_sf(Plan &pl, const int32_t *order, int64_t n, const double *x, double *y, double scale,
-                      cudaStream_t s)
+template <typename V> static const V *sf_table(const Plan &pl);
+template <> const double *sf_table<double>(const Plan &pl) { return pl.sf_D.p; }
+template <> const float *sf_table<float>(const Plan &pl) { return pl.sf_D32.p; }
+
+template <int DIM, typename V>
+static void launch_sf(Plan &pl, const int32_t *order, int64_t n, const V *x, V *y, double scale, cudaStream_t s)
 {
   if (n == 0) return;
-  SfCoef cf;
-  cf.u01 = pl.sf_T[1] / pl.sf_T[0];
-  cf.u10 = pl.sf_T[3] / pl.sf_T[4];
-  cf.pa = pl.sf_pint[0]; cf.pb = pl.sf_pint[1]; cf.pc = pl.sf_pint[2];
+  SfCoef<V> cf;
+  cf.u01 = (V) (pl.sf_T[1] / pl.sf_T[0]);
+  cf.u10 = (V) (pl.sf_T[3] / pl.sf_T[4]);
+  cf.pa = (V) pl.sf_pint[0]; cf.pb = (V) pl.sf_pint[1]; cf.pc = (V) pl.sf_pint[2];
+  const bool fp64 = std::is_same<V, double>::value;
   const int64_t per_block = 4 * 10;   // 4 warps of 10 leaves
   const unsigned blocks = (unsigned) ((n + per_block - 1) / per_block);
-  k_matvec_q2sf<DIM><<<blocks, 128, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, order,
-                                            n, cf, pl.sf_D.p, x, y, pl.op.uses_scale ? scale : 1.0,
-                                            pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_v.p,
-                                            pl.conforming ? 1 : 0);
+  k_matvec_q2sf<DIM, V><<<blocks, 128, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, order,
+                                               n, cf, sf_table<V>(pl), x, y, (V) (pl.op.uses_scale ? scale : 1.0),
+                                               (fp64 && pl.st_ready) ? pl.st_hzoff.p : nullptr, pl.st_hztab.p,
+                                               pl.st_v.p, pl.conforming ? 1 : 0);
   check_launch("matvec_q2sf");
 }
 
-static void launch_sf_dim(Plan &pl, const int32_t *order, int64_t n, const double *x, double *y, double scale,
-                          cudaStream_t s)
+template <typename V>
+static void launch_sf_dim(Plan &pl, const int32_t *order, int64_t n, const V *x, V *y, double scale, cudaStream_t s)
 {
   switch (pl.dim) {
-    case 2: launch_sf<2>(pl, order, n, x, y, scale, s); break;
-    case 3: launch_sf<3>(pl, order, n, x, y, scale, s); break;
-    case 4: launch_sf<4>(pl, order, n, x, y, scale, s); break;
+    case 2: launch_sf<2, V>(pl, order, n, x, y, scale, s); break;
+    case 3: launch_sf<3, V>(pl, order, n, x, y, scale, s); break;
+    case 4: launch_sf<4, V>(pl, order, n, x, y, scale, s); break;
     default: throw std::runtime_error("unsupported dim");
   }
   if (n > 0) pl.n_launch++;
+}
+
+// Binary32 product y = A x (y zeroed here), the order-2 counterpart of the
+// Q1 binary32 kernels: same leaf order, float values, float atomics.
+void q2sf_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
+{
+  if (!pl.sf_ready || !pl.f32_ready) throw std::runtime_error("binary32 Q2 product needs a plan without stale reads");
+  DKT_CUDA(cudaMemsetAsync(y, 0, pl.n_nodes * sizeof(float), s));
+  launch_sf_dim<float>(pl, pl.sf_order.p, pl.sf_n_main, x, y, 1.0, s);
 }
 
 void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s);
@@ -432,7 +459,7 @@ void q2sf_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_
     DKT_CUDA(cudaEventCreate(&e1));
     DKT_CUDA(cudaEventRecord(e0, s));
   }
-  launch_sf_dim(pl, pl.sf_order.p, pl.sf_n_main, x, y, scale, s);
+  launch_sf_dim<double>(pl, pl.sf_order.p, pl.sf_n_main, x, y, scale, s);
   if (pl.timing) {
     DKT_CUDA(cudaEventRecord(e1, s));
     pl.ev.push_back(e0);
@@ -441,7 +468,7 @@ void q2sf_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_
   }
   if (pl.sf_split) {
     DKT_CUDA(cudaStreamWaitEvent(s, pl.st_join, 0));
-    launch_sf_dim(pl, pl.st_hleaves.p, pl.st_n_hleaf, x, y, scale, s);
+    launch_sf_dim<double>(pl, pl.st_hleaves.p, pl.st_n_hleaf, x, y, scale, s);
   }
 }
 

@@ -417,7 +417,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
 {
   const int64_t n = pl.n_nodes;
   if (precision == 1 && !pl.f32_ready)
-    throw std::runtime_error("mixed precision needs a Q1 built-in operator without stale parent reads");
+    throw std::runtime_error("mixed precision needs a Q1 or Q2 built-in operator without stale parent reads");
   const bool saved_timing = pl.timing;
   pl.timing = false;
   cudaStream_t s = nullptr;

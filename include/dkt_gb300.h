@@ -180,11 +180,11 @@ int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter
  * mesh converges on its own (relative to its own ||b||); iters, refinements
  * and relres are then arrays with one entry per mesh.  DKT_PREC_FP64: Jacobi-PCG
  * in FP64.  DKT_PREC_MIXED: Jacobi-PCG on binary32 vectors with the binary32
- * Q1 product and reliable updates -- the correction is folded into x in FP64
- * and the residual recomputed exactly (b - A x, fixed-point product) each
+ * product and reliable updates -- the correction is folded into x in FP64
+ * and the residual recomputed with the FP64 product (b - A x) each
  * time the binary32 residual has fallen 1000x -- until ||b - A x||_2 <=
  * tol ||b||_2 (FP64 residual); refinements counts the updates.  Dot products
- * accumulate in FP64 in both.  Mixed needs a Q1 built-in operator without
+ * accumulate in FP64 in both.  Mixed needs a Q1 or Q2 built-in operator without
  * stale parent reads (a conforming plan, or a mesh without them); it is the
  * solver of HeatMat::cgSolve (FEM/examples/src/heatMat.cpp:164-325) with the
  * precision split that the reference does not have.  iters = CG iterations
@@ -211,17 +211,18 @@ int dkt_plan_mesh_offsets(dkt_plan plan, int64_t *offsets);
  * untiled kernel) on this plan and keeps the fastest. */
 int dkt_plan_autotune(dkt_plan plan, int *best_tile, double *best_ms);
 
-/* Binary32 feMatrix product y = A x with the Q1 built-in operator of the
- * plan (boundary entries zeroed in and out as feMatrix::matVec does for the
- * operators with Dirichlet steps).  No counterpart in the reference, which is
+/* Binary32 feMatrix product y = A x with the Q1 or Q2 built-in operator of
+ * the plan (boundary entries zeroed in and out as feMatrix::matVec does for
+ * the operators with Dirichlet steps).  No counterpart in the reference, which is
  * FP64 only; accuracy about 1e-6 relative. */
 int dkt_matvec_f32(dkt_plan plan, const float *x_dev, float *y_dev, void *stream);
 
 /* Arithmetic of the leaf kernel.  AUTO (default) uses FIXED where it applies:
  * the Q1 built-in operators are diagonal in the Hadamard basis and run in
  * exact int64 fixed point (deterministic, ~2^-50 relative to max|x|*|K|,
- * well inside the 1e-12 parity tolerance); FP64 forces the dense native-FP64
- * kernel (used for Q2 and custom operators). */
+ * well inside the 1e-12 parity tolerance), and the Q2 built-in operators run
+ * on the sum-factorised FP64 kernel; FP64 forces the dense native-FP64
+ * kernel (always used for custom operators). */
 #define DKT_ARITH_AUTO 0
 #define DKT_ARITH_FP64 1
 #define DKT_ARITH_FIXED 2

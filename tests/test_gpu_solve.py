@@ -37,17 +37,23 @@ def _poisson_rhs(dkt, da, seed):
 
 
 def _mesh(dkt, kind):
-    if kind == "gauss3d":
+    """gauss3d / ball4d at order 1; the _q2 kinds are the same meshes at
+    order 2 (the Gaussian tree one level finer in coordinates, so that Q2 node
+    spacing never collapses)."""
+    order = 2 if kind.endswith("_q2") else 1
+    if kind.startswith("gauss3d"):
         md = 9
         pts = dkt.gaussian_points(4000, 3, md, seed=1)
         tc, tl = dkt.tree_from_points(pts, 3, md)
-        return dkt.DA(tc, tl, 3, order=1, max_depth=md), 3, md
+        if order == 2:
+            tc, md = tc << np.uint32(1), md + 1
+        return dkt.DA(tc, tl, 3, order=order, max_depth=md), 3, md
     md, level = 8, 4
     tc, tl = dkt.moving_ball_tree(max_depth=md, level=level)
-    return dkt.DA(tc, tl, 4, order=1, max_depth=md), 4, md
+    return dkt.DA(tc, tl, 4, order=order, max_depth=md), 4, md
 
 
-@pytest.mark.parametrize("kind", ["gauss3d", "ball4d"])
+@pytest.mark.parametrize("kind", ["gauss3d", "ball4d", "gauss3d_q2", "ball4d_q2"])
 def test_f32_product_close_to_fp64(dkt, kind):
     import torch
     da, dim, md = _mesh(dkt, kind)
@@ -64,7 +70,7 @@ def test_f32_product_close_to_fp64(dkt, kind):
         assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 2e-6
 
 
-@pytest.mark.parametrize("kind", ["gauss3d", "ball4d"])
+@pytest.mark.parametrize("kind", ["gauss3d", "ball4d", "gauss3d_q2", "ball4d_q2"])
 def test_fp64_and_mixed_pcg_reach_1e10(dkt, kind):
     import torch
     da, dim, md = _mesh(dkt, kind)
@@ -87,12 +93,14 @@ def test_fp64_and_mixed_pcg_reach_1e10(dkt, kind):
     assert np.linalg.norm(x64 - xm) / np.linalg.norm(x64) <= 1e-6
 
 
-def test_mixed_solution_against_oracle(dkt):
-    """4D moving-ball Poisson: the mixed-precision solution satisfies the
-    oracle's own (conforming) operator to 1e-10 and matches the oracle's FP64
-    CG solution."""
+@pytest.mark.parametrize("kind", ["ball4d", "ball4d_q2"])
+def test_mixed_solution_against_oracle(dkt, kind):
+    """4D moving-ball Poisson (Q1 and Q2): the mixed-precision solution
+    satisfies the oracle's own (conforming) operator to 1e-10 and matches the
+    oracle's FP64 CG solution."""
     import torch
-    da, dim, md = _mesh(dkt, "ball4d")
+    da, dim, md = _mesh(dkt, kind)
+    order = 2 if kind.endswith("_q2") else 1
     A = dkt.Matrix(da, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
     b = _poisson_rhs(dkt, da, seed=3)
     bd = _t(b)
@@ -105,9 +113,11 @@ def test_mixed_solution_against_oracle(dkt):
     orc.set_stale_mode(1)
     try:
         sc, sl = da.tree()
-        ora = orc.DA(sc, sl, dim, 1, dkt.OP_LAPLACE)
+        ora = orc.DA(sc, sl, dim, order, dkt.OP_LAPLACE)
         r = b - ora.matvec(x)
         assert np.linalg.norm(r) / np.linalg.norm(b) <= 2e-10
+        if order == 2:
+            return   # the oracle's own CG at order 2 takes minutes; the residual above pins x
         xo, ito, rro = ora.cg(b, max_iter=20000, tol=1e-12)
         assert rro <= 1e-12
         assert np.linalg.norm(x - xo) / np.linalg.norm(xo) <= 1e-7
