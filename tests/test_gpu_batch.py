@@ -18,11 +18,15 @@ def dkt():
     return ge.load_package()
 
 
-def _meshes(dkt, sizes, dim=3, md=10):
+def _meshes(dkt, sizes, dim=3, md=10, order=1):
     out = []
     for k, n in enumerate(sizes):
-        tc, tl = dkt.tree_from_points(dkt.cluster_points(n, dim, md, seed=k), dim, md)
-        out.append(dkt.DA(tc, tl, dim, order=1, max_depth=md))
+        # order 2: the tree one level coarser in coordinates, so Q2 node spacing stays integral
+        gmd = md - 1 if order == 2 else md
+        tc, tl = dkt.tree_from_points(dkt.cluster_points(n, dim, gmd, seed=k), dim, gmd)
+        if order == 2:
+            tc = tc << np.uint32(1)
+        out.append(dkt.DA(tc, tl, dim, order=order, max_depth=md))
     return out
 
 
@@ -34,8 +38,9 @@ def _mv(A, x):
     return yd.cpu().numpy()
 
 
-def test_batched_product_equals_single_products(dkt):
-    das = _meshes(dkt, [300, 1200, 50, 2500])
+@pytest.mark.parametrize("order", [1, 2])
+def test_batched_product_equals_single_products(dkt, order):
+    das = _meshes(dkt, [300, 1200, 50, 2500], order=order)
     mats = [dkt.Matrix(d, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING) for d in das]
     B = dkt.Matrix.batch(mats)
     off = B.mesh_offsets()
@@ -48,10 +53,10 @@ def test_batched_product_equals_single_products(dkt):
         assert np.linalg.norm(seg - y) <= 1e-12 * np.linalg.norm(y), k
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_batched_pcg_per_mesh_convergence(dkt, precision):
+@pytest.mark.parametrize("precision,order", [(0, 1), (1, 1), (0, 2), (1, 2)])
+def test_batched_pcg_per_mesh_convergence(dkt, precision, order):
     import torch
-    das = _meshes(dkt, [400, 2000, 100, 3000, 800])
+    das = _meshes(dkt, [400, 2000, 100, 3000, 800], order=order)
     mats = [dkt.Matrix(d, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING) for d in das]
     B = dkt.Matrix.batch(mats)
     off = B.mesh_offsets()
@@ -76,7 +81,10 @@ def test_batched_pcg_per_mesh_convergence(dkt, precision):
         x1 = x1.cpu().numpy()
         assert np.linalg.norm(xk - x1) <= 1e-6 * np.linalg.norm(x1), k
         if precision == 0:
-            assert abs(int(it[k]) - it1) <= 2, (k, it[k], it1)
+            # Q1 products are exact integers; the Q2 product sums with FP64
+            # atomics, whose order varies, so its iteration counts may differ a little
+            slack = 2 if order == 1 else max(2, it1 // 100)
+            assert abs(int(it[k]) - it1) <= slack, (k, it[k], it1)
 
 
 def test_autotune_keeps_result(dkt):
