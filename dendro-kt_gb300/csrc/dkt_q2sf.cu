@@ -158,7 +158,7 @@ __device__ __forceinline__ void to_a(V (&v)[NV], V *buf, int k, bool act)
 // V = double: the FP64 product; V = float: the binary32 product (inner
 // operator of the mixed-precision solver; plans without stale reads).
 template <int DIM, typename V>
-__global__ void __launch_bounds__(128, 3) k_matvec_q2sf(
+__global__ void __launch_bounds__(128, std::is_same<V, float>::value ? 6 : 3) k_matvec_q2sf(
     const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, const int32_t *__restrict__ order,
     int64_t n_leaf, SfCoef<V> cf, const V *__restrict__ Dtab, const V *__restrict__ x, V *__restrict__ y,
