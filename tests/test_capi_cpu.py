@@ -71,13 +71,13 @@ def test_gaussian_points_deterministic(dkt):
     assert abs(x.mean() - 0.5) < 0.02 and abs(x.std() - 0.1) < 0.02
 
 
-def test_moving_ball_is_balanced(dkt):
+def test_moving_ball_is_complete(dkt):
     tc, tl = dkt.moving_ball_tree(max_depth=6, level=4)
     dim, md = 4, 6
     orc.set_curve(dim, md)
     sc, sl = orc.tree_sort(tc, tl, dim)
-    # The balancing is idempotent: rebuilding from the balanced tree's own cells
-    # through the oracle's propagate+reconstruct leaves it unchanged.
+    # complete: the cells' volumes sum to the domain's (2:1 balance is checked
+    # in test_tree_properties.py)
     vol = np.sum((2.0 ** -sl.astype(np.float64)) ** dim)
     assert abs(vol - 1.0) < 1e-12
     assert sl.max() == 4
