@@ -51,6 +51,29 @@ def test_error_codes_without_device(dkt):
     assert L.dkt_da_create(3, 1, 0, 10, dkt._p(c2), dkt._p(lv2), 1, 1, ctypes.byref(h)) == dkt.E_ARG
     assert b"aligned" in L.dkt_last_error()
     assert L.dkt_plan_create(None, 2, None, ctypes.byref(h)) == dkt.E_ARG
+    # entry points added for feVector, DA(func) and the device tree builder:
+    # argument errors come back before any device work
+    x = np.zeros(4)
+    assert L.dkt_fevector_compute_vec(None, dkt._p(x), dkt._p(x), ctypes.c_double(1.0), None) == dkt.E_ARG
+    n = ctypes.c_int64()
+    pc, pl = ctypes.c_void_p(), ctypes.c_void_p()
+    pts = np.zeros((2, 3), np.uint32)
+    assert L.dkt_mesh_tree_from_points_device(dkt._p(pts), 2, 5, 8, 1, ctypes.byref(n), ctypes.byref(pc),
+                                              ctypes.byref(pl)) == dkt.E_ARG          # dim 5
+    assert L.dkt_mesh_tree_from_points_device(dkt._p(pts), 2, 3, 8, 0, ctypes.byref(n), ctypes.byref(pc),
+                                              ctypes.byref(pl)) == dkt.E_ARG          # max_pts 0
+    far = np.full((1, 3), 1 << 9, np.uint32)
+    assert L.dkt_mesh_tree_from_points_device(dkt._p(far), 1, 3, 8, 1, ctypes.byref(n), ctypes.byref(pc),
+                                              ctypes.byref(pl)) == dkt.E_ARG          # outside 2^8
+    assert b"outside" in L.dkt_last_error()
+    assert L.dkt_mesh_function2octree(None, None, 1, 3, 8, 1, ctypes.c_double(1e-3), 1, ctypes.byref(n),
+                                      ctypes.byref(pc), ctypes.byref(pl)) == dkt.E_ARG   # no callback
+    cb = dkt._FIELD_FN(lambda *a: 0)
+    fp = ctypes.cast(cb, ctypes.c_void_p)
+    assert L.dkt_mesh_function2octree(fp, None, 1, 3, 8, 3, ctypes.c_double(1e-3), 1, ctypes.byref(n),
+                                      ctypes.byref(pc), ctypes.byref(pl)) == dkt.E_ARG   # order 3
+    assert L.dkt_mesh_function2octree(fp, None, 0, 3, 8, 1, ctypes.c_double(1e-3), 1, ctypes.byref(n),
+                                      ctypes.byref(pc), ctypes.byref(pl)) == dkt.E_ARG   # no fields
 
 
 @pytest.mark.parametrize("dim,n,md", [(2, 300, 8), (3, 500, 9), (4, 80, 6)])
