@@ -536,3 +536,20 @@ def uniform_pm1(seed, n):
     with np.errstate(over="ignore"):
         r = splitmix64(np.uint64(seed) * np.uint64(0xD1B54A32D192ED03) + np.arange(n, dtype=np.uint64))
     return 2.0 * ((r >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)) - 1.0
+
+
+def uniform_pm1_coords(seed, coords):
+    """Nodal vector keyed by node coordinates instead of DA position: the same
+    node gets the same value in any node order (Morton or Hilbert DA, any
+    partition).  x = 2u - 1, u from splitmix64 chained over the coordinates."""
+    def splitmix64(z):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+    c = np.asarray(coords, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        h = np.full(c.shape[0], np.uint64(seed) * np.uint64(0xD1B54A32D192ED03), np.uint64)
+        for d in range(c.shape[1]):
+            h = splitmix64(h ^ c[:, d])
+    return 2.0 * ((h >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)) - 1.0

@@ -485,3 +485,28 @@ def test_offset_views_as_vectors(dkt):
     A.matvec(xb[1:], yb[1:])
     torch.cuda.synchronize()
     assert torch.equal(yb[1:], y)
+
+
+@pytest.mark.parametrize("dim,order", [(3, 1), (4, 1), (3, 2)])
+def test_product_independent_of_curve(dkt, dim, order):
+    """With a coordinate-keyed input, the Morton-ordered and the
+    Hilbert-ordered plans of one tree give the same product node by node
+    (conforming traversal: the reference traversal's static-buffer reads
+    depend on the visiting order, so only its stale-free meshes qualify)."""
+    import torch
+    md = 9 if order == 1 else 10
+    gmd = md - 1 if order == 2 else md
+    pts = dkt.gaussian_points(3000, dim, gmd, seed=8)
+    tc, tl = dkt.tree_from_points(pts, dim, gmd)
+    if order == 2:
+        tc = tc << np.uint32(1)
+    ys = []
+    for curve in (dkt.CURVE_MORTON, dkt.CURVE_HILBERT):
+        da = dkt.DA(tc, tl, dim, order=order, max_depth=md, curve=curve)
+        A = dkt.Matrix(da, op=dkt.OP_LAPMASS, traversal=dkt.TRAVERSAL_CONFORMING)
+        nc, _ = da.nodes()
+        y = _gpu_mv(A, dkt.uniform_pm1_coords(5, nc))
+        order_idx = np.lexsort(nc.T[::-1])
+        ys.append((nc[order_idx], y[order_idx]))
+    assert np.array_equal(ys[0][0], ys[1][0])
+    assert _rel(ys[1][1], ys[0][1]) <= TOL
