@@ -68,6 +68,8 @@ def cases():
     # driver (1 / (eps + |x - c|^2)), then 2:1 balance
     for dim, md, order, tol in ((2, 8, 1, 0.2), (3, 7, 1, 1.0), (3, 7, 2, 1.0), (4, 6, 1, 4.0)):
         out.append((f"morton_d{dim}_p{order}_op2_f2o", "morton", dim, md, order, 2, ("f2o", tol)))
+    for dim, md, order, tol in ((3, 7, 1, 1.0), (4, 6, 1, 4.0)):
+        out.append((f"hilbert_d{dim}_p{order}_op2_f2o", "hilbert", dim, md, order, 2, ("f2o", tol)))
     return out
 
 
