@@ -5,8 +5,11 @@
 //
 // The vectors are cut into chunks that never straddle two meshes; one CTA
 // per chunk does the vector work and writes per-chunk partial sums, and a
-// one-thread-per-mesh kernel adds each mesh's partials in a fixed order, so
-// every dot product accumulates in FP64 and is bitwise reproducible.  All
+// one-warp-per-mesh kernel adds each mesh's partials in a fixed order (lane
+// sums over a fixed stride, then a fixed shuffle tree), so every dot product
+// accumulates in FP64 and is bitwise reproducible.  Chunks are small (2048
+// nodes, eight per thread) because FP64 additions are long-latency on this
+// part: a thread's chain of dependent FP64 accumulations must stay short.  All
 // scalars (alpha, beta, r.z, r.r, a converged flag) stay on the device, so a
 // block of iterations has no host synchronisation and is captured once into
 // a CUDA graph that is relaunched until every mesh has converged.  A
@@ -37,7 +40,7 @@ void diagonal(const Plan &pl, double *diag, cudaStream_t s);
 namespace {
 
 constexpr int ST = 256;                 // threads of the vector kernels
-constexpr int64_t CHK = 16384;          // nodes per chunk
+constexpr int64_t CHK = 2048;           // nodes per chunk
 constexpr int CHUNK_IT = 16;            // CG iterations per captured graph
 
 struct CgScal {
@@ -90,6 +93,23 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
   return v;
 }
 
+// Widening of a binary32 value to FP64 with integer operations: a hardware
+// conversion runs on the FP64 pipe, which on this part retires about one
+// warp instruction per 64 cycles per sub-partition and would bound the
+// binary32 vector kernels.  Exact for normal numbers, zeros, infinities and
+// NaNs; binary32 subnormals (below 1.2e-38) become signed zeros, which
+// changes a dot product by less than 1e-38 per term.
+__device__ __forceinline__ double widen(float f)
+{
+  const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  uint64_t r = e == 0u ? 0ull
+                       : (e == 0xFFu ? (0x7FF0000000000000ull | ((uint64_t) m << 29))
+                                     : (((uint64_t) (e + 896u) << 52) | ((uint64_t) m << 29)));
+  r |= (uint64_t) (u & 0x80000000u) << 32;
+  return __longlong_as_double((long long) r);
+}
+__device__ __forceinline__ double widen(double d) { return d; }
+
 // part[c] = sum over chunk c of a*b (FP64 accumulation)
 template <typename T>
 __global__ void __launch_bounds__(ST) k_dot(const T *__restrict__ a, const T *__restrict__ b,
@@ -104,26 +124,35 @@ __global__ void __launch_bounds__(ST) k_dot(const T *__restrict__ a, const T *__
     return;
   }
   double s = 0.0;
-  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) s += (double) a[i] * (double) b[i];
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) s = fma(widen(a[i]), widen(b[i]), s);
   s = block_sum(s, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// per mesh: sum of its chunks' partials, in chunk order
-__device__ __forceinline__ double mesh_sum(const double *part, int stride, int off, int c0, int c1)
+// Per mesh (one warp): sum of its chunks' partials in a fixed order -- lane l
+// adds chunks c0 + l, c0 + l + 32, ... in turn, then a fixed shuffle tree.
+// Every lane returns the total.
+__device__ __forceinline__ double mesh_sum(const double *part, int stride, int off, int c0, int c1, int lane)
 {
   double s = 0.0;
-  for (int c = c0; c < c1; c++) s += part[(int64_t) c * stride + off];
+#pragma unroll 8
+  for (int c = c0 + lane; c < c1; c += 32) s += part[(int64_t) c * stride + off];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
 }
+// one warp per mesh in the finalisers (the whole warp returns together)
+#define MESH_OF_WARP(P)                                                      \
+  const int lane = threadIdx.x & 31;                                         \
+  const int p = (int) ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);        \
+  if (p >= (P)) return;
 
 // alpha = r.z / p.q (0 once converged or on breakdown)
 __global__ void k_fin_alpha(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
                             CgScal *__restrict__ sc)
 {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  const double pq = mesh_sum(part, 1, 0, first[p], first[p + 1]);
+  MESH_OF_WARP(P)
+  const double pq = mesh_sum(part, 1, 0, first[p], first[p + 1], lane);
+  if (lane != 0) return;
   CgScal &q = sc[p];
   q.pq = pq;
   q.alpha = (q.done || !(pq != 0.0)) ? 0.0 : q.rz / pq;
@@ -154,8 +183,9 @@ __global__ void __launch_bounds__(ST) k_update(T *__restrict__ x, T *__restrict_
     }
     const T zi = dinv ? ri * dinv[i] : ri;
     z[i] = zi;
-    srz += (double) ri * (double) zi;
-    srr += (double) ri * (double) ri;
+    const double rd = widen(ri);
+    srz = fma(rd, widen(zi), srz);
+    srr = fma(rd, rd, srr);
   }
   srz = block_sum(srz, sh);
   srr = block_sum(srr, sh);
@@ -166,10 +196,10 @@ __global__ void __launch_bounds__(ST) k_update(T *__restrict__ x, T *__restrict_
 __global__ void k_fin_beta(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
                            CgScal *__restrict__ sc, int count, int *__restrict__ n_done)
 {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  const double a = mesh_sum(part, 2, 0, first[p], first[p + 1]);
-  const double b = mesh_sum(part, 2, 1, first[p], first[p + 1]);
+  MESH_OF_WARP(P)
+  const double a = mesh_sum(part, 2, 0, first[p], first[p + 1], lane);
+  const double b = mesh_sum(part, 2, 1, first[p], first[p + 1], lane);
+  if (lane != 0) return;
   CgScal &q = sc[p];
   if (!q.done) {
     if (count) q.it++;
@@ -207,9 +237,9 @@ __global__ void k_residual(const double *__restrict__ b, const double *__restric
 __global__ void k_norms(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
                         double *__restrict__ nrm)
 {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  nrm[p] = sqrt(mesh_sum(part, 1, 0, first[p], first[p + 1]));
+  MESH_OF_WARP(P)
+  const double v = sqrt(mesh_sum(part, 1, 0, first[p], first[p + 1], lane));
+  if (lane == 0) nrm[p] = v;
 }
 
 // r32 = r / |r| on meshes still above tolerance, 0 elsewhere
@@ -263,6 +293,7 @@ template <> struct CgOp<float> {
 };
 
 inline unsigned pgrid(int P) { return (unsigned) ((P + 127) / 128); }
+inline unsigned wgrid(int P) { return (unsigned) ((P + 3) / 4); }   // blocks of 128 threads, a warp per mesh
 
 // Jacobi-PCG on all meshes of the plan, in type T (FP64 dots).  r must hold
 // b - A x on entry.
@@ -299,9 +330,9 @@ struct Cg {
     CgOp<T>::apply(pl, p.p, q.p, s);
     k_dot<T><<<nb, ST, 0, s>>>(p.p, q.p, ch.lo.p, ch.hi.p, part.p, &sc.p[0].done, ch.prob.p,
                                (int) (sizeof(CgScal) / sizeof(int)));
-    k_fin_alpha<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p);
+    k_fin_alpha<<<wgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p);
     k_update<T><<<nb, ST, 0, s>>>(x, r, z.p, p.p, q.p, dinv, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, part.p);
-    k_fin_beta<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 1, n_done.p);
+    k_fin_beta<<<wgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 1, n_done.p);
     k_pupd<T><<<nb, ST, 0, s>>>(p.p, z.p, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, 0);
     check_launch("cg_iteration");
     pl.n_launch += 5;
@@ -316,7 +347,7 @@ struct Cg {
     k_init_scal<<<pgrid(ch.P), 128, 0, s>>>(sc.p, ch.P, rr_stop_dev, rr_stop, n_done.p);
     // z = dinv r, r.z, r.r (alpha = 0 leaves x and r unchanged), p = z
     k_update<T><<<nb, ST, 0, s>>>(x, r, z.p, p.p, q.p, dinv, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, part.p);
-    k_fin_beta<<<pgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 0, n_done.p);
+    k_fin_beta<<<wgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 0, n_done.p);
     k_pupd<T><<<nb, ST, 0, s>>>(p.p, z.p, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, 1);
     check_launch("cg_start");
     pl.n_launch += 4;
@@ -444,7 +475,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
     }
     // per-mesh ||b||
     k_dot<double><<<nb, ST, 0, s>>>(b, b, ch.lo.p, ch.hi.p, part.p);
-    k_norms<<<pgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, bnrm.p);
+    k_norms<<<wgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, bnrm.p);
     pl.n_launch += 2;
     DKT_CUDA(cudaMemcpyAsync(hb.data(), bnrm.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
     DKT_CUDA(cudaStreamSynchronize(s));
@@ -491,7 +522,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
         fematrix_matvec(pl, x, ax.p, 1.0, s);
         k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
         k_dot<double><<<nb, ST, 0, s>>>(r.p, r.p, ch.lo.p, ch.hi.p, part.p);
-        k_norms<<<pgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, signew.p);
+        k_norms<<<wgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, signew.p);
         pl.n_launch += 3;
         DKT_CUDA(cudaMemcpyAsync(hr.data(), signew.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
         DKT_CUDA(cudaStreamSynchronize(s));
@@ -514,7 +545,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
         k_mark<<<pgrid(P), 128, 0, s>>>(cg.sc.p, act.p, P);
         k_update<float><<<nb, ST, 0, s>>>(xc.p, r32.p, cg.z.p, cg.p.p, cg.q.p, dinv32.p ? dinv32.p : nullptr,
                                           ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, cg.part.p);
-        k_fin_beta<<<pgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
+        k_fin_beta<<<wgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
         k_pupd<float><<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, 1);
         pl.n_launch += 6;
         hsig = hr;
@@ -556,7 +587,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           k_mark<<<pgrid(P), 128, 0, s>>>(cg.sc.p, act.p, P);
           k_update<float><<<nb, ST, 0, s>>>(xc.p, r32.p, cg.z.p, cg.p.p, cg.q.p, jacobi ? dinv32.p : nullptr,
                                             ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, cg.part.p);
-          k_fin_beta<<<pgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
+          k_fin_beta<<<wgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
           pl.n_launch += 4;
           // the kept direction only fits a residual that the recursion still
           // tracks; where the true residual is far above the recursive one
