@@ -242,24 +242,6 @@ __global__ void k_norms(const double *__restrict__ part, const int32_t *__restri
   if (lane == 0) nrm[p] = v;
 }
 
-// r32 = r / |r| on meshes still above tolerance, 0 elsewhere
-__global__ void k_scale_down(const double *__restrict__ r, float *__restrict__ r32, const int64_t *__restrict__ lo,
-                             const int64_t *__restrict__ hi, const int32_t *__restrict__ prob,
-                             const double *__restrict__ nrm, const int *__restrict__ active)
-{
-  const int p = prob[blockIdx.x];
-  const double s = (active[p] && nrm[p] > 0.0) ? 1.0 / nrm[p] : 0.0;
-  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) r32[i] = (float) (r[i] * s);
-}
-__global__ void k_add_scaled(double *__restrict__ x, const float *__restrict__ d, const int64_t *__restrict__ lo,
-                             const int64_t *__restrict__ hi, const int32_t *__restrict__ prob,
-                             const double *__restrict__ nrm, const int *__restrict__ active)
-{
-  const int p = prob[blockIdx.x];
-  if (!active[p]) return;
-  const double s = nrm[p];
-  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) x[i] += s * (double) d[i];
-}
 __global__ void k_invert(const double *__restrict__ d, double *__restrict__ o64, float *__restrict__ o32, int64_t n)
 {
   for (int64_t i = (int64_t) blockIdx.x * ST + threadIdx.x; i < n; i += (int64_t) gridDim.x * ST) {
