@@ -87,6 +87,7 @@ def load(build_if_missing=True):
         "dkt_mesh_tree_from_points": ([P, I64, I, I, I64, P, P, P], I),
         "dkt_mesh_tree_from_points_device": ([P, I64, I, I, I64, P, P, P], I),
         "dkt_mesh_function2octree": ([P, P, I, I, I, I, ctypes.c_double, I, P, P, P], I),
+        "dkt_da_set_vector_by_function": ([P, P, P, I, P], I),
         "dkt_write_vtu": ([ctypes.c_char_p, I, I, P, P, I64, P, ctypes.c_char_p], I),
         "dkt_mesh_moving_ball": ([I, I, ctypes.c_double, ctypes.c_double, P, P, P, P, P], I),
         "dkt_free": ([P], None),
@@ -168,6 +169,29 @@ class DA:
         lv = np.empty(ne, np.uint8)
         _check(load().dkt_da_get_tree(self._h, _p(c), _p(lv)))
         return c, lv
+
+    def set_vector_by_function(self, func, dof=1):
+        """DA::setVectorByFunction: func(x) with x [n, min(dim, 3)] node
+        coordinates in [0, 1] returns [n, dof]; the nodal vector [n, dof]."""
+        out = np.empty((self.n, dof), np.float64)
+        err = []
+
+        def cb(xp, n, d, outp, nv, _user):
+            try:
+                x = np.ctypeslib.as_array(xp, shape=(n, d))
+                o = np.ctypeslib.as_array(outp, shape=(n, nv))
+                o[...] = np.asarray(func(x), dtype=np.float64).reshape(n, nv)
+                return 0
+            except Exception as e:   # reported after the call
+                err.append(e)
+                return 1
+
+        fn = _FIELD_FN(cb)
+        rc = load().dkt_da_set_vector_by_function(self._h, ctypes.cast(fn, ctypes.c_void_p), None, int(dof), _p(out))
+        if err:
+            raise err[0]
+        _check(rc)
+        return out if dof > 1 else out[:, 0]
 
     def __del__(self):
         try:

@@ -201,6 +201,30 @@ int dkt_da_get_tree(dkt_da da, uint32_t *coords, uint8_t *levels)
   });
 }
 
+int dkt_da_set_vector_by_function(dkt_da da, dkt_field_fn fn, void *user, int dof, double *out)
+{
+  if (!da || !fn || !out || dof < 1) return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    const dkt::DA &d = da->da;
+    const int64_t n = d.n_nodes;
+    const int edim = d.dim < 3 ? d.dim : 3;
+    std::vector<uint32_t> nx((size_t) n * d.dim);
+    if (n) DKT_CUDA(cudaMemcpy(nx.data(), d.node_x.p, (size_t) n * d.dim * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    const double scale = 1.0 / (double) (1u << d.md);
+    const int64_t batch = int64_t(1) << 20;
+    std::vector<double> pts;
+    for (int64_t b0 = 0; b0 < n; b0 += batch) {
+      const int64_t nb = std::min(batch, n - b0);
+      pts.resize((size_t) nb * edim);
+      for (int64_t k = 0; k < nb; k++)
+        for (int a = 0; a < edim; a++) pts[k * edim + a] = scale * (double) nx[(b0 + k) * d.dim + a];
+      if (fn(pts.data(), nb, edim, out + b0 * dof, dof, user) != 0)
+        throw std::runtime_error("setVectorByFunction: the field callback reported an error");
+    }
+    return DKT_OK;
+  });
+}
+
 void dkt_da_destroy(dkt_da da) { delete da; }
 
 static int plan_common(int dim, int order, int curve, int md, const uint32_t *node_x_dev, const uint8_t *node_lev_dev,

@@ -82,6 +82,17 @@ int dkt_da_get_nodes(dkt_da da, uint32_t *coords, uint8_t *levels);
 int dkt_da_get_boundary_ids(dkt_da da, uint32_t *ids);
 /* Host copy of the SFC-ordered tree the DA was built on. */
 int dkt_da_get_tree(dkt_da da, uint32_t *coords, uint8_t *levels);
+
+/* Fields evaluated by the caller on batches of points: x [n][dim] with
+ * coordinates in [0, 1], out [n][n_vars]; a nonzero return is a failure. */
+typedef int (*dkt_field_fn)(const double *x, int64_t n, int dim, double *out, int n_vars, void *user);
+
+/* DA<dim>::setVectorByFunction (include/oda.tcc:437-470) on a host nodal
+ * vector: out [n][dof] (interleaved, [abc][abc]) gets fn at every DA node.
+ * As in the reference, the function sees the first min(dim, 3) coordinates
+ * of the node, scaled by 1/2^max_depth (dim passed to fn accordingly).  fn is
+ * called on batches of about 1 M nodes. */
+int dkt_da_set_vector_by_function(dkt_da da, dkt_field_fn fn, void *user, int dof, double *out);
 void dkt_da_destroy(dkt_da da);
 
 /* ---- fem::matvec -----------------------------------------------------------

@@ -10,6 +10,7 @@
 #define DKT_GB300_MESH_H
 
 #include <stdint.h>
+#include "dkt_gb300.h"   /* dkt_field_fn */
 
 #ifdef __cplusplus
 extern "C" {
@@ -53,7 +54,6 @@ int dkt_mesh_moving_ball_device(int max_depth, int level, double radius, double 
  * coordinates in [0, 1], out [n][n_vars]; a nonzero return aborts with
  * DKT_E_INTERNAL.  With balance = 1 the tree is then 2:1 balanced.  Arrays
  * are freed with dkt_free. */
-typedef int (*dkt_field_fn)(const double *x, int64_t n, int dim, double *out, int n_vars, void *user);
 int dkt_mesh_function2octree(dkt_field_fn fn, void *user, int n_vars, int dim, int max_depth, int order,
                              double interp_tol, int balance, int64_t *n_out, uint32_t **coords, uint8_t **levels);
 

@@ -510,3 +510,23 @@ def test_product_independent_of_curve(dkt, dim, order):
         ys.append((nc[order_idx], y[order_idx]))
     assert np.array_equal(ys[0][0], ys[1][0])
     assert _rel(ys[1][1], ys[0][1]) <= TOL
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_set_vector_by_function(dkt, dim):
+    """DA::setVectorByFunction: every node gets f at its coordinates scaled to
+    [0, 1], interleaved by dof; in 4D the function sees x, y, z only, as the
+    reference's (include/oda.tcc:441-444)."""
+    md = {2: 10, 3: 8, 4: 6}[dim]
+    c, l = dkt.tree_from_points(dkt.gaussian_points(500, dim, md, seed=1), dim, md)
+    da = dkt.DA(c, l, dim, order=1, max_depth=md)
+    seen = []
+
+    def f(x):
+        seen.append(x.shape[1])
+        return np.stack([np.sin(3.0 * x[:, 0]) + x[:, -1], x.sum(axis=1)], axis=1)
+    v = da.set_vector_by_function(f, dof=2)
+    nc, _ = da.nodes()
+    xs = nc[:, :min(dim, 3)].astype(np.float64) / (1 << md)
+    assert set(seen) == {min(dim, 3)}
+    assert np.array_equal(v, f(xs))
