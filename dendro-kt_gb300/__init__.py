@@ -67,6 +67,7 @@ def load(build_if_missing=True):
         "dkt_matvec": ([P, P, P, ctypes.c_double, P], I),
         "dkt_fematrix_matvec": ([P, P, P, ctypes.c_double, P], I),
         "dkt_fematrix_matvec_host": ([P, P, P, ctypes.c_double], I),
+        "dkt_fematrix_matvec_host_many": ([P, P, P, I, ctypes.c_double], I),
         "dkt_fematrix_matvec_noalloc": ([P, P, P, ctypes.c_double, P], I),
         "dkt_fevector_compute_vec": ([P, P, P, ctypes.c_double, P], I),
         "dkt_diagonal": ([P, P, P], I),
@@ -282,6 +283,20 @@ class Matrix:
             raise ValueError("out must be a contiguous float64 array of the plan's size")
         _check(load().dkt_fematrix_matvec_host(self._h, _p(x), _p(y), scale))
         return y
+
+    def matvec_host_many(self, xs, ys, scale=1.0):
+        """feMatrix::matVec of several host vectors, pipelined: copies of the
+        neighbouring products overlap each product (pass pinned arrays)."""
+        if len(xs) != len(ys):
+            raise ValueError("one output per input")
+        for a in list(xs) + list(ys):
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size != self.n:
+                raise ValueError("vectors must be contiguous float64 arrays of the plan's size")
+        k = len(xs)
+        xp = (ctypes.c_void_p * max(k, 1))(*[a.ctypes.data for a in xs])
+        yp = (ctypes.c_void_p * max(k, 1))(*[a.ctypes.data for a in ys])
+        _check(load().dkt_fematrix_matvec_host_many(self._h, xp, yp, k, scale))
+        return ys
 
     def set_arithmetic(self, mode):
         """ARITH_AUTO (fixed point where it applies), ARITH_FP64 or ARITH_FIXED."""

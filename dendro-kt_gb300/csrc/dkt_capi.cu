@@ -399,6 +399,66 @@ int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host
   });
 }
 
+int dkt_fematrix_matvec_host_many(dkt_plan plan, const double *const *x_host, double *const *y_host, int count,
+                                  double scale)
+{
+  if (!plan || count < 0 || (count > 0 && (!x_host || !y_host))) return fail(DKT_E_ARG, "bad argument");
+  for (int k = 0; k < count; k++)
+    if (!x_host[k] || !y_host[k]) return fail(DKT_E_ARG, "null vector");
+  return guarded([&]() {
+    dkt::Plan &pl = plan->pl;
+    const int64_t n = pl.n_nodes;
+    const size_t bytes = (size_t) n * sizeof(double);
+    dkt::DBuf<double> din[2], dout[2];
+    for (int b = 0; b < 2; b++) { din[b].alloc(n); dout[b].alloc(n); }
+    cudaStream_t sc = 0, si = nullptr, so = nullptr;   // compute: the caller thread's default stream
+    cudaEvent_t in_ready[2], in_free[2], out_ready[2], out_free[2];
+    DKT_CUDA(cudaStreamCreateWithFlags(&si, cudaStreamNonBlocking));
+    DKT_CUDA(cudaStreamCreateWithFlags(&so, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; b++) {
+      DKT_CUDA(cudaEventCreateWithFlags(&in_ready[b], cudaEventDisableTiming));
+      DKT_CUDA(cudaEventCreateWithFlags(&in_free[b], cudaEventDisableTiming));
+      DKT_CUDA(cudaEventCreateWithFlags(&out_ready[b], cudaEventDisableTiming));
+      DKT_CUDA(cudaEventCreateWithFlags(&out_free[b], cudaEventDisableTiming));
+    }
+    auto cleanup = [&]() {
+      cudaStreamSynchronize(si);
+      cudaStreamSynchronize(so);
+      cudaStreamSynchronize(sc);
+      for (int b = 0; b < 2; b++) {
+        cudaEventDestroy(in_ready[b]); cudaEventDestroy(in_free[b]);
+        cudaEventDestroy(out_ready[b]); cudaEventDestroy(out_free[b]);
+      }
+      cudaStreamDestroy(si);
+      cudaStreamDestroy(so);
+    };
+    try {
+      // buffer b serves products b, b + 2, ...: its copy-in waits until the
+      // product two steps back has read it, its copy-out until the product wrote it
+      for (int k = 0; k < count; k++) {
+        const int b = k & 1;
+        if (k >= 2) DKT_CUDA(cudaStreamWaitEvent(si, in_free[b], 0));
+        DKT_CUDA(cudaMemcpyAsync(din[b].p, x_host[k], bytes, cudaMemcpyHostToDevice, si));
+        DKT_CUDA(cudaEventRecord(in_ready[b], si));
+        DKT_CUDA(cudaStreamWaitEvent(sc, in_ready[b], 0));
+        if (k >= 2) DKT_CUDA(cudaStreamWaitEvent(sc, out_free[b], 0));
+        dkt::fematrix_matvec(pl, din[b].p, dout[b].p, scale, sc);
+        DKT_CUDA(cudaEventRecord(in_free[b], sc));
+        DKT_CUDA(cudaEventRecord(out_ready[b], sc));
+        DKT_CUDA(cudaStreamWaitEvent(so, out_ready[b], 0));
+        DKT_CUDA(cudaMemcpyAsync(y_host[k], dout[b].p, bytes, cudaMemcpyDeviceToHost, so));
+        DKT_CUDA(cudaEventRecord(out_free[b], so));
+      }
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+    DKT_CUDA(cudaGetLastError());
+    return DKT_OK;
+  });
+}
+
 int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream)
 {
   if (!plan || !diag_dev) return fail(DKT_E_ARG, "null argument");

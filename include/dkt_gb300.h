@@ -165,6 +165,14 @@ int dkt_fematrix_matvec_noalloc(dkt_plan plan, const double *x_dev, double *y_de
 /* Same with host arrays: copies in, computes, copies out, synchronises. */
 int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host, double scale);
 
+/* count products y_k = A x_k with host arrays (no counterpart in the
+ * reference), pipelined: while product k runs, x_{k+1} is copied in and
+ * y_{k-1} copied out, on separate streams with two device buffers each way.
+ * With pinned host arrays the copies overlap the compute.  Returns when every
+ * y_k is on the host; each is what dkt_fematrix_matvec_host would give. */
+int dkt_fematrix_matvec_host_many(dkt_plan plan, const double *const *x_host, double *const *y_host, int count,
+                                  double scale);
+
 /* feVector<T,dim>::computeVec(in, out, scale) (FEM/include/feVector.h:122-168):
  * preComputeVec on the input copy, fem::matvec with elementalComputeVec,
  * postComputeVec on the output.  The plan's operator is the vector's

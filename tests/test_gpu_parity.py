@@ -530,3 +530,19 @@ def test_set_vector_by_function(dkt, dim):
     xs = nc[:, :min(dim, 3)].astype(np.float64) / (1 << md)
     assert set(seen) == {min(dim, 3)}
     assert np.array_equal(v, f(xs))
+
+
+def test_pipelined_host_products_equal_single(dkt):
+    """dkt_fematrix_matvec_host_many: every result equals the one-product host
+    call (bitwise: the Q1 product is exact integer arithmetic), for an odd
+    number of vectors so both buffers and the tail are used."""
+    import torch
+    md, level = 10, 4
+    tc, tl = dkt.moving_ball_tree(max_depth=md, level=level, device=True)
+    da = dkt.DA(tc, tl, 4, order=1, max_depth=md)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    xs = [torch.from_numpy(dkt.uniform_pm1(20 + k, da.n)).pin_memory().numpy() for k in range(5)]
+    ys = [torch.empty(da.n, dtype=torch.float64).pin_memory().numpy() for _ in range(5)]
+    A.matvec_host_many(xs, ys)
+    for x, y in zip(xs, ys):
+        assert np.array_equal(y, A.matvec_host(x))
