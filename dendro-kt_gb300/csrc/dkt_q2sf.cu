@@ -396,8 +396,10 @@ template <typename V> static const V *sf_table(const Plan &pl);
 template <> const double *sf_table<double>(const Plan &pl) { return pl.sf_D.p; }
 template <> const float *sf_table<float>(const Plan &pl) { return pl.sf_D32.p; }
 
+// stale: the launch covers leaves that may read stale slots
 template <int DIM, typename V>
-static void launch_sf(Plan &pl, const int32_t *order, int64_t n, const V *x, V *y, double scale, cudaStream_t s)
+static void launch_sf(Plan &pl, const int32_t *order, int64_t n, const V *x, V *y, double scale, bool stale,
+                      cudaStream_t s)
 {
   if (n == 0) return;
   SfCoef<V> cf;
@@ -409,18 +411,19 @@ static void launch_sf(Plan &pl, const int32_t *order, int64_t n, const V *x, V *
   const unsigned blocks = (unsigned) ((n + per_block - 1) / per_block);
   k_matvec_q2sf<DIM, V><<<blocks, 128, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, order,
                                                n, cf, sf_table<V>(pl), x, y, (V) (pl.op.uses_scale ? scale : 1.0),
-                                               (fp64 && pl.st_ready) ? pl.st_hzoff.p : nullptr, pl.st_hztab.p,
+                                               (fp64 && stale && pl.st_ready) ? pl.st_hzoff.p : nullptr, pl.st_hztab.p,
                                                pl.st_v.p, pl.conforming ? 1 : 0);
   check_launch("matvec_q2sf");
 }
 
 template <typename V>
-static void launch_sf_dim(Plan &pl, const int32_t *order, int64_t n, const V *x, V *y, double scale, cudaStream_t s)
+static void launch_sf_dim(Plan &pl, const int32_t *order, int64_t n, const V *x, V *y, double scale, bool stale,
+                          cudaStream_t s)
 {
   switch (pl.dim) {
-    case 2: launch_sf<2, V>(pl, order, n, x, y, scale, s); break;
-    case 3: launch_sf<3, V>(pl, order, n, x, y, scale, s); break;
-    case 4: launch_sf<4, V>(pl, order, n, x, y, scale, s); break;
+    case 2: launch_sf<2, V>(pl, order, n, x, y, scale, stale, s); break;
+    case 3: launch_sf<3, V>(pl, order, n, x, y, scale, stale, s); break;
+    case 4: launch_sf<4, V>(pl, order, n, x, y, scale, stale, s); break;
     default: throw std::runtime_error("unsupported dim");
   }
   if (n > 0) pl.n_launch++;
@@ -432,7 +435,7 @@ void q2sf_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
 {
   if (!pl.sf_ready || !pl.f32_ready) throw std::runtime_error("binary32 Q2 product needs a plan without stale reads");
   DKT_CUDA(cudaMemsetAsync(y, 0, pl.n_nodes * sizeof(float), s));
-  launch_sf_dim<float>(pl, pl.sf_order.p, pl.sf_n_main, x, y, 1.0, s);
+  launch_sf_dim<float>(pl, pl.sf_order.p, pl.sf_n_main, x, y, 1.0, false, s);
 }
 
 void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s);
@@ -459,7 +462,8 @@ void q2sf_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_
     DKT_CUDA(cudaEventCreate(&e1));
     DKT_CUDA(cudaEventRecord(e0, s));
   }
-  launch_sf_dim<double>(pl, pl.sf_order.p, pl.sf_n_main, x, y, scale, s);
+  // split: the main launch leaves out every leaf that reads stale slots
+  launch_sf_dim<double>(pl, pl.sf_order.p, pl.sf_n_main, x, y, scale, !pl.sf_split, s);
   if (pl.timing) {
     DKT_CUDA(cudaEventRecord(e1, s));
     pl.ev.push_back(e0);
@@ -468,7 +472,7 @@ void q2sf_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_
   }
   if (pl.sf_split) {
     DKT_CUDA(cudaStreamWaitEvent(s, pl.st_join, 0));
-    launch_sf_dim<double>(pl, pl.st_hleaves.p, pl.st_n_hleaf, x, y, scale, s);
+    launch_sf_dim<double>(pl, pl.st_hleaves.p, pl.st_n_hleaf, x, y, scale, true, s);
   }
 }
 

@@ -604,11 +604,13 @@ static void launch_tiled_dim(Plan &pl, const void *fm, const int *fe, const type
   pl.n_launch++;
 }
 
-// skip_stale: leave the leaves that read stale slots to a later launch
+// skip_stale: leave the leaves that read stale slots to a later launch.  The
+// leaves that remain read no stale slot, so they need no look-up of one.
 void tiled_fixed(Plan &pl, bool skip_stale, cudaStream_t s)
 {
-  launch_tiled_dim<FixedArith>(pl, pl.fx_fm.p, pl.fx_fe.p, pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr,
-                               pl.st_hztab.p, pl.st_vq.p, skip_stale, s);
+  launch_tiled_dim<FixedArith>(pl, pl.fx_fm.p, pl.fx_fe.p, pl.xq.p, pl.yq.p,
+                               (pl.st_ready && !skip_stale) ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p,
+                               skip_stale, s);
 }
 
 void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
