@@ -6,6 +6,7 @@ host C++ unit into one shared library that exports the C ABI declared in
 include/dkt_gb300.h and include/dkt_gb300_mesh.h.
 """
 import concurrent.futures as cf
+import fcntl
 import os
 import shutil
 import subprocess
@@ -66,13 +67,23 @@ def build(force=False, verbose_ptxas=False):
     if not force and up_to_date():
         return LIB
     os.makedirs(OUT, exist_ok=True)
+    # one build at a time across processes (pool workers that all find the
+    # library out of date): the others wait, then see it up to date
+    with open(os.path.join(OUT, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and up_to_date():
+            return LIB
+        return _build_locked(verbose_ptxas)
+
+
+def _build_locked(verbose_ptxas):
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         res = list(ex.map(lambda s: _compile(s, verbose_ptxas), _sources()))
     objs = [o for o, _ in res]
     if verbose_ptxas:
         for _, err in res:
             print(err)
-    tmp = LIB + ".tmp"
+    tmp = "%s.%d.tmp" % (LIB, os.getpid())
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
