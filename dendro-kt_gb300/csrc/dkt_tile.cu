@@ -322,11 +322,30 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // The tiled leaf kernel.  One thread per leaf; blockDim.x == T.
 // ---------------------------------------------------------------------------
+// Walsh-Hadamard transform over the DIM axes.  Integers: two axes per pass,
+// each output a sum of four inputs, which integer hardware adds three at a
+// time (fewer instructions than two passes of pairwise butterflies; integer
+// sums are exact, so the result is the same as axis by axis).  Binary32: axis
+// by axis.
 template <int DIM, typename T>
 __device__ __forceinline__ void wht(T (&v)[1 << DIM])
 {
+  constexpr int D4 = std::is_integral<T>::value ? DIM / 2 * 2 : 0;   // axes done two at a time
 #pragma unroll
-  for (int d = 0; d < DIM; d++)
+  for (int d = 0; d < D4; d += 2)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (3 << d))) {
+        const int i1 = 1 << d, i2 = 2 << d;
+        const T a = v[k], b = v[k | i1], c = v[k | i2], e = v[k | i1 | i2];
+        const T s = a + b, t = a - b;
+        v[k] = s + c + e;
+        v[k | i1] = t + c - e;
+        v[k | i2] = s - c - e;
+        v[k | i1 | i2] = t - c + e;
+      }
+#pragma unroll
+  for (int d = D4; d < DIM; d++)
 #pragma unroll
     for (int k = 0; k < (1 << DIM); k++)
       if (!(k & (1 << d))) {
@@ -405,6 +424,54 @@ __device__ __forceinline__ void transpose_child0(V *v)
       }
 }
 
+// A thread's node slots of the tile are visited in groups of four, the four
+// id loads issued before anything that depends on them: one global round trip
+// per group for the ids and one for the values, instead of two per slot.
+constexpr int TILE_G = 4;
+
+template <int T_LEAVES, typename V, typename ACC>
+__device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U,
+                                            const V *__restrict__ xq, V *xs, uint32_t *ys)
+{
+  for (int b = threadIdx.x; b < U; b += TILE_G * T_LEAVES) {
+    uint32_t id[TILE_G];
+    V xv[TILE_G];
+#pragma unroll
+    for (int j = 0; j < TILE_G; j++) {
+      const int u = b + j * T_LEAVES;
+      id[j] = u < U ? __ldg(tile_nodes + u0 + u) & ~TL_EXCL : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < TILE_G; j++) xv[j] = b + j * T_LEAVES < U ? __ldg(xq + id[j]) : V(0);
+#pragma unroll
+    for (int j = 0; j < TILE_G; j++) {
+      const int u = b + j * T_LEAVES;
+      if (u < U) {
+        xs[u] = xv[j];
+        ACC::zero(ys, U, u);
+      }
+    }
+  }
+}
+
+// The tile's sums out: stored where the tile is the node's only toucher,
+// added atomically elsewhere.  put(id, u) writes slot u to node id.
+template <int T_LEAVES, typename PUT>
+__device__ __forceinline__ void tile_scatter(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, PUT put)
+{
+  for (int b = threadIdx.x; b < U; b += TILE_G * T_LEAVES) {
+    uint32_t id[TILE_G];
+#pragma unroll
+    for (int j = 0; j < TILE_G; j++) {
+      const int u = b + j * T_LEAVES;
+      id[j] = u < U ? __ldg(tile_nodes + u0 + u) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < TILE_G; j++)
+      if (b + j * T_LEAVES < U) put(id[j], b + j * T_LEAVES);
+  }
+}
+
 template <int DIM, int T_LEAVES, typename AR>
 __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
@@ -449,11 +516,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
   V *xs = reinterpret_cast<V *>(fac + n_fac);
   uint32_t *ys = reinterpret_cast<uint32_t *>(xs + U);   // ACC::WORDS words per node
   for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) fac[k] = AR::load_factor(fm, fe, k);
-  for (int u = threadIdx.x; u < U; u += T_LEAVES) {
-    const uint32_t id = __ldg(tile_nodes + u0 + u) & ~TL_EXCL;
-    xs[u] = __ldg(xq + id);
-    ACC::zero(ys, U, u);
-  }
+  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, xq, xs, ys);
   __shared__ uint32_t s_max;
   if (threadIdx.x == 0) s_max = 0u;
   __syncthreads();
@@ -554,21 +617,19 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     }
     __syncthreads();
     const float down = ldexpf(1.0f, e - 23);
-    for (int u = threadIdx.x; u < U; u += T_LEAVES) {
-      const uint32_t id = __ldg(tile_nodes + u0 + u);
+    tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
       const int a = reinterpret_cast<const int *>(ys)[u];
       if (id & TL_EXCL) yq[id & ~TL_EXCL] = (V) a * down;
       else if (a != 0) atomicAdd(yq + id, (V) a * down);
-    }
+    });
     return;
   }
   __syncthreads();
-  for (int u = threadIdx.x; u < U; u += T_LEAVES) {
-    const uint32_t id = __ldg(tile_nodes + u0 + u);
+  tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
     const V a = ACC::get(ys, U, u);
     if (id & TL_EXCL) yq[id & ~TL_EXCL] = a;
     else if (a != V(0)) AR::add(yq + id, a);
-  }
+  });
 }
 
 template <int DIM, int TL, typename AR>
