@@ -189,7 +189,7 @@ struct Plan {
   bool fx_ready = false;
   int fx_c = 0;
   DBuf<long long> fx_fm, xq, yq;
-  DBuf<int> fx_fe, fx_sx;
+  DBuf<int> fx_sx;
   DBuf<unsigned long long> fx_amax;
   // Sum-factorised order-2 kernel (dkt_q2sf.cu): 1D transform T (row-major),
   // child-interpolation middle row, per-level diagonals, hanging-first order.

@@ -47,7 +47,7 @@ template <int DIM, typename AR>
 __global__ void __launch_bounds__(256) k_matvec_q1(
     const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
-    const void *__restrict__ fm, const int *__restrict__ fe, const typename AR::T *__restrict__ xq,
+    const void *__restrict__ fm, const typename AR::T *__restrict__ xq,
     typename AR::T *__restrict__ yq, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
     const typename AR::T *__restrict__ stvq, int conforming, const int32_t *__restrict__ leaf_list = nullptr,
     int64_t n_list = 0)
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) k_matvec_q1(
   }
   if (valid) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k] = AR::scale(v[k], fm, fe, L * NPE + rb + k);
+    for (int k = 0; k < 4; k++) v[k] = AR::scale(v[k], fm, L * NPE + rb + k);
   }
   bfly_reg<T>(v, 0);
   bfly_reg<T>(v, 1);
@@ -371,24 +371,20 @@ bool q1fx_setup(Plan &pl, cudaStream_t s)
   int emax = 0;
   std::frexp(maxD, &emax);                    // maxD < 2^emax
   const int c = -6 - dim - emax;             // max factor < 2^(-6-dim)
+  // Factor f = D * 2^c stored as fm = round(f * 2^64) < 2^(58-dim) and
+  // applied as the high word of the 128-bit product v * fm: a transformed
+  // value |v| <= 2^60 then carries an error below 2^60 * 2^-65 from the
+  // rounding of fm, on top of the floor of the product -- the same unit as
+  // the floor itself, so no per-factor exponent (and no variable shift) is
+  // needed.
   std::vector<long long> fm((size_t) nlev * NPE);
-  std::vector<int> fe((size_t) nlev * NPE);
-  for (size_t k = 0; k < D.size(); k++) {
-    const double f = std::ldexp(D[k], c);
-    if (f == 0.0) { fm[k] = 0; fe[k] = 64; continue; }
-    int ef = 0;
-    std::frexp(f, &ef);                       // f < 2^ef, ef <= -6-dim
-    const int e = 62 - ef;                    // fm = f * 2^e < 2^62
-    fe[k] = std::min(e, 126);
-    fm[k] = (long long) std::llround(std::ldexp(f, fe[k]));
-  }
+  for (size_t k = 0; k < D.size(); k++) fm[k] = (long long) std::llround(std::ldexp(D[k], c + 64));
   std::vector<float> f32(D.size());
   for (size_t k = 0; k < D.size(); k++) f32[k] = (float) D[k];
   pl.f32_f.upload(f32.data(), f32.size(), s);
   pl.f32_ready = !pl.st_ready || pl.st_n_runs == 0;
   pl.fx_c = c;
   pl.fx_fm.upload(fm.data(), fm.size(), s);
-  pl.fx_fe.upload(fe.data(), fe.size(), s);
   pl.xq.alloc(pl.n_nodes);
   pl.yq.alloc(pl.n_nodes);
   pl.fx_amax.alloc(1);
@@ -406,7 +402,7 @@ static void launch_q1fx_stale_leaves(Plan &pl, cudaStream_t s)
 {
   const unsigned threads = 256;
   k_matvec_q1<DIM, FixedArith><<<grid_for(pl.st_n_hleaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
-      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.fx_fe.p, pl.xq.p,
+      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.xq.p,
       pl.yq.p, pl.st_hzoff.p, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0, pl.st_hleaves.p, pl.st_n_hleaf);
   check_launch("matvec_q1fx_stale_leaves");
   pl.n_launch++;
@@ -424,7 +420,7 @@ static void launch_q1fx(Plan &pl, bool skip_stale, cudaStream_t s)
   }
   if (pl.tl_ready) tiled_fixed(pl, skip_stale, s);
   else k_matvec_q1<DIM, FixedArith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
-      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.fx_fe.p,
+      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p,
       pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0);
   if (!pl.tl_ready) {
     check_launch("matvec_q1fx");
@@ -444,7 +440,7 @@ static void launch_q1f32(Plan &pl, const float *x, float *y, cudaStream_t s)
   const unsigned threads = 256;
   if (pl.tl_ready) { tiled_f32(pl, x, y, s); return; }
   k_matvec_q1<DIM, F32Arith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
-      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.f32_f.p, nullptr, x, y,
+      pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.f32_f.p, x, y,
       nullptr, nullptr, nullptr, pl.conforming ? 1 : 0);
   check_launch("matvec_q1f32");
   pl.n_launch++;

@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
     const int64_t *__restrict__ tile_hb, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
     const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
-    const int *__restrict__ fe, int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
+    int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
     int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
     const int *__restrict__ skip_mesh, int skip_stride)
@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
   F *fac = reinterpret_cast<F *>(smem);
   V *xs = reinterpret_cast<V *>(fac + n_fac);
   uint32_t *ys = reinterpret_cast<uint32_t *>(xs + U);   // ACC::WORDS words per node
-  for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) fac[k] = AR::load_factor(fm, fe, k);
+  for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) fac[k] = AR::load_factor(fm, k);
   tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, xq, xs, ys);
   __shared__ uint32_t s_max;
   if (threadIdx.x == 0) s_max = 0u;
@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
 }
 
 template <int DIM, int TL, typename AR>
-static void launch_tiled(Plan &pl, const void *fm, const int *fe, const typename AR::T *x, typename AR::T *y,
+static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y,
                          const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
                          cudaStream_t s)
 {
@@ -642,18 +642,18 @@ static void launch_tiled(Plan &pl, const void *fm, const int *fe, const typename
   const size_t smem = (size_t) n_fac * sizeof(typename AR::Factor) + (size_t) 2 * pl.tl_umax * sizeof(typename AR::T);
   ensure_dyn_smem(kfn, smem);
   kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
-                                           pl.tl_lstart.p, pl.tl_nodes.p, fm, fe, n_fac, x, y, hzoff, hztab, stv,
+                                           pl.tl_lstart.p, pl.tl_nodes.p, fm, n_fac, x, y, hzoff, hztab, stv,
                                            pl.conforming ? 1 : 0, skip_stale ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p,
                                            pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride);
 }
 
 template <typename AR>
-static void launch_tiled_dim(Plan &pl, const void *fm, const int *fe, const typename AR::T *x, typename AR::T *y,
+static void launch_tiled_dim(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y,
                              const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
                              cudaStream_t s)
 {
 #define DKT_TL_CASE(D, TL) \
-  case (D) * 10000 + (TL): launch_tiled<D, TL, AR>(pl, fm, fe, x, y, hzoff, hztab, stv, skip_stale, s); break;
+  case (D) * 10000 + (TL): launch_tiled<D, TL, AR>(pl, fm, x, y, hzoff, hztab, stv, skip_stale, s); break;
   switch (pl.dim * 10000 + pl.tl_T) {
     DKT_TL_CASE(2, 128) DKT_TL_CASE(2, 256) DKT_TL_CASE(2, 512)
     DKT_TL_CASE(3, 128) DKT_TL_CASE(3, 256) DKT_TL_CASE(3, 512)
@@ -669,14 +669,14 @@ static void launch_tiled_dim(Plan &pl, const void *fm, const int *fe, const type
 // leaves that remain read no stale slot, so they need no look-up of one.
 void tiled_fixed(Plan &pl, bool skip_stale, cudaStream_t s)
 {
-  launch_tiled_dim<FixedArith>(pl, pl.fx_fm.p, pl.fx_fe.p, pl.xq.p, pl.yq.p,
+  launch_tiled_dim<FixedArith>(pl, pl.fx_fm.p, pl.xq.p, pl.yq.p,
                                (pl.st_ready && !skip_stale) ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p,
                                skip_stale, s);
 }
 
 void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
 {
-  launch_tiled_dim<F32Arith>(pl, pl.f32_f.p, nullptr, x, y, nullptr, nullptr, nullptr, false, s);
+  launch_tiled_dim<F32Arith>(pl, pl.f32_f.p, x, y, nullptr, nullptr, nullptr, false, s);
 }
 
 bool tile_size_supported(int dim, int T)
