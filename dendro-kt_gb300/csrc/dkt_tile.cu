@@ -34,6 +34,7 @@ namespace dkt {
 
 constexpr uint16_t TL_NONE = 0xFFFFu;
 constexpr uint32_t TL_EXCL = 0x80000000u;
+constexpr int TL_SINKS = 32;   // sink entries past a tile's nodes, one per lane
 
 // ---------------------------------------------------------------------------
 // Plan-time tile build: one CTA per tile sorts the tile's (node, slot) pairs
@@ -228,6 +229,27 @@ __global__ void k_tile_lstart(int64_t *__restrict__ ls, int64_t n_tile, int64_t 
   if (t <= n_tile) ls[t] = t < n_tile ? t * T : n_leaf;
 }
 
+// Slots with no node (TL_NONE) are pointed at one of TL_SINKS per-lane sink
+// entries past the tile's U nodes (U + lane): the leaf kernel reads 0 there
+// and adds into a sink that is never written out, with no test per slot.
+// Lanes of one warp have distinct sinks.  One CTA of `T` threads per tile.
+__global__ void k_tile_sinks(uint16_t *__restrict__ e2l, uint16_t *__restrict__ p2l,
+                             const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+                             const int64_t *__restrict__ ls, const int64_t *__restrict__ off, int npe)
+{
+  const int64_t t = blockIdx.x;
+  const int64_t i = ls[t] + threadIdx.x;
+  if (i >= ls[t + 1]) return;
+  const uint16_t sink = (uint16_t) (off[t + 1] - off[t] + (threadIdx.x & (TL_SINKS - 1)));
+  for (int k = 0; k < npe; k++)
+    if (e2l[i * npe + k] == TL_NONE) e2l[i * npe + k] = sink;
+  if ((info[i] >> 16) & 1u) {
+    const int64_t h = hidx[i];
+    for (int k = 0; k < npe; k++)
+      if (p2l[h * npe + k] == TL_NONE) p2l[h * npe + k] = sink;
+  }
+}
+
 void tile_setup(Plan &pl, int T, cudaStream_t s)
 {
   pl.tl_ready = false;
@@ -299,6 +321,9 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   k_tile_lstart<<<grid_for(n_tile + 1), 256, 0, s>>>(pl.tl_lstart.p, n_tile, T, pl.n_leaf);
   pl.tl_hb.alloc(n_tile + 1);
   k_tile_ranks<<<(unsigned) n_tile, T, 0, s>>>(pl.info.p, pl.hidx.p, pl.tl_lstart.p, pl.tl_hb.p);
+  // U <= 2 T npe <= 32768 (T <= 1024, npe <= 16), so U + TL_SINKS stays clear of TL_NONE
+  k_tile_sinks<<<(unsigned) n_tile, T, 0, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.hidx.p, pl.tl_lstart.p,
+                                               pl.tl_off.p, npe);
   check_launch("tile_masks");
   DKT_CUDA(cudaStreamSynchronize(s));
   if (pl.lseg.size() >= 2) {
@@ -430,9 +455,13 @@ __device__ __forceinline__ void transpose_child0(V *v)
 constexpr int TILE_G = 4;
 
 template <int T_LEAVES, typename V, typename ACC>
-__device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U,
+__device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, int Us,
                                             const V *__restrict__ xq, V *xs, uint32_t *ys)
 {
+  if (threadIdx.x < TL_SINKS) {
+    xs[U + threadIdx.x] = V(0);
+    ACC::zero(ys, Us, U + threadIdx.x);
+  }
   for (int b = threadIdx.x; b < U; b += TILE_G * T_LEAVES) {
     uint32_t id[TILE_G];
     V xv[TILE_G];
@@ -448,7 +477,7 @@ __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_no
       const int u = b + j * T_LEAVES;
       if (u < U) {
         xs[u] = xv[j];
-        ACC::zero(ys, U, u);
+        ACC::zero(ys, Us, u);
       }
     }
   }
@@ -513,10 +542,11 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
   }
   using ACC = TileAcc<AR>;
   F *fac = reinterpret_cast<F *>(smem);
+  const int Us = U + TL_SINKS;                            // the tile's nodes, then the sinks
   V *xs = reinterpret_cast<V *>(fac + n_fac);
-  uint32_t *ys = reinterpret_cast<uint32_t *>(xs + U);   // ACC::WORDS words per node
+  uint32_t *ys = reinterpret_cast<uint32_t *>(xs + Us);  // ACC::WORDS words per entry
   for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) fac[k] = AR::load_factor(fm, k);
-  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, xq, xs, ys);
+  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, Us, xq, xs, ys);
   __shared__ uint32_t s_max;
   if (threadIdx.x == 0) s_max = 0u;
   __syncthreads();
@@ -529,14 +559,15 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
       const int c = (int) ((inf >> 8) & 0xFFu);
       const int32_t hz = hzoff ? __ldg(hzoff + h) : -1;
 #pragma unroll
-      for (int k = 0; k < NPE; k++) {
-        const uint32_t p = idx16<NPE>(pw, k);
-        v[k] = V(0);
-        if (p != TL_NONE) v[k] = xs[p];
-        else if (hz >= 0) {
-          const int32_t id = __ldg(hztab + (int64_t) hz * NPE + (k ^ c));
-          if (id >= 0) v[k] = __ldg(stvq + id);
-        }
+      for (int k = 0; k < NPE; k++) v[k] = xs[idx16<NPE>(pw, k)];   // a sink reads 0
+      if (hz >= 0) {
+        // the parent slots with no node read the emulated static buffer
+#pragma unroll
+        for (int k = 0; k < NPE; k++)
+          if (idx16<NPE>(pw, k) >= (uint32_t) U) {
+            const int32_t id = __ldg(hztab + (int64_t) hz * NPE + (k ^ c));
+            if (id >= 0) v[k] = __ldg(stvq + id);
+          }
       }
       // parent -> child-0 interpolation, axes in order
 #pragma unroll
@@ -549,10 +580,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
         if ((fmask >> k) & 1u) v[k] = xs[lidx(k)];
     } else {
 #pragma unroll
-      for (int k = 0; k < NPE; k++) {
-        const uint32_t l = lidx(k);
-        v[k] = l != TL_NONE ? xs[l] : V(0);
-      }
+      for (int k = 0; k < NPE; k++) v[k] = xs[lidx(k)];
     }
     wht<DIM, V>(v);
 #pragma unroll
@@ -560,10 +588,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     wht<DIM, V>(v);
     if constexpr (std::is_same<AR, FixedArith>::value) {
 #pragma unroll
-      for (int k = 0; k < NPE; k++) {
-        const uint32_t l = lidx(k);
-        if (l != TL_NONE) ACC::add(ys, U, l, v[k]);
-      }
+      for (int k = 0; k < NPE; k++) ACC::add(ys, Us, lidx(k), v[k]);
       if (hang) {
         // transpose of the child-0 interpolation on the unfilled ranks, into the parent nodes
 #pragma unroll
@@ -573,7 +598,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
 #pragma unroll
         for (int k = 0; k < NPE; k++) {
           const uint32_t p = idx16<NPE>(pw, k);
-          if (p != TL_NONE && (conforming || !((fmask >> k) & 1u))) ACC::add(ys, U, p, v[k]);
+          if (conforming || !((fmask >> k) & 1u)) ACC::add(ys, Us, p, v[k]);
         }
       }
     } else {
@@ -590,7 +615,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     if (valid) {
 #pragma unroll
       for (int k = 0; k < NPE; k++) {
-        if (idx16<NPE>(w, k) != TL_NONE) m = fmaxf(m, fabsf(v[k]));
+        if (idx16<NPE>(w, k) < (uint32_t) U) m = fmaxf(m, fabsf(v[k]));
         m = fmaxf(m, fabsf(zt[k]));
       }
     }
@@ -603,14 +628,13 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     if (valid) {
 #pragma unroll
       for (int k = 0; k < NPE; k++) {
-        const uint32_t l = idx16<NPE>(w, k);
-        if (l != TL_NONE) atomicAdd(reinterpret_cast<int *>(ys) + l, __float2int_rn(v[k] * up));
+        atomicAdd(reinterpret_cast<int *>(ys) + idx16<NPE>(w, k), __float2int_rn(v[k] * up));
       }
       if (h >= 0) {
 #pragma unroll
         for (int k = 0; k < NPE; k++) {
           const uint32_t p = idx16<NPE>(pw, k);
-          if (p != TL_NONE && (conforming || !((fmask >> k) & 1u)))
+          if (conforming || !((fmask >> k) & 1u))
             atomicAdd(reinterpret_cast<int *>(ys) + p, __float2int_rn(zt[k] * up));
         }
       }
@@ -626,7 +650,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
   }
   __syncthreads();
   tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
-    const V a = ACC::get(ys, U, u);
+    const V a = ACC::get(ys, Us, u);
     if (id & TL_EXCL) yq[id & ~TL_EXCL] = a;
     else if (a != V(0)) AR::add(yq + id, a);
   });
@@ -639,7 +663,7 @@ static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, type
 {
   auto kfn = k_matvec_q1t<DIM, TL, AR>;
   const int n_fac = (pl.md + 1) * (1 << DIM);
-  const size_t smem = (size_t) n_fac * sizeof(typename AR::Factor) + (size_t) 2 * pl.tl_umax * sizeof(typename AR::T);
+  const size_t smem = (size_t) n_fac * sizeof(typename AR::Factor) + (size_t) 2 * (pl.tl_umax + TL_SINKS) * sizeof(typename AR::T);
   ensure_dyn_smem(kfn, smem);
   kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
                                            pl.tl_lstart.p, pl.tl_nodes.p, fm, n_fac, x, y, hzoff, hztab, stv,
