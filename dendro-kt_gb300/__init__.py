@@ -20,6 +20,7 @@ OP_IDENTITY, OP_HEAT, OP_LAPMASS, OP_CUSTOM, OP_LAPLACE, OP_MASS, OP_HEATVEC = 0
 ARITH_AUTO, ARITH_FP64, ARITH_FIXED = 0, 1, 2
 TRAVERSAL_REFERENCE, TRAVERSAL_CONFORMING = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+CG_JACOBI, CG_REFERENCE = 1, 2
 
 
 class DktError(RuntimeError):
@@ -322,14 +323,18 @@ class Matrix:
     def diagonal(self, d_dev, stream=None):
         _check(load().dkt_diagonal(self._h, _p(d_dev), _stream(stream)))
 
-    def cg(self, b_dev, x_dev, max_iter=10000, tol=1e-10, jacobi=True, stream=None):
+    def cg(self, b_dev, x_dev, max_iter=10000, tol=1e-10, jacobi=True, reference=False, stream=None):
+        """CG on device tensors.  reference=True: HeatMat::cgSolve itself (no
+        preconditioner, relative L-infinity stop).  Returns (iterations,
+        final relative residual, converged)."""
         it = ctypes.c_int(0)
         rr = ctypes.c_double(0.0)
-        rc = load().dkt_cg_solve(self._h, _p(b_dev), _p(x_dev), max_iter, tol, int(bool(jacobi)),
+        flags = CG_REFERENCE if reference else (CG_JACOBI if jacobi else 0)
+        rc = load().dkt_cg_solve(self._h, _p(b_dev), _p(x_dev), max_iter, tol, flags,
                                  ctypes.byref(it), ctypes.byref(rr), _stream(stream))
         if rc not in (OK, E_NOCONV):
             _check(rc)
-        return it.value, rr.value
+        return it.value, rr.value, rc == OK
 
     def pcg(self, b_dev, x_dev, precision=0, max_iter=100000, tol=1e-10, jacobi=True, stream=None):
         """Device-resident Jacobi-PCG (precision PREC_FP64) or mixed-precision

@@ -43,8 +43,8 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
 void q1f32_apply(Plan &pl, const float *x, float *y, bool bc_in, bool bc_out, cudaStream_t s);
 void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t s);
 void fematrix_matvec(Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
-int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,
-             cudaStream_t s);
+int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, bool linf, int *iters,
+             double *relres, cudaStream_t s);
 
 }  // namespace dkt
 
@@ -468,12 +468,33 @@ int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream)
   });
 }
 
-int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int jacobi,
+int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int flags,
                  int *iters, double *relres, void *stream)
 {
   if (!plan || !b_dev || !x_dev || max_iter < 0 || !(tol > 0)) return fail(DKT_E_ARG, "bad argument");
+  if (flags & ~(DKT_CG_JACOBI | DKT_CG_REFERENCE)) return fail(DKT_E_ARG, "unknown CG flags");
   return guarded([&]() {
-    return dkt::cg_solve(plan->pl, b_dev, x_dev, max_iter, tol, jacobi != 0, iters, relres, (cudaStream_t) stream);
+    return dkt::cg_solve(plan->pl, b_dev, x_dev, max_iter, tol, (flags & DKT_CG_JACOBI) != 0,
+                         (flags & DKT_CG_REFERENCE) != 0, iters, relres, (cudaStream_t) stream);
+  });
+}
+
+int dkt_cg_solve_host(dkt_plan plan, const double *b_host, double *x_host, int max_iter, double tol, int flags,
+                      int *iters, double *relres)
+{
+  if (!plan || !b_host || !x_host || max_iter < 0 || !(tol > 0)) return fail(DKT_E_ARG, "bad argument");
+  if (flags & ~(DKT_CG_JACOBI | DKT_CG_REFERENCE)) return fail(DKT_E_ARG, "unknown CG flags");
+  return guarded([&]() {
+    dkt::Plan &pl = plan->pl;
+    const int64_t n = pl.n_nodes;
+    dkt::DBuf<double> b(n), x(n);
+    DKT_CUDA(cudaMemcpyAsync(b.p, b_host, n * sizeof(double), cudaMemcpyHostToDevice, 0));
+    DKT_CUDA(cudaMemcpyAsync(x.p, x_host, n * sizeof(double), cudaMemcpyHostToDevice, 0));
+    const int rc = dkt::cg_solve(pl, b.p, x.p, max_iter, tol, (flags & DKT_CG_JACOBI) != 0,
+                                 (flags & DKT_CG_REFERENCE) != 0, iters, relres, 0);
+    DKT_CUDA(cudaMemcpyAsync(x_host, x.p, n * sizeof(double), cudaMemcpyDeviceToHost, 0));
+    DKT_CUDA(cudaStreamSynchronize(0));
+    return rc;
   });
 }
 

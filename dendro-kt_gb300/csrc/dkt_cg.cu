@@ -1,7 +1,10 @@
 // Conjugate gradients on feMatrix::matVec in the form of HeatMat::cgSolve
 // (FEM/examples/src/heatMat.cpp:164-325), with an optional Jacobi
-// preconditioner.  All vectors stay on the device; reductions are two-stage
-// with a fixed summation order, so a solve is bitwise reproducible.
+// preconditioner, stopping on the relative 2-norm residual -- or, in the
+// reference mode, HeatMat::cgSolve itself: no preconditioner and the stop
+// ||r||_inf / ||b||_inf <= tol (heatMat.cpp:207-227, 251-257).  All vectors
+// stay on the device; reductions are two-stage with a fixed summation order,
+// so a solve is bitwise reproducible.
 #include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
@@ -41,6 +44,51 @@ __global__ void k_sum_partials(const double *__restrict__ part, int n, double *_
     __syncthreads();
   }
   if (threadIdx.x == 0) *out = sh[0];
+}
+
+// max |a_i| per block, NaN if the block holds a NaN (normLInfty,
+// include/mathUtils.tcc:69-80, returns NaN for any NaN entry)
+__global__ void k_absmax_partial(const double *__restrict__ a, int64_t n, double *__restrict__ part)
+{
+  __shared__ double sh[RED_THREADS];
+  double m = 0.0;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
+    const double v = fabs(a[i]);
+    m = (v > m || v != v) ? v : m;   // a NaN sticks
+  }
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = RED_THREADS / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      const double v = sh[threadIdx.x + o];
+      if (v > sh[threadIdx.x] || v != v) sh[threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_max_partials(const double *__restrict__ part, int n, double *__restrict__ out)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double m = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double v = part[i];
+    if (v > m || v != v) m = v;
+    if (m != m) break;
+  }
+  *out = m;
+}
+
+static double norm_inf(const double *a, int64_t n, double *part, double *res, cudaStream_t s)
+{
+  k_absmax_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, n, part);
+  k_max_partials<<<1, 32, 0, s>>>(part, RED_BLOCKS, res);
+  check_launch("norm_inf");
+  double h = 0.0;
+  DKT_CUDA(cudaMemcpyAsync(&h, res, sizeof(double), cudaMemcpyDeviceToHost, s));
+  DKT_CUDA(cudaStreamSynchronize(s));
+  return h;
 }
 
 static double dot(const double *a, const double *b, int64_t n, double *part, double *res, cudaStream_t s)
@@ -143,38 +191,58 @@ void diagonal(const Plan &pl, double *diag, cudaStream_t s)
   DKT_CUDA(cudaStreamSynchronize(s));   // dq is freed on return
 }
 
-int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, int *iters, double *relres,
-             cudaStream_t s)
+// linf: the reference's own stopping rule (no preconditioner, relative
+// L-infinity residual); status -5 when max_iter iterations did not reach tol.
+int cg_solve(Plan &pl, const double *b, double *x, int max_iter, double tol, bool jacobi, bool linf, int *iters,
+             double *relres, cudaStream_t s)
 {
   const int64_t n = pl.n_nodes;
+  if (linf) jacobi = false;
   DBuf<double> r(n), z(n), p(n), Ap(n), dinv(jacobi ? n : 0), part(RED_BLOCKS), res(1);
   if (jacobi) {
     diagonal(pl, dinv.p, s);
     k_invert_diag<<<grid_for(n), 256, 0, s>>>(dinv.p, n);
   }
-  fematrix_matvec(pl, x, Ap.p, 1.0, s);
-  k_sub<<<grid_for(n), 256, 0, s>>>(b, Ap.p, r.p, n);
-  double nb = std::sqrt(dot(b, b, n, part.p, res.p, s));
+  auto norm = [&](const double *v) {
+    return linf ? norm_inf(v, n, part.p, res.p, s) : std::sqrt(dot(v, v, n, part.p, res.p, s));
+  };
+  double nb = norm(b);
   if (nb == 0.0) nb = 1.0;
-  k_prec<<<grid_for(n), 256, 0, s>>>(r.p, jacobi ? dinv.p : nullptr, z.p, n);
-  DKT_CUDA(cudaMemcpyAsync(p.p, z.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  double rz = dot(r.p, z.p, n, part.p, res.p, s);
-  double rr = std::sqrt(dot(r.p, r.p, n, part.p, res.p, s)) / nb;
-  int it = 0;
-  while (rr > tol && it < max_iter) {
-    fematrix_matvec(pl, p.p, Ap.p, 1.0, s);
-    const double pAp = dot(p.p, Ap.p, n, part.p, res.p, s);
-    if (pAp == 0.0) break;
-    const double alpha = rz / pAp;
-    k_axpy2<<<grid_for(n), 256, 0, s>>>(x, r.p, p.p, Ap.p, alpha, n);
-    rr = std::sqrt(dot(r.p, r.p, n, part.p, res.p, s)) / nb;
-    it++;
-    if (rr <= tol) break;
+  double rz = 0.0, rr = 0.0;
+  // r = b - A x, z, p = z, r.z and the relative residual
+  auto start = [&]() {
+    fematrix_matvec(pl, x, Ap.p, 1.0, s);
+    k_sub<<<grid_for(n), 256, 0, s>>>(b, Ap.p, r.p, n);
     k_prec<<<grid_for(n), 256, 0, s>>>(r.p, jacobi ? dinv.p : nullptr, z.p, n);
-    const double rz2 = dot(r.p, z.p, n, part.p, res.p, s);
-    const double beta = rz2 / rz;
-    rz = rz2;
-    k_pupdate<<<grid_for(n), 256, 0, s>>>(p.p, z.p, beta, n);
+    DKT_CUDA(cudaMemcpyAsync(p.p, z.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    rz = dot(r.p, z.p, n, part.p, res.p, s);
+    rr = norm(r.p) / nb;
+  };
+  start();
+  int it = 0;
+  for (int confirm = 0;; confirm++) {
+    while (rr > tol && it < max_iter) {
+      fematrix_matvec(pl, p.p, Ap.p, 1.0, s);
+      const double pAp = dot(p.p, Ap.p, n, part.p, res.p, s);
+      if (pAp == 0.0) break;
+      const double alpha = rz / pAp;
+      k_axpy2<<<grid_for(n), 256, 0, s>>>(x, r.p, p.p, Ap.p, alpha, n);
+      rr = norm(r.p) / nb;
+      it++;
+      if (rr <= tol) break;
+      k_prec<<<grid_for(n), 256, 0, s>>>(r.p, jacobi ? dinv.p : nullptr, z.p, n);
+      const double rz2 = dot(r.p, z.p, n, part.p, res.p, s);
+      const double beta = rz2 / rz;
+      rz = rz2;
+      k_pupdate<<<grid_for(n), 256, 0, s>>>(p.p, z.p, beta, n);
+    }
+    // The reference mode stops on its recursive residual, as cgSolve does.
+    // Otherwise convergence is confirmed on the true residual b - A x, and
+    // the iteration restarts from x while that is still above tol (the
+    // recursive residual drifts from it by round-off).
+    if (linf || rr > tol || confirm >= 8) break;
+    start();
+    if (rr <= tol || it >= max_iter) break;
   }
   check_launch("cg");
   DKT_CUDA(cudaStreamSynchronize(s));

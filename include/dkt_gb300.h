@@ -185,11 +185,32 @@ int dkt_fevector_compute_vec(dkt_plan plan, const double *in_dev, double *out_de
 int dkt_diagonal(dkt_plan plan, double *diag_dev, void *stream);
 
 /* CG on feMatrix::matVec in the form of HeatMat::cgSolve
- * (FEM/examples/src/heatMat.cpp:164-325), optionally Jacobi-preconditioned,
- * stopping when ||r||_2 <= tol * ||b||_2.  x_dev holds the initial guess and
- * receives the solution.  iters/relres may be NULL. */
-int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int jacobi,
+ * (FEM/examples/src/heatMat.cpp:164-325).  flags:
+ *   0                  unpreconditioned, stopping when ||r||_2 <= tol ||b||_2,
+ *                      confirmed on the true residual b - A x (the iteration
+ *                      restarts from x while that is above tol);
+ *   DKT_CG_JACOBI      the same, Jacobi-preconditioned;
+ *   DKT_CG_REFERENCE   HeatMat::cgSolve itself: no preconditioner,
+ *                      alpha = <r0,r0>/<p,Ap>, beta = <r1,r1>/<r0,r0>, stopping
+ *                      when ||r||_inf <= tol ||b||_inf (||b||_inf = 0 counts as 1,
+ *                      heatMat.cpp:207-227) on the plan's own traversal; relres
+ *                      is then the final relative L-infinity residual (the tol
+ *                      that cgSolve writes back) and iters the iteration at
+ *                      which it stopped (0 if x already met tol).
+ * x_dev holds the initial guess and receives the solution.  iters/relres may
+ * be NULL.  Returns DKT_OK on convergence, -5 when max_iter was reached
+ * (cgSolve's status 1). */
+#define DKT_CG_JACOBI 1
+#define DKT_CG_REFERENCE 2
+int dkt_cg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int max_iter, double tol, int flags,
                  int *iters, double *relres, void *stream);
+
+/* The same with host arrays (b, and x in and out; copies in and out, then
+ * synchronises): with DKT_CG_REFERENCE the drop-in for HeatMat::cgSolve
+ * (FEM/examples/src/heatMat.cpp:164-325) in the feMatrixGpu binding
+ * (include/feMatrixGpu.h). */
+int dkt_cg_solve_host(dkt_plan plan, const double *b_host, double *x_host, int max_iter, double tol, int flags,
+                      int *iters, double *relres);
 
 #define DKT_PREC_FP64 0
 #define DKT_PREC_MIXED 1

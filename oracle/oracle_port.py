@@ -56,6 +56,7 @@ def lib():
         L.dkto_set_stale_mode.argtypes = [ctypes.c_int]
         L.dkto_set_conforming.argtypes = [ctypes.c_int]
         L.dkto_cg.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_double, P, P]
+        L.dkto_cg_ref.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, P, P, P]
         _lib = L
     return _lib
 
@@ -163,6 +164,17 @@ class DA:
         _check(lib().dkto_cg(self._h, _ptr(b), _ptr(x), None if d is None else _ptr(d),
                              max_iter, tol, ctypes.byref(it), ctypes.byref(rr)))
         return x, it.value, rr.value
+
+    def cg_ref(self, b, x0=None, max_iter=1000, tol=1e-10):
+        """HeatMat::cgSolve: unpreconditioned, relative L-infinity stop.
+        Returns (x, iterations, final relative residual, status)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.n) if x0 is None else np.array(x0, dtype=np.float64)
+        it, st = ctypes.c_int(0), ctypes.c_int(0)
+        rr = ctypes.c_double(0)
+        _check(lib().dkto_cg_ref(self._h, _ptr(b), _ptr(x), max_iter, tol, ctypes.byref(it), ctypes.byref(rr),
+                                 ctypes.byref(st)))
+        return x, it.value, rr.value, st.value
 
     def __del__(self):
         try:

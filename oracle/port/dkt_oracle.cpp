@@ -1105,4 +1105,55 @@ int dkto_cg(void *hp, const double *b, double *x, const double *diag, int max_it
   return 0;
 }
 
+// HeatMat::cgSolve itself (FEM/examples/src/heatMat.cpp:164-325): no
+// preconditioner, alpha = <r0,r0>/<p,Ap>, beta = <r1,r1>/<r0,r0>, stopping
+// when ||r||_inf / ||b||_inf <= tol (||b||_inf = 0 counts as 1); dots are plain
+// sums in index order (include/mathUtils.tcc:205-212) and the L-infinity norm
+// is NaN if any entry is NaN (include/mathUtils.tcc:69-80).  iters = the
+// iteration at which it stopped (0 when the initial guess already meets tol,
+// max_iter when it did not converge); resid = the last relative residual;
+// status 0 on convergence, 1 otherwise.
+int dkto_cg_ref(void *hp, const double *b, double *x, int max_iter, double tol, int *iters, double *resid,
+                int *status)
+{
+  OracleDA *h = (OracleDA *) hp;
+  const size_t n = h->nodeL.size();
+  std::vector<double> p(n), Ax(n), Ap(n), r0(n), r1(n);
+  auto dot = [&](const std::vector<double> &a, const std::vector<double> &c) {
+    double s = 0.0;
+    for (size_t i = 0; i < n; i++) s += a[i] * c[i];
+    return s;
+  };
+  auto linf = [&](const double *v) {
+    if (n == 0) return 0.0;
+    if (std::isnan(v[0])) return (double) NAN;
+    double m = std::fabs(v[0]);
+    for (size_t i = 1; i < n; i++) {
+      if (std::isnan(v[i])) return (double) NAN;
+      if (m < std::fabs(v[i])) m = std::fabs(v[i]);
+    }
+    return m;
+  };
+  double normb = linf(b);
+  dkto_fematrix_matvec(hp, x, Ax.data());
+  for (size_t i = 0; i < n; i++) { r0[i] = b[i] - Ax[i]; p[i] = r0[i]; }
+  if (normb == 0.0) normb = 1;
+  double res = linf(r0.data()) / normb;
+  *iters = 0;
+  *status = 1;
+  if (res <= tol) { *resid = res; *status = 0; return 0; }
+  for (int i = 1; i <= max_iter; i++) {
+    dkto_fematrix_matvec(hp, p.data(), Ap.data());
+    const double alpha = dot(r0, r0) / dot(p, Ap);
+    for (size_t e = 0; e < n; e++) { x[e] += alpha * p[e]; r1[e] = r0[e] - alpha * Ap[e]; }
+    res = linf(r1.data()) / normb;
+    *iters = i;
+    if (res <= tol) { *status = 0; break; }
+    const double beta = dot(r1, r1) / dot(r0, r0);
+    for (size_t e = 0; e < n; e++) { p[e] = r1[e] + beta * p[e]; r0[e] = r1[e]; }
+  }
+  *resid = res;
+  return 0;
+}
+
 }  // extern "C"

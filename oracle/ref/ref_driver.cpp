@@ -19,6 +19,11 @@
 //             mass right-hand side with boundary zeroing; a 3D operator
 //   * the raw fem::matvec output (FEM/include/matvec.h:231-240), no pre/post
 //   * the RefElement 1D matrices (FEM/src/refel.cpp:75-220)
+//   * op 7: HeatEq::HeatMat<dim>::cgSolve (FEM/examples/src/heatMat.cpp:164-325)
+//     from x = 0 on b = the HeatVec<dim> right-hand side of the input vector
+//     (feVector::computeVec, as FEM/examples/src/heatEq.cpp:112-118 builds
+//     it), with the tolerance and iteration cap of the input; the matVec
+//     outputs are HeatMat's (as op 1)
 //
 // The binary formats are the ones tests/golden/refio.py writes and reads.
 #include <mpi.h>
@@ -34,6 +39,8 @@
 #include "heatVec.h"
 
 #include <chrono>
+#include <iostream>
+#include <sstream>
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
@@ -198,6 +205,9 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
   std::vector<double> xIn(nxIn);
   in.arr(xIn.data(), nxIn);
   const double interpTol = inputKind == 3 ? in.get<double>() : 0.0;
+  // op 7: the cgSolve tolerance and iteration cap
+  const double cgTol = op == 7 ? in.get<double>() : 0.0;
+  const int cgMaxIter = op == 7 ? in.get<int32_t>() : 0;
 
   std::vector<TN> tree;
   double t0 = now_s();
@@ -254,7 +264,7 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
   lm.setProblemDimensions(pmin, pmax);
   hv.setProblemDimensions(pmin, pmax);
   if (op == 0) mv = [&](const double *a, double *b) { idm.matVec(a, b, 1.0); };
-  else if (op == 1) mv = [&](const double *a, double *b) { heat.matVec(a, b, 1.0); };
+  else if (op == 1 || op == 7) mv = [&](const double *a, double *b) { heat.matVec(a, b, 1.0); };
   else if (op == 6) mv = [&](const double *a, double *b) { hv.computeVec(a, b, 1.0); };
   else mv = [&](const double *a, double *b) { lm.matVec(a, b, 1.0); };
 
@@ -274,7 +284,7 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
     using namespace std::placeholders;
     fem::EleOpT<double> eop;
     if (op == 0) eop = std::bind(&IdentityMat<dim>::elementalMatVec, &idm, _1, _2, _3, _4);
-    else if (op == 1) eop = std::bind(&HeatEq::HeatMat<dim>::elementalMatVec, &heat, _1, _2, _3, _4);
+    else if (op == 1 || op == 7) eop = std::bind(&HeatEq::HeatMat<dim>::elementalMatVec, &heat, _1, _2, _3, _4);
     else if (op == 6) eop = std::bind(&HeatEq::HeatVec<dim>::elementalComputeVec, &hv, _1, _2, _3, _4);
     else eop = std::bind(&LapMassMat<dim>::elementalMatVec, &lm, _1, _2, _3, _4);
     fem::matvec(xg.data(), yraw.data(), da->getTNCoords(), nTotal, *da->getTreePartFront(), *da->getTreePartBack(),
@@ -302,6 +312,31 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
   out.arr(re->getQ1d(), M * M);
   out.arr(re->getDg1d(), M * M);
   out.arr(re->getWgq(), M);
+  if (op == 7) {
+    // b = HeatVec right-hand side of x; x0 = 0; cgSolve writes its final
+    // relative L-infinity residual into tol and prints the iteration at
+    // which it stopped, which is read back from its output
+    std::vector<double> rhs(nLocal, 0.0), sol(nLocal, 0.0);
+    hv.computeVec(x.data(), rhs.data(), 1.0);
+    double tol = cgTol;
+    std::ostringstream log;
+    std::streambuf *saved = std::cout.rdbuf(log.rdbuf());
+    const int status = heat.cgSolve(sol.data(), rhs.data(), cgMaxIter, tol);
+    std::cout.rdbuf(saved);
+    int iters = 0;
+    std::istringstream lines(log.str());
+    std::string line;
+    while (std::getline(lines, line)) {
+      int k = 0;
+      if (std::sscanf(line.c_str(), " iteration : %d", &k) == 1) iters = k;
+    }
+    if (status != 0) iters = cgMaxIter;
+    out.put<int32_t>(status);
+    out.put<double>(tol);
+    out.put<int32_t>(iters);
+    out.put<uint64_t>(nLocal); out.arr(rhs.data(), nLocal);
+    out.put<uint64_t>(nLocal); out.arr(sol.data(), nLocal);
+  }
   delete da;
   return 0;
 }

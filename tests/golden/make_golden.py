@@ -5,7 +5,10 @@ unmodified Dendro-KT sources + single-rank MPI stand-in) and records, for a
 set of small meshes, the reference's own outputs:
   tree (SFC order), DA node list (coords, levels), boundary node ids,
   input vector x, feMatrix::matVec output y, raw fem::matvec output y_raw,
-  and the RefElement 1D operators.
+  and the RefElement 1D operators; for the driver's op 7 also
+  HeatMat<3>::cgSolve from x = 0 on the HeatVec<3> right-hand side of x
+  (status, final relative L-infinity residual, iterations, right-hand side,
+  solution).
 Usage:  python tests/golden/make_golden.py [name-substring ...]
         (with arguments, only the fixtures whose names contain one of them)
 """
@@ -28,12 +31,15 @@ def build_ref():
     subprocess.run(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j2"], check=True)
 
 
+CG_TOL, CG_MAX_ITER = 1e-10, 1000
+
+
 def run_ref(curve, dim, md, order, op, coords, levels, kind, seed, x=None, interp_tol=None):
     exe = os.path.join(REF_DIR, "ref_driver_" + curve)
     inp = os.path.join("/tmp", "dkt_golden_in.bin")
     out = os.path.join("/tmp", "dkt_golden_out.bin")
     refio.write_input(inp, dim, md, order, op, coords, levels, input_kind=kind, seed=seed, x=x,
-                      interp_tol=interp_tol)
+                      interp_tol=interp_tol, cg_tol=CG_TOL, cg_max_iter=CG_MAX_ITER)
     subprocess.run([exe, inp, out], check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return refio.read_output(out, dim)
 
@@ -64,6 +70,9 @@ def cases():
         # RefElement::getElementSz() is 0 and HeatVec's Jacobian 1/(0/sz) is inf.
         out.append((f"{curve}_d3_p1_op6_gauss300", curve, 3, 8, 1, 6, ("gauss", 300)))
         out.append((f"{curve}_d3_p1_op6_ex1L4", curve, 3, 6, 1, 6, ("ex1", 4)))
+        # HeatMat<3>::cgSolve (unpreconditioned CG, relative L-infinity stop);
+        # the driver's op 7, stored as op 1 (its matVec outputs are HeatMat's)
+        out.append((f"{curve}_d3_p1_op1_cg_gauss300", curve, 3, 8, 1, 7, ("gauss", 300)))
     # ot::DA<dim>::DA(func, ...): function2Octree of the two test fields of the
     # driver (1 / (eps + |x - c|^2)), then 2:1 balance
     for dim, md, order, tol in ((2, 8, 1, 0.2), (3, 7, 1, 1.0), (3, 7, 2, 1.0), (4, 6, 1, 4.0)):
@@ -101,9 +110,13 @@ def main(only=()):
             c, lv = gen(dim, arg, md)
             r = run_ref(curve, dim, md, order, op, c, lv, 2, seed=1)
             inputs = dict(in_kind=2, in_coords=c, in_levels=lv)
+        extra = {}
+        if op == 7:
+            extra = dict(cg_tol=CG_TOL, cg_max_iter=CG_MAX_ITER, cg_status=r["cg_status"],
+                         cg_resid=r["cg_resid"], cg_iters=r["cg_iters"], cg_b=r["cg_b"], cg_x=r["cg_x"])
         np.savez_compressed(
-            os.path.join(HERE, name + ".npz"),
-            curve=curve, dim=dim, md=md, order=order, op=op, seed=1, **inputs,
+            os.path.join(HERE, name + ".npz"), **extra,
+            curve=curve, dim=dim, md=md, order=order, op=1 if op == 7 else op, seed=1, **inputs,
             tree_coords=r["tree_coords"], tree_levels=r["tree_levels"],
             node_coords=r["node_coords"], node_levels=r["node_levels"], bdry=r["bdry"],
             x=r["x"], y=r["y"], y_raw=r["y_raw"],

@@ -9,7 +9,7 @@ import numpy as np
 
 
 def write_input(path, dim, max_depth, order, op, coords, levels=None, input_kind=0,
-                n_calls=1, seed=1, x=None, interp_tol=None):
+                n_calls=1, seed=1, x=None, interp_tol=None, cg_tol=None, cg_max_iter=None):
     coords = np.ascontiguousarray(coords, dtype=np.uint32).reshape(-1, dim)
     with open(path, "wb") as f:
         f.write(b"DKTI")
@@ -27,6 +27,8 @@ def write_input(path, dim, max_depth, order, op, coords, levels=None, input_kind
             f.write(x.tobytes())
         if input_kind == 3:
             f.write(struct.pack("<d", interp_tol))
+        if op == 7:
+            f.write(struct.pack("<di", cg_tol, cg_max_iter))
 
 
 def read_output(path, dim):
@@ -63,4 +65,14 @@ def read_output(path, dim):
     out["Q1d"] = take(np.float64, m * m).reshape(m, m)
     out["Dg"] = take(np.float64, m * m).reshape(m, m)
     out["W"] = take(np.float64, m)
+    if off < len(buf):
+        # op 7: HeatMat::cgSolve status, final relative L-infinity residual,
+        # iterations, right-hand side and solution
+        out["cg_status"] = int(take(np.int32, 1)[0])
+        out["cg_resid"] = float(take(np.float64, 1)[0])
+        out["cg_iters"] = int(take(np.int32, 1)[0])
+        n = int(take(np.uint64, 1)[0])
+        out["cg_b"] = take(np.float64, n)
+        n = int(take(np.uint64, 1)[0])
+        out["cg_x"] = take(np.float64, n)
     return out

@@ -134,3 +134,32 @@ def test_no_stale_parent_reads_on_nondegenerate_meshes():
         da = op.DA(g["tree_coords"], g["tree_levels"], dim, int(g["order"]), int(g["op"]))
         da.matvec(g["x"])
         assert da.stats()["stale_reads"] == 0, path
+
+
+CG = [g for g in GOLDEN if "_cg_" in os.path.basename(g)]
+
+
+@pytest.mark.parametrize("path", CG, ids=[os.path.basename(p)[:-4] for p in CG])
+def test_oracle_cgsolve_matches_reference(path):
+    """HeatMat<3>::cgSolve restated in the oracle (no preconditioner,
+    relative L-infinity stop) against the reference's own run on the same
+    mesh and right-hand side: the same iteration count and final residual,
+    and the solution within 1e-12 relative."""
+    import __graft_entry__ as ge
+    g = np.load(path)
+    dim, md = int(g["dim"]), int(g["md"])
+    if os.path.basename(path).startswith("hilbert_"):
+        dkt = ge.load_package()
+        op.set_curve(dim, md, *dkt.curve_tables(dkt.CURVE_HILBERT, dim))
+    else:
+        op.set_curve(dim, md)
+    try:
+        da = op.DA(g["tree_coords"], g["tree_levels"], dim, int(g["order"]), int(g["op"]))
+        assert np.array_equal(da.node_coords, g["node_coords"])
+        x, it, res, status = da.cg_ref(g["cg_b"], max_iter=int(g["cg_max_iter"]), tol=float(g["cg_tol"]))
+        assert status == int(g["cg_status"]) == 0
+        assert it == int(g["cg_iters"])
+        assert abs(res - float(g["cg_resid"])) <= 1e-6 * float(g["cg_resid"])
+        assert _rel(x, g["cg_x"]) <= 1e-12
+    finally:
+        op.set_curve(dim, md)
