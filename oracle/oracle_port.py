@@ -57,6 +57,8 @@ def lib():
         L.dkto_set_conforming.argtypes = [ctypes.c_int]
         L.dkto_cg.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_double, P, P]
         L.dkto_cg_ref.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, P, P, P]
+        L.dkto_moving_ball.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, P, P, ctypes.c_int,
+                                        ctypes.c_int64, P]
         _lib = L
     return _lib
 
@@ -99,6 +101,25 @@ def tree_balance(points, dim, max_pts=1):
     n = ctypes.c_int64(0)
     _check(lib().dkto_tree_balance(dim, _ptr(pts), pts.shape[0], max_pts, ctypes.byref(n)))
     c = np.empty((n.value, dim), np.uint32)
+    lv = np.empty(n.value, np.uint8)
+    _check(lib().dkto_tree_fetch(_ptr(c), _ptr(lv)))
+    return c, lv
+
+
+def moving_ball_tree(level, radius=0.2, halfwidth=None, c0=(0.3, 0.3, 0.3), c1=(0.7, 0.7, 0.7), part_level=0,
+                     part_index=0):
+    """The spacetime moving-ball mesh (dim 4, max_depth of set_curve),
+    2:1 balanced; with part_level > 0 only the level-part_level cell of
+    Morton index part_index is refined (one partition of the mesh).
+    Returns (coords, levels) in no particular order."""
+    if halfwidth is None:
+        halfwidth = 2.0 ** -level
+    a0 = np.ascontiguousarray(c0, dtype=np.float64)
+    a1 = np.ascontiguousarray(c1, dtype=np.float64)
+    n = ctypes.c_int64(0)
+    _check(lib().dkto_moving_ball(level, radius, halfwidth, _ptr(a0), _ptr(a1), part_level, part_index,
+                                  ctypes.byref(n)))
+    c = np.empty((n.value, 4), np.uint32)
     lv = np.empty(n.value, np.uint8)
     _check(lib().dkto_tree_fetch(_ptr(c), _ptr(lv)))
     return c, lv

@@ -955,6 +955,106 @@ int dkto_tree_balance(int dim, const uint32_t *pts, int64_t n, int64_t max_pts, 
   *n_out = (int64_t) s_treeL.size();
   return 0;
 }
+// The benchmark's spacetime moving-ball mesh (dim 4: x, y, z, t), restated
+// for the CPU side: every cell whose box meets the shell
+// | |(x,y,z) - c(t)| - R | <= w, c(t) = c0 + (c1 - c0) t, is refined down to
+// `level`, then the tree is 2:1 balanced with propagateNeighbours +
+// reconstruction (src/tsort.cpp:777-854, as loc_tree_balancing).  For a cell
+// [lo,hi]^3 x [t0,t1] the distance from c(t) to the spatial box is convex in t,
+// so its minimum over [t0,t1] is found by golden-section search (80 steps);
+// the largest distance is convex too and peaks at t0 or t1.  The cell meets
+// the shell iff min-distance <= R + w and max-distance >= R - w.
+// With part_level > 0 only the cell of Morton index part_index at level
+// part_level is refined (the rest of the domain stays at the coarsest cells
+// on the path to it before balancing): one partition of the mesh.
+namespace {
+double mb_box_dist(const double *lo, const double *hi, const double *c)
+{
+  double s = 0.0;
+  for (int d = 0; d < 3; d++) {
+    const double g = c[d] < lo[d] ? lo[d] - c[d] : (c[d] > hi[d] ? c[d] - hi[d] : 0.0);
+    s += g * g;
+  }
+  return std::sqrt(s);
+}
+double mb_box_far(const double *lo, const double *hi, const double *c)
+{
+  double s = 0.0;
+  for (int d = 0; d < 3; d++) {
+    const double f = std::max(std::fabs(c[d] - lo[d]), std::fabs(hi[d] - c[d]));
+    s += f * f;
+  }
+  return std::sqrt(s);
+}
+bool mb_meets(const TN<4> &c, double R, double w, const double *c0, const double *c1)
+{
+  const double s = std::ldexp(1.0, -(int) g_md), h = std::ldexp(1.0, -(int) c.lev);
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; d++) { lo[d] = c.x[d] * s; hi[d] = lo[d] + h; }
+  const double t0 = c.x[3] * s, t1 = t0 + h;
+  auto centre = [&](double t, double *out) { for (int d = 0; d < 3; d++) out[d] = c0[d] + (c1[d] - c0[d]) * t; };
+  double ca[3], cb[3];
+  centre(t0, ca);
+  centre(t1, cb);
+  const double dmax = std::max(mb_box_far(lo, hi, ca), mb_box_far(lo, hi, cb));
+  double a = t0, b = t1;
+  const double gr = 0.5 * (std::sqrt(5.0) - 1.0);
+  for (int it = 0; it < 80; it++) {
+    const double m1 = b - gr * (b - a), m2 = a + gr * (b - a);
+    double p1[3], p2[3];
+    centre(m1, p1);
+    centre(m2, p2);
+    if (mb_box_dist(lo, hi, p1) <= mb_box_dist(lo, hi, p2)) b = m2; else a = m1;
+  }
+  double pm[3];
+  centre(0.5 * (a + b), pm);
+  const double dmin = std::min({mb_box_dist(lo, hi, pm), mb_box_dist(lo, hi, ca), mb_box_dist(lo, hi, cb)});
+  return dmin <= R + w && dmax >= R - w;
+}
+void mb_refine(const TN<4> &c, unsigned level, double R, double w, const double *c0, const double *c1,
+               unsigned part_level, const TN<4> &part, std::vector<TN<4>> &leaves)
+{
+  // inside the partition cell (or on the path of cells down to it): the
+  // cell and the partition cell agree on their common levels
+  const unsigned common = std::min(c.lev, part_level);
+  bool inside = true;
+  for (int d = 0; d < 4; d++)
+    if ((part.x[d] >> (g_md - common)) != (c.x[d] >> (g_md - common))) inside = false;
+  const bool split = inside && (c.lev < part_level || (c.lev < level && mb_meets(c, R, w, c0, c1)));
+  if (!split) { leaves.push_back(c); return; }
+  for (int ch = 0; ch < 16; ch++) {
+    TN<4> k = c;
+    k.lev = c.lev + 1;
+    const uint32_t cl = 1u << (g_md - k.lev);
+    for (int d = 0; d < 4; d++) k.x[d] = c.x[d] | (((ch >> d) & 1) ? cl : 0u);
+    mb_refine(k, level, R, w, c0, c1, part_level, part, leaves);
+  }
+}
+}  // namespace
+
+int dkto_moving_ball(int level, double R, double w, const double *c0, const double *c1, int part_level,
+                     int64_t part_index, int64_t *n_out)
+{
+  if (level < 1 || level > (int) g_md || part_level < 0 || part_level > level) { g_err = "bad level"; return 1; }
+  s_treeC.clear(); s_treeL.clear();
+  TN<4> part{};
+  part.lev = (uint32_t) part_level;
+  for (int l = 0; l < part_level; l++) {
+    const int64_t digit = (part_index >> (4 * (part_level - 1 - l))) & 15;
+    for (int d = 0; d < 4; d++)
+      if ((digit >> d) & 1) part.x[d] |= 1u << (g_md - 1 - l);
+  }
+  TN<4> root{};
+  root.lev = 0;
+  std::vector<TN<4>> leaves, nt;
+  mb_refine(root, (unsigned) level, R, w, c0, c1, (unsigned) part_level, part, leaves);
+  propagate_neighbours(leaves);
+  loc_tree_construction<4>(leaves.data(), nt, 1, 0, leaves.size(), 1, g_md, 0, root);
+  for (auto &e : nt) { for (int d = 0; d < 4; d++) s_treeC.push_back(e.x[d]); s_treeL.push_back((uint8_t) e.lev); }
+  *n_out = (int64_t) s_treeL.size();
+  return 0;
+}
+
 int dkto_tree_fetch(uint32_t *coords, uint8_t *levels)
 {
   std::copy(s_treeC.begin(), s_treeC.end(), coords);

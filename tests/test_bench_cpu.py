@@ -45,3 +45,26 @@ def test_reference_arm_two_ranks_gloo():
     assert len(lines) == 1   # rank 0 only
     _check(lines[0])
     assert lines[0]["n_gpus"] == 2
+
+
+def test_reference_arm_mesh_equals_library_mesh():
+    """The reference arm builds its meshes with the oracle's restatement of
+    the moving-ball refinement and 2:1 balance (no GB300 library in that
+    process); it reproduces the library's host-built tree cell for cell, and
+    its level-2 partitions hold the same cells inside their partition cell."""
+    import numpy as np
+    import __graft_entry__ as ge
+    import oracle_port as orc
+    dkt = ge.load_package()
+    orc.set_curve(4, 10)
+    oc, ol = orc.moving_ball_tree(4)
+    hc, hl = dkt.moving_ball_tree(max_depth=10, level=4)
+    a = sorted(map(tuple, np.concatenate([oc, ol[:, None]], 1).tolist()))
+    b = sorted(map(tuple, np.concatenate([hc, hl[:, None]], 1).tolist()))
+    assert a == b
+    k = 5                                        # level-2 cell, Morton digits (0, 5)
+    pc, pl = orc.moving_ball_tree(4, part_level=2, part_index=k)
+    anc = np.array([((k >> d) & 1) << 8 for d in range(4)], np.uint32)
+    ins = lambda c, l: np.all((c >= anc) & (c < anc + 256), axis=1) & (l >= 2)
+    assert set(map(tuple, np.concatenate([pc, pl[:, None]], 1)[ins(pc, pl)].tolist())) == \
+        set(map(tuple, np.concatenate([oc, ol[:, None]], 1)[ins(oc, ol)].tolist()))
