@@ -76,6 +76,7 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
     out.tl_hb.alloc(nt + 1);
     out.tl_fm.alloc(std::max<int64_t>(nh, 1));
     out.tl_nodes.alloc(std::max<int64_t>(su, 1));
+    out.tl_tau.alloc(std::max<int64_t>(nt, 1));
     out.tl_e2l.alloc((size_t) nl * npe);
     out.tl_p2l.alloc((size_t) std::max<int64_t>(nh, 1) * npe);
   }
@@ -99,7 +100,8 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
       copy_to(out.tl_fm.p + bh, p->tl_fm.p, (size_t) p->n_hang, s);
       if (p->tl_sum_u)
         k_offset_u32<<<grid_for(p->tl_sum_u), 256, 0, s>>>(p->tl_nodes.p, out.tl_nodes.p + bu, p->tl_sum_u,
-                                                            (uint32_t) bn, 0x80000000u);
+                                                            (uint32_t) bn, 0xF8000000u);   // keep level + flag bits
+      copy_to(out.tl_tau.p + bt, p->tl_tau.p, (size_t) p->tl_n, s);
       copy_to(out.tl_e2l.p + bl * npe, p->tl_e2l.p, ne, s);
       copy_to(out.tl_p2l.p + bh * npe, p->tl_p2l.p, np_, s);
     }

@@ -117,6 +117,9 @@ __host__ __device__ inline uint64_t cell_key(const uint32_t *a, int lev, int dim
   return k;
 }
 
+// Status of the allocation-free product (dkt_matvec.cu).
+enum { NOALLOC_OK = 0, NOALLOC_TOO_LARGE = 1, NOALLOC_CUDA = 2 };
+
 // Device-resident distributed array (ot::DA on one rank).
 struct DA {
   int dim = 3, order = 1, md = 10, curve = 0;
@@ -188,8 +191,23 @@ struct Plan {
   int arith = 0;                     // 0 auto, 1 native FP64, 2 fixed point
   bool fx_ready = false;
   int fx_c = 0;
-  DBuf<long long> fx_fm, xq, yq;
+  DBuf<long long> fx_fm, xq, yq;     // fx_fm: [unit level tau][leaf level L][mode] (q1fx_setup)
   DBuf<int> fx_sx;
+  // Dyadic scaling (every level factor of the operator a power of two or
+  // zero): 0 = multiply-high factors; 1 / 2 / 3 = the tiled kernel scales a
+  // mode value with small integer multiples and shifts (Laplacian term, mass
+  // term, both; fx_shift[L] = s_L | d_L << 8), and yq carries fx_div = 3^dim
+  // times the product.  |xq| <= 2^fx_bx.
+  int fx_scale = 0, fx_div = 1, fx_bx = 56;
+  DBuf<uint32_t> fx_shift;
+  // Per-level units: a level-L leaf's contributions are exact in a unit
+  // 2^(-kappa L) times the level-0 unit, kappa the level exponent of the
+  // operator's leading term (dim - 2 for the Laplacian, dim for the mass);
+  // node n keeps its sum in the unit of fx_lam[n], the coarsest level of a
+  // leaf adding into it, and a tile computes in the unit of tl_tau[t], its
+  // coarsest leaf level.  kappa = 0: one unit for all.
+  int fx_kappa = 0;
+  DBuf<uint8_t> fx_lam;
   DBuf<unsigned long long> fx_amax;
   // Sum-factorised order-2 kernel (dkt_q2sf.cu): 1D transform T (row-major),
   // child-interpolation middle row, per-level diagonals, hanging-first order.
@@ -211,6 +229,7 @@ struct Plan {
   DBuf<int64_t> tl_off, tl_lstart, tl_hb;   // per tile: node-list offset, first leaf, first hanging index
   DBuf<uint32_t> tl_nodes, tl_fm;     // distinct nodes (| exclusive flag); reflected fill masks
   DBuf<uint16_t> tl_e2l, tl_p2l;
+  DBuf<uint8_t> tl_tau;              // per tile: coarsest leaf level (its fixed-point unit)
   // Optional CUDA-event timing of the leaf kernel on its launching stream.
   bool timing = false;
   std::vector<cudaEvent_t> ev;       // start/stop pairs of the current window

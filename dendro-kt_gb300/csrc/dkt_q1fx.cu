@@ -19,6 +19,7 @@
 // 2^(54-dim) and a node can absorb 256 of them; y = yq * 2^-(sx+c).
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include "dkt_internal.cuh"
 #include "dkt_q1.cuh"
 
@@ -43,14 +44,27 @@ __device__ __forceinline__ void bfly_reg(T *v, int d)
   }
 }
 
+// A contribution of a level-L leaf (fixed point: in level L's unit) added
+// into node n, whose sum is in the unit of its coarsest contributing level
+// lam[n] <= L: floor(v / 2^(kappa (L - lam[n]))).
+template <typename AR>
+__device__ __forceinline__ void add_to_node(typename AR::T *yq, int n, typename AR::T v, int L,
+                                            const uint8_t *__restrict__ lam, int kappa)
+{
+  if constexpr (std::is_same<AR, FixedArith>::value) {
+    if (lam) v >>= kappa * (L - (int) __ldg(lam + n));
+  }
+  AR::add(yq + n, v);
+}
+
 template <int DIM, typename AR>
 __global__ void __launch_bounds__(256) k_matvec_q1(
     const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, const uint32_t *__restrict__ fill, int64_t n_leaf, int64_t n_hang,
     const void *__restrict__ fm, const typename AR::T *__restrict__ xq,
     typename AR::T *__restrict__ yq, const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab,
-    const typename AR::T *__restrict__ stvq, int conforming, const int32_t *__restrict__ leaf_list = nullptr,
-    int64_t n_list = 0)
+    const typename AR::T *__restrict__ stvq, int conforming, const uint8_t *__restrict__ lam, int kappa, int nlev,
+    const int32_t *__restrict__ leaf_list = nullptr, int64_t n_list = 0)
 {
   using T = typename AR::T;
   constexpr int NPE = 1 << DIM, LPL = NPE / 4;
@@ -132,8 +146,11 @@ __global__ void __launch_bounds__(256) k_matvec_q1(
     }
   }
   if (valid) {
+    // fixed point: the factors of the leaf's own level unit (row L of the
+    // per-unit table); binary32: one row per level
+    const int frow = std::is_same<AR, FixedArith>::value ? (L * nlev + L) * NPE : L * NPE;
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k] = AR::scale(v[k], fm, L * NPE + rb + k);
+    for (int k = 0; k < 4; k++) v[k] = AR::scale(v[k], fm, frow + rb + k);
   }
   bfly_reg<T>(v, 0);
   bfly_reg<T>(v, 1);
@@ -148,7 +165,7 @@ __global__ void __launch_bounds__(256) k_matvec_q1(
   }
 #pragma unroll
   for (int k = 0; k < 4; k++)
-    if (nd[k] >= 0) AR::add(yq + nd[k], v[k]);
+    if (nd[k] >= 0) add_to_node<AR>(yq, nd[k], v[k], L, lam, kappa);
   if (grp_hang) {
     // transpose of the interpolation on the unfilled ranks, into the parent nodes
     T z[4];
@@ -178,7 +195,7 @@ __global__ void __launch_bounds__(256) k_matvec_q1(
     if (hang) {
 #pragma unroll
       for (int k = 0; k < 4; k++)
-        if (pn[k] >= 0 && (conforming || !((fmask >> (rb + k)) & 1u))) AR::add(yq + pn[k], z[k]);
+        if (pn[k] >= 0 && (conforming || !((fmask >> (rb + k)) & 1u))) add_to_node<AR>(yq, pn[k], z[k], L, lam, kappa);
     }
   }
 }
@@ -227,14 +244,14 @@ __global__ void __launch_bounds__(256) k_absmax(const double *__restrict__ x, in
   }
 }
 
-// sx from max|x|: xq = round(x * 2^sx) keeps |xq| <= 2^(60-dim)
-__device__ __forceinline__ int fixed_exponent(const unsigned long long *amax, int dim)
+// sx from max|x|: xq = round(x * 2^sx) keeps |xq| <= 2^bx
+__device__ __forceinline__ int fixed_exponent(const unsigned long long *amax, int bx)
 {
   const unsigned long long b = *amax;
-  if (b == 0) return 60 - dim;
+  if (b == 0) return bx;
   const int ef = (int) (b >> 52);                       // biased exponent (|x| finite)
   const int e = ef == 0 ? -1010 - __clzll(b) : ef - 1022;   // max|x| < 2^e, as frexp
-  return (60 - dim) - e;
+  return bx - e;
 }
 
 // x * 2^k as two exact power-of-two products (|k| <= 2046); ldexp(x, k)
@@ -302,9 +319,9 @@ inline unsigned pair_grid(int64_t n) { return grid_for((n + 1) / 2); }
 
 // xq = round(x * 2^sx)
 __global__ void k_to_fixed(const double *__restrict__ x, long long *__restrict__ xq, int64_t n,
-                           const unsigned long long *__restrict__ amax, int *__restrict__ sx_out, int dim)
+                           const unsigned long long *__restrict__ amax, int *__restrict__ sx_out, int bx)
 {
-  const int sx = fixed_exponent(amax, dim);
+  const int sx = fixed_exponent(amax, bx);
   const int64_t i = 2 * ((int64_t) blockIdx.x * blockDim.x + threadIdx.x);
   if (i == 0) *sx_out = sx;
   if (i + 1 < n && (reinterpret_cast<uintptr_t>(x) & 15u) == 0) {
@@ -316,17 +333,40 @@ __global__ void k_to_fixed(const double *__restrict__ x, long long *__restrict__
   }
 }
 
+// round(v / DIV), halves away from zero (DIV a compile-time constant: a
+// multiply-high, no division instruction)
+template <int DIV>
+__device__ __forceinline__ long long div_round(long long v)
+{
+  if constexpr (DIV == 1) return v;
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long) v : (unsigned long long) v;
+  const long long q = (long long) ((a + DIV / 2) / (unsigned long long) DIV);
+  return v < 0 ? -q : q;
+}
+
+// y = round(yq / DIV) * 2^-(sx + c + kappa lam[i]): the dyadic scaling leaves
+// 3^dim times the product in yq (DIV = 3^dim), the per-mode factors the
+// product itself; node i's sum is in the unit of its level lam[i] (lam
+// null: one unit)
+template <int DIV>
 __global__ void k_from_fixed(const long long *__restrict__ yq, double *__restrict__ y, int64_t n,
-                             const int *__restrict__ sx, int c)
+                             const int *__restrict__ sx, int c, const uint8_t *__restrict__ lam, int kappa)
 {
   const int sh = -(*sx + c);
   const int64_t i = 2 * ((int64_t) blockIdx.x * blockDim.x + threadIdx.x);
   if (i + 1 < n && (reinterpret_cast<uintptr_t>(y) & 15u) == 0) {
     const longlong2 v = reinterpret_cast<const longlong2 *>(yq)[i >> 1];
-    reinterpret_cast<double2 *>(y)[i >> 1] = make_double2(double_from_fixed(v.x, sh), double_from_fixed(v.y, sh));
+    int s0 = sh, s1 = sh;
+    if (lam) {
+      const uchar2 l = reinterpret_cast<const uchar2 *>(lam)[i >> 1];
+      s0 -= kappa * l.x;
+      s1 -= kappa * l.y;
+    }
+    reinterpret_cast<double2 *>(y)[i >> 1] =
+        make_double2(double_from_fixed(div_round<DIV>(v.x), s0), double_from_fixed(div_round<DIV>(v.y), s1));
   } else {
-    if (i < n) y[i] = double_from_fixed(yq[i], sh);
-    if (i + 1 < n) y[i + 1] = double_from_fixed(yq[i + 1], sh);
+    if (i < n) y[i] = double_from_fixed(div_round<DIV>(yq[i]), sh - (lam ? kappa * lam[i] : 0));
+    if (i + 1 < n) y[i + 1] = double_from_fixed(div_round<DIV>(yq[i + 1]), sh - (lam ? kappa * lam[i + 1] : 0));
   }
 }
 
@@ -348,10 +388,51 @@ __global__ void k_min_level(const uint32_t *__restrict__ info, int64_t n, int *_
   atomicMin(out, m);
 }
 
+// lam[n] = the coarsest level of a leaf that adds into node n (its own
+// ranks, and the parent ranks of the hanging leaves)
+__global__ void k_node_minlev(const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info,
+                              const int32_t *__restrict__ hidx, const int32_t *__restrict__ p2n, int64_t n_leaf,
+                              int npe, uint32_t *__restrict__ lam)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_leaf) return;
+  const uint32_t inf = info[i];
+  const uint32_t L = inf & 0xFFu;
+  for (int k = 0; k < npe; k++) {
+    const int32_t n = e2n[i * npe + k];
+    if (n >= 0) atomicMin(lam + n, L);
+  }
+  if ((inf >> 16) & 1u) {
+    const int64_t h = hidx[i];
+    for (int k = 0; k < npe; k++) {
+      const int32_t n = p2n[h * npe + k];
+      if (n >= 0) atomicMin(lam + n, L);
+    }
+  }
+}
+__global__ void k_lam_narrow(const uint32_t *__restrict__ in, uint8_t *__restrict__ out, int64_t n, uint32_t dflt)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (uint8_t) (in[i] == 0xFFFFFFFFu ? dflt : in[i]);
+}
+
 void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s);
 
 // Host setup of the per-(level, mode) factors.  Returns false when the
 // operator is not one of the diagonalisable Q1 built-ins.
+//
+// Fixed-point units.  The built-in operators are K_L = alpha_L A + beta_L B
+// (A the Laplacian, B the mass); on the unit cube alpha_L and beta_L are
+// powers of two that fall by 2^kappa per level (kappa = dim - 2 for the
+// Laplacian, dim for the mass).  One unit for every level would leave the
+// finest levels' contributions 2^(kappa (L - lmin)) smaller than the unit's
+// scale -- some forty bits at level 8 in 4D instead of fifty.  So each level L
+// has its own unit, 2^(-kappa L) times the level-0 unit: a node keeps its sum
+// in the unit of the coarsest level adding into it (fx_lam), a tile computes
+// in the unit of its coarsest leaf level tau (tl_tau) and converts each node
+// sum once when it flushes it, and the per-leaf kernel computes in its leaf's
+// own unit.  fx_fm holds the multiply-high factors of every (unit level tau,
+// leaf level L >= tau, mode): row tau is a tile's factor table.
 bool q1fx_setup(Plan &pl, cudaStream_t s)
 {
   if (pl.order != 1 || pl.op.kind == OP_CUSTOM || pl.n_leaf == 0) return false;
@@ -364,6 +445,7 @@ bool q1fx_setup(Plan &pl, cudaStream_t s)
   int lmin = 0;
   DKT_CUDA(cudaMemcpyAsync(&lmin, dmin.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   DKT_CUDA(cudaStreamSynchronize(s));
+  // D_L[s]: the element matrix of level L in the Hadamard basis
   std::vector<double> D((size_t) nlev * NPE, 0.0);
   double maxD = 0.0;
   for (int L = 0; L < nlev; L++)
@@ -385,23 +467,115 @@ bool q1fx_setup(Plan &pl, cudaStream_t s)
       if (L >= lmin) maxD = std::max(maxD, std::fabs(v));
     }
   if (!(maxD > 0.0)) return false;
-  int emax = 0;
-  std::frexp(maxD, &emax);                    // maxD < 2^emax
-  const int c = -6 - dim - emax;             // max factor < 2^(-6-dim)
-  // Factor f = D * 2^c stored as fm = round(f * 2^64) < 2^(58-dim) and
-  // applied as the high word of the 128-bit product v * fm: a transformed
-  // value |v| <= 2^60 then carries an error below 2^60 * 2^-65 from the
-  // rounding of fm, on top of the floor of the product -- the same unit as
-  // the floor itself, so no per-factor exponent (and no variable shift) is
-  // needed.
-  std::vector<long long> fm((size_t) nlev * NPE);
-  for (size_t k = 0; k < D.size(); k++) fm[k] = (long long) std::llround(std::ldexp(D[k], c + 64));
+  // In the Hadamard basis 6^dim D_L[s] = C1(k) alpha_L + C2(k) beta_L with
+  // k = popcount(s), C1(k) = k 3^(dim-k+1), C2(k) = 3^(dim-k) (integers).
+  int p3 = 1;
+  for (int a = 0; a < dim; a++) p3 *= 3;
+  std::vector<double> C1(dim + 1), C2(dim + 1);
+  for (int k = 0; k <= dim; k++) {
+    int t = 1;
+    for (int a = 0; a < dim - k; a++) t *= 3;
+    C2[k] = t;
+    C1[k] = k == 0 ? 0.0 : (double) k * t * 3;
+  }
+  // Dyadic operators: every alpha_L, beta_L (L >= lmin) a power of two or zero.
+  const int kind = pl.op.kind;
+  bool dy = kind == OP_LAPMASS || kind == OP_LAPLACE || kind == OP_MASS || kind == OP_HEAT || kind == OP_HEATVEC;
+  int mode = 0;
+  std::vector<int> ea(nlev, 0), eb(nlev, 0);
+  auto pow2 = [](double v, int &e) {   // v = 2^e exactly
+    int q = 0;
+    const double m = std::frexp(v, &q);
+    e = q - 1;
+    return m == 0.5;
+  };
+  for (int L = lmin; L < nlev && dy; L++) {
+    const double al = pl.op.alpha[L], be = pl.op.beta[L];
+    if (al != 0.0) { mode |= 1; dy = dy && al > 0.0 && pow2(al, ea[L]); }
+    if (be != 0.0) { mode |= 2; dy = dy && be > 0.0 && pow2(be, eb[L]); }
+  }
+  dy = dy && mode != 0;
+  if (dy) {
+    // the integer form against D computed directly
+    for (int L = lmin; L < nlev; L++)
+      for (int sidx = 0; sidx < NPE; sidx++) {
+        const int k = __builtin_popcount(sidx);
+        const double e = (C1[k] * pl.op.alpha[L] + C2[k] * pl.op.beta[L]) / std::ldexp((double) p3, dim);
+        const double d = D[(size_t) L * NPE + sidx];
+        if (std::fabs(e - d) > 1e-15 * std::fabs(d)) dy = false;
+      }
+  }
+  // kappa: the level exponent of the leading term
+  int kappa = 0;
+  if (dy && lmin + 1 < nlev) {
+    const std::vector<int> &ex = (mode & 1) ? ea : eb;
+    kappa = ex[lmin] - ex[lmin + 1];
+    for (int L = lmin; L + 1 < nlev; L++)
+      if (ex[L] - ex[L + 1] != kappa) kappa = -1;
+    if (kappa < 0 || kappa > 4) kappa = 0;
+  }
+  // Per level the scaled factors F_L[s] (6^dim D_L[s] when dyadic, else
+  // D_L[s]); unit exponents cp + kappa L keep F_L 2^(cp + kappa L) below
+  // 2^-6 for every level and mode (dyadic), or below 2^(-6-dim) (one unit).
+  auto F = [&](int L, int sidx) {
+    return dy ? C1[__builtin_popcount(sidx)] * pl.op.alpha[L] + C2[__builtin_popcount(sidx)] * pl.op.beta[L]
+              : D[(size_t) L * NPE + sidx];
+  };
+  double g = 0.0;
+  for (int L = lmin; L < nlev; L++)
+    for (int sidx = 0; sidx < NPE; sidx++) g = std::max(g, std::ldexp(std::fabs(F(L, sidx)), kappa * L));
+  int eg = 0;
+  std::frexp(g, &eg);                        // g < 2^eg
+  const int cp = dy ? -6 - eg : -6 - dim - eg;
+  // fm[(tau nlev + L) NPE + s] = round(F_L[s] 2^(cp + kappa tau + 64)) < 2^58
+  // for lmin <= tau <= L (0 elsewhere): a transformed value (below
+  // 2^(bx + dim)) times the factor, high word, stays below 2^(bx + dim - 6)
+  std::vector<long long> fm((size_t) nlev * nlev * NPE, 0);
+  for (int tau = lmin; tau < nlev; tau++)
+    for (int L = tau; L < nlev; L++)
+      for (int sidx = 0; sidx < NPE; sidx++)
+        fm[((size_t) tau * nlev + L) * NPE + sidx] =
+            (long long) std::llround(std::ldexp(F(L, sidx), cp + kappa * tau + 64));
+  // Dyadic scaling in the tiled kernel: the mode value w of a level-L leaf
+  // in a tile of unit level tau becomes
+  //   (C1(k) w + (C2(k) w >> d_L)) >> (s_L - kappa tau)       (both terms)
+  //   (C(k) w) >> (s_L - kappa tau)                          (one term)
+  // with every shift below 32 (two-instruction shifts); otherwise the
+  // multiply-high factors are used.
+  std::vector<uint32_t> sh(nlev, 0u);
+  int sc_mode = 0;
+  if (dy) {
+    sc_mode = mode;
+    for (int L = lmin; L < nlev && sc_mode; L++) {
+      const int e_lead = (mode & 1) ? ea[L] : eb[L];   // the leading term's exponent
+      const int sl = -(e_lead + cp);
+      const int dl = (mode == 3) ? ea[L] - eb[L] : 0;
+      // the coarsest unit a level-L leaf can be computed in is level lmin's
+      if (sl - kappa * L < 0 || sl - kappa * lmin > 31 || dl < 0 || dl > 31 || (mode == 3 && dl < 1)) sc_mode = 0;
+      sh[L] = (uint32_t) sl | ((uint32_t) dl << 8);
+    }
+  }
+  pl.fx_shift.upload(sh.data(), sh.size(), s);
+  pl.fx_fm.upload(fm.data(), fm.size(), s);
+  pl.fx_scale = sc_mode;
+  pl.fx_div = dy ? p3 : 1;
+  pl.fx_bx = dy ? 60 - 2 * dim : 60 - dim;
+  pl.fx_c = dy ? cp + dim : cp;
+  pl.fx_kappa = kappa;
+  if (kappa > 0) {
+    DBuf<uint32_t> lam32(pl.n_nodes);
+    DKT_CUDA(cudaMemsetAsync(lam32.p, 0xFF, pl.n_nodes * sizeof(uint32_t), s));
+    k_node_minlev<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.n_leaf, NPE,
+                                                      lam32.p);
+    pl.fx_lam.alloc(pl.n_nodes);
+    k_lam_narrow<<<grid_for(pl.n_nodes), 256, 0, s>>>(lam32.p, pl.fx_lam.p, pl.n_nodes, (uint32_t) lmin);
+    check_launch("node_levels");
+    DKT_CUDA(cudaStreamSynchronize(s));
+  }
   std::vector<float> f32(D.size());
   for (size_t k = 0; k < D.size(); k++) f32[k] = (float) D[k];
   pl.f32_f.upload(f32.data(), f32.size(), s);
   pl.f32_ready = !pl.st_ready || pl.st_n_runs == 0;
-  pl.fx_c = c;
-  pl.fx_fm.upload(fm.data(), fm.size(), s);
   pl.xq.alloc(pl.n_nodes);
   pl.yq.alloc(pl.n_nodes);
   pl.fx_amax.alloc(1);
@@ -420,7 +594,8 @@ static void launch_q1fx_stale_leaves(Plan &pl, cudaStream_t s)
   const unsigned threads = 256;
   k_matvec_q1<DIM, FixedArith><<<grid_for(pl.st_n_hleaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.xq.p,
-      pl.yq.p, pl.st_hzoff.p, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0, pl.st_hleaves.p, pl.st_n_hleaf);
+      pl.yq.p, pl.st_hzoff.p, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0,
+      pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr, pl.fx_kappa, pl.md + 1, pl.st_hleaves.p, pl.st_n_hleaf);
   check_launch("matvec_q1fx_stale_leaves");
   pl.n_launch++;
 }
@@ -438,7 +613,8 @@ static void launch_q1fx(Plan &pl, bool skip_stale, cudaStream_t s)
   if (pl.tl_ready) tiled_fixed(pl, skip_stale, s);
   else k_matvec_q1<DIM, FixedArith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p,
-      pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0);
+      pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0,
+      pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr, pl.fx_kappa, pl.md + 1);
   if (!pl.tl_ready) {
     check_launch("matvec_q1fx");
     pl.n_launch++;
@@ -458,7 +634,7 @@ static void launch_q1f32(Plan &pl, const float *x, float *y, cudaStream_t s)
   if (pl.tl_ready) { tiled_f32(pl, x, y, s); return; }
   k_matvec_q1<DIM, F32Arith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.f32_f.p, x, y,
-      nullptr, nullptr, nullptr, pl.conforming ? 1 : 0);
+      nullptr, nullptr, nullptr, pl.conforming ? 1 : 0, nullptr, 0, pl.md + 1);
   check_launch("matvec_q1f32");
   pl.n_launch++;
 }
@@ -538,7 +714,7 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
   const int64_t n = pl.n_nodes;
   DKT_CUDA(cudaMemsetAsync(pl.fx_amax.p, 0, sizeof(unsigned long long), s));
   k_absmax<<<std::max<unsigned>(1u, std::min<unsigned>(grid_for(n, 1024), 152 * 8)), 256, 0, s>>>(x, n, pl.fx_amax.p);
-  k_to_fixed<<<pair_grid(n), 256, 0, s>>>(x, pl.xq.p, n, pl.fx_amax.p, pl.fx_sx.p, pl.dim);
+  k_to_fixed<<<pair_grid(n), 256, 0, s>>>(x, pl.xq.p, n, pl.fx_amax.p, pl.fx_sx.p, pl.fx_bx);
   check_launch("to_fixed");
   pl.n_launch += 2;
   if (bc && pl.n_bdry > 0) {
@@ -574,7 +750,14 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
       case 4: launch_q1fx_stale_leaves<4>(pl, s); break;
     }
   }
-  k_from_fixed<<<pair_grid(n), 256, 0, s>>>(pl.yq.p, y, n, pl.fx_sx.p, pl.fx_c);
+  const uint8_t *lam = pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr;
+  switch (pl.fx_div) {
+#define DKT_FROM(D) \
+  case D: k_from_fixed<D><<<pair_grid(n), 256, 0, s>>>(pl.yq.p, y, n, pl.fx_sx.p, pl.fx_c, lam, pl.fx_kappa); break;
+    DKT_FROM(1) DKT_FROM(9) DKT_FROM(27) DKT_FROM(81)
+#undef DKT_FROM
+    default: throw std::runtime_error("unsupported fixed-point divisor");
+  }
   check_launch("from_fixed");
   pl.n_launch++;
   if (bc && pl.n_bdry > 0) {

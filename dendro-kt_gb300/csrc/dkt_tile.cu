@@ -33,7 +33,12 @@
 namespace dkt {
 
 constexpr uint16_t TL_NONE = 0xFFFFu;
+// A tile's node entry: node id (bits 0-26), the node's fixed-point unit level
+// (bits 27-30, see Plan::fx_lam) and the exclusive flag (bit 31: no other
+// tile touches the node).
 constexpr uint32_t TL_EXCL = 0x80000000u;
+constexpr uint32_t TL_ID = 0x07FFFFFFu;
+constexpr int TL_LAM = 27;
 constexpr int TL_SINKS = 32;   // sink entries past a tile's nodes, one per lane
 
 // ---------------------------------------------------------------------------
@@ -51,7 +56,7 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(
     int mode, const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
     const int32_t *__restrict__ p2n, int64_t n_leaf, int npe, int T, int cap, uint32_t *__restrict__ node_tiles,
     uint32_t *__restrict__ tile_cnt, const int64_t *__restrict__ tile_off, uint32_t *__restrict__ tile_nodes,
-    uint16_t *__restrict__ e2l, uint16_t *__restrict__ p2l)
+    uint16_t *__restrict__ e2l, uint16_t *__restrict__ p2l, const uint8_t *__restrict__ lam)
 // (mode 1 writes the maps of hanging leaves reflected: rank r at position r ^ c)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -116,7 +121,9 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(
     if (head) {
       rank++;
       if (mode == 0) atomicAdd(node_tiles + node, 1u);
-      else tile_nodes[base + rank - 1] = node | (node_tiles[node] == 1u ? TL_EXCL : 0u);
+      else
+        tile_nodes[base + rank - 1] = node | (node_tiles[node] == 1u ? TL_EXCL : 0u) |
+                                      (lam ? ((uint32_t) lam[node] & 15u) << TL_LAM : 0u);
     }
     if (mode == 1) {
       const int s = (int) (uint32_t) a;
@@ -223,6 +230,19 @@ __global__ void k_tile_ranks(uint32_t *__restrict__ info, const int32_t *__restr
   }
 }
 
+// tau[t] = the coarsest leaf level of tile t (its fixed-point unit)
+__global__ void k_tile_tau(const uint32_t *__restrict__ info, const int64_t *__restrict__ ls,
+                           uint8_t *__restrict__ tau)
+{
+  __shared__ uint32_t m;
+  if (threadIdx.x == 0) m = 255u;
+  __syncthreads();
+  const int64_t i = ls[blockIdx.x] + threadIdx.x;
+  if (i < ls[blockIdx.x + 1]) atomicMin(&m, info[i] & 0xFFu);
+  __syncthreads();
+  if (threadIdx.x == 0) tau[blockIdx.x] = (uint8_t) (m == 255u ? 0u : m);
+}
+
 __global__ void k_tile_lstart(int64_t *__restrict__ ls, int64_t n_tile, int64_t T, int64_t n_leaf)
 {
   const int64_t t = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -261,6 +281,7 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   while (cap < 2 * T * npe) cap <<= 1;
   cap = std::max(cap, TB_THREADS);
   if (cap > 65536) throw std::invalid_argument("tile too large");   // 16-bit local indices
+  if (pl.n_nodes > (int64_t) TL_ID + 1) throw std::invalid_argument("too many nodes for tiles");
   const int64_t n_tile = (pl.n_leaf + T - 1) / T;
   if (pl.seg.empty()) {
     // hanging leaves first within each tile (a single mesh: a batch keeps the
@@ -293,7 +314,7 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   ensure_dyn_smem(k_tile_build, smem);
   k_tile_build<<<(unsigned) n_tile, TB_THREADS, smem, s>>>(0, pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.n_leaf,
                                                           npe, T, cap, node_tiles.p, cnt.p, nullptr, nullptr,
-                                                          nullptr, nullptr);
+                                                          nullptr, nullptr, nullptr);
   check_launch("tile_count");
   // offsets (host scan: one value per tile) and the largest tile
   std::vector<uint32_t> hc(n_tile);
@@ -313,7 +334,8 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   DKT_CUDA(cudaMemsetAsync(pl.tl_p2l.p, 0xFF, (size_t) std::max<int64_t>(pl.n_hang, 1) * npe * sizeof(uint16_t), s));
   k_tile_build<<<(unsigned) n_tile, TB_THREADS, smem, s>>>(1, pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.n_leaf,
                                                           npe, T, cap, node_tiles.p, cnt.p, pl.tl_off.p,
-                                                          pl.tl_nodes.p, pl.tl_e2l.p, pl.tl_p2l.p);
+                                                          pl.tl_nodes.p, pl.tl_e2l.p, pl.tl_p2l.p,
+                                                          pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr);
   check_launch("tile_fill");
   pl.tl_fm.alloc(std::max<int64_t>(pl.n_hang, 1));
   k_tile_fmask<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.info.p, pl.hidx.p, pl.fill.p, pl.n_leaf, npe, pl.tl_fm.p);
@@ -324,6 +346,8 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   // U <= 2 T npe <= 32768 (T <= 1024, npe <= 16), so U + TL_SINKS stays clear of TL_NONE
   k_tile_sinks<<<(unsigned) n_tile, T, 0, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.hidx.p, pl.tl_lstart.p,
                                                pl.tl_off.p, npe);
+  pl.tl_tau.alloc(n_tile);
+  k_tile_tau<<<(unsigned) n_tile, T, 0, s>>>(pl.info.p, pl.tl_lstart.p, pl.tl_tau.p);
   check_launch("tile_masks");
   DKT_CUDA(cudaStreamSynchronize(s));
   if (pl.lseg.size() >= 2) {
@@ -449,6 +473,86 @@ __device__ __forceinline__ void transpose_child0(V *v)
       }
 }
 
+// The integer multiples of the dyadic scaling (6^dim D_L = C1(k) alpha_L +
+// C2(k) beta_L, k the popcount of the mode), passed as a kernel parameter:
+// their loads are constant-bank operands of the multiply-adds.
+struct DyConst {
+  uint32_t c1[5], c2[5];
+};
+static int pow3_i(int e) { return e <= 0 ? 1 : 3 * pow3_i(e - 1); }
+static int dy_c1(int dim, int k) { return k == 0 ? 0 : k * pow3_i(dim - k + 1); }
+static int dy_c2(int dim, int k) { return pow3_i(dim - k); }
+
+// c * v (0 <= c < 2^31, the product within 63 bits): one 32 x 32 -> 64
+// multiply of the low word and one multiply-add of the high word.
+__device__ __forceinline__ long long mul_small(long long v, uint32_t c)
+{
+  const uint32_t lo = (uint32_t) (unsigned long long) v, hi = (uint32_t) ((unsigned long long) v >> 32);
+  unsigned long long p;
+  asm("mul.wide.u32 %0, %1, %2;" : "=l"(p) : "r"(lo), "r"(c));
+  uint32_t phi = (uint32_t) (p >> 32);
+  asm("mad.lo.u32 %0, %1, %2, %0;" : "+r"(phi) : "r"(hi), "r"(c));
+  return (long long) (((unsigned long long) phi << 32) | (uint32_t) p);
+}
+// v >> s (arithmetic) for 0 <= s <= 31: a funnel shift of the low word and a
+// shift of the high word.
+__device__ __forceinline__ long long sar_lt32(long long v, uint32_t s)
+{
+  const uint32_t lo = (uint32_t) (unsigned long long) v, hi = (uint32_t) ((unsigned long long) v >> 32);
+  uint32_t rlo, rhi;
+  asm("shf.r.clamp.b32 %0, %1, %2, %3;" : "=r"(rlo) : "r"(lo), "r"(hi), "r"(s));
+  asm("shr.s32 %0, %1, %2;" : "=r"(rhi) : "r"(hi), "r"(s));
+  return (long long) (((unsigned long long) rhi << 32) | rlo);
+}
+
+// v[k] <- sum over the subsets j of k of v[j] (integers; two axes per pass,
+// each output of a pass at most one three-input sum)
+template <int DIM, typename T>
+__device__ __forceinline__ void subset_sums(T (&v)[1 << DIM])
+{
+  constexpr int D2 = DIM / 2 * 2;
+#pragma unroll
+  for (int d = 0; d < D2; d += 2)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (3 << d))) {
+        const int i1 = 1 << d, i2 = 2 << d;
+        const T a = v[k], b = v[k | i1], c = v[k | i2], e = v[k | i1 | i2];
+        const T t = a + b;
+        v[k | i1] = t;
+        v[k | i2] = a + c;
+        v[k | i1 | i2] = t + c + e;
+      }
+#pragma unroll
+  for (int d = D2; d < DIM; d++)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (1 << d))) v[k | (1 << d)] += v[k];
+}
+// v[j] <- sum over the supersets k of j of v[k]
+template <int DIM, typename T>
+__device__ __forceinline__ void superset_sums(T (&v)[1 << DIM])
+{
+  constexpr int D2 = DIM / 2 * 2;
+#pragma unroll
+  for (int d = 0; d < D2; d += 2)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (3 << d))) {
+        const int i1 = 1 << d, i2 = 2 << d;
+        const T a = v[k], b = v[k | i1], c = v[k | i2], e = v[k | i1 | i2];
+        const T t = b + e;
+        v[k | i1] = t;
+        v[k | i2] = c + e;
+        v[k] = t + a + c;
+      }
+#pragma unroll
+  for (int d = D2; d < DIM; d++)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (1 << d))) v[k] += v[k | (1 << d)];
+}
+
 // A thread's node slots of the tile are visited in groups of four, the four
 // id loads issued before anything that depends on them: one global round trip
 // per group for the ids and one for the values, instead of two per slot.
@@ -468,7 +572,7 @@ __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_no
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) {
       const int u = b + j * T_LEAVES;
-      id[j] = u < U ? __ldg(tile_nodes + u0 + u) & ~TL_EXCL : 0u;
+      id[j] = u < U ? __ldg(tile_nodes + u0 + u) & TL_ID : 0u;
     }
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) xv[j] = b + j * T_LEAVES < U ? __ldg(xq + id[j]) : V(0);
@@ -501,7 +605,11 @@ __device__ __forceinline__ void tile_scatter(const uint32_t *__restrict__ tile_n
   }
 }
 
-template <int DIM, int T_LEAVES, typename AR>
+// SC (fixed point only): 0 = per-(level, mode) multiply-high factors of the
+// tile's unit (fm: the per-unit factor table); 1, 2, 3 = dyadic scaling with
+// the Laplacian term (bit 0) and / or the mass term (bit 1), fm then pointing
+// at the per-level shift words.
+template <int DIM, int T_LEAVES, typename AR, int SC>
 __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
     const int64_t *__restrict__ tile_hb, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
@@ -509,7 +617,8 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
     int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
-    const int *__restrict__ skip_mesh, int skip_stride)
+    const int *__restrict__ skip_mesh, int skip_stride, const __grid_constant__ DyConst dyc,
+    const uint8_t *__restrict__ tile_tau, int kappa)
 {
   using V = typename AR::T;
   using F = typename AR::Factor;
@@ -541,11 +650,20 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     }
   }
   using ACC = TileAcc<AR>;
+  constexpr bool FX = std::is_same<AR, FixedArith>::value;
+  static_assert(FX || SC == 0, "dyadic scaling is a fixed-point form");
   F *fac = reinterpret_cast<F *>(smem);
+  uint32_t *fsh = reinterpret_cast<uint32_t *>(smem);     // SC != 0: per-level shift words
   const int Us = U + TL_SINKS;                            // the tile's nodes, then the sinks
-  V *xs = reinterpret_cast<V *>(fac + n_fac);
+  const int fac_bytes = SC ? ((n_fac * 4 + 15) & ~15) : n_fac * (int) sizeof(F);
+  V *xs = reinterpret_cast<V *>(smem + fac_bytes);
   uint32_t *ys = reinterpret_cast<uint32_t *>(xs + Us);  // ACC::WORDS words per entry
-  for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) fac[k] = AR::load_factor(fm, k);
+  // the tile's fixed-point unit: its coarsest leaf level (factor table row)
+  const int tau = FX ? (int) tile_tau[tile] : 0;
+  for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) {
+    if constexpr (SC != 0) fsh[k] = static_cast<const uint32_t *>(fm)[k];
+    else fac[k] = AR::load_factor(fm, tau * n_fac + k);
+  }
   tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, Us, xq, xs, ys);
   __shared__ uint32_t s_max;
   if (threadIdx.x == 0) s_max = 0u;
@@ -569,12 +687,19 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
             if (id >= 0) v[k] = __ldg(stvq + id);
           }
       }
-      // parent -> child-0 interpolation, axes in order
+      // parent -> child-0 interpolation: rank k takes the mean of the parent
+      // values on the subsets of k (fixed point: the exact sum, one shift)
+      if constexpr (FX) {
+        subset_sums<DIM, V>(v);
 #pragma unroll
-      for (int d = 0; d < DIM; d++)
+        for (int k = 1; k < NPE; k++) v[k] >>= __popc(k);
+      } else {
 #pragma unroll
-        for (int k = 0; k < NPE; k++)
-          if (!(k & (1 << d))) v[k | (1 << d)] = AR::half_sum(v[k], v[k | (1 << d)]);
+        for (int d = 0; d < DIM; d++)
+#pragma unroll
+          for (int k = 0; k < NPE; k++)
+            if (!(k & (1 << d))) v[k | (1 << d)] = AR::half_sum(v[k], v[k | (1 << d)]);
+      }
 #pragma unroll
       for (int k = 0; k < NPE; k++)
         if ((fmask >> k) & 1u) v[k] = xs[lidx(k)];
@@ -583,18 +708,41 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
       for (int k = 0; k < NPE; k++) v[k] = xs[lidx(k)];
     }
     wht<DIM, V>(v);
+    if constexpr (SC == 0) {
 #pragma unroll
-    for (int k = 0; k < NPE; k++) v[k] = AR::apply(v[k], fac[L * NPE + k]);
+      for (int k = 0; k < NPE; k++) v[k] = AR::apply(v[k], fac[L * NPE + k]);
+    } else {
+      // k = popcount of the mode; in the tile's unit (level tau):
+      //   both terms  (C1(k) w + (C2(k) w >> d_L)) >> (s_L - kappa tau)
+      //   one term    (C(k) w) >> (s_L - kappa tau)
+      // every shift below 32 (checked when the plan was set up)
+      const uint32_t sh = fsh[L];
+      const uint32_t sl = (sh & 0xFFu) - (uint32_t) (kappa * tau), dl = (sh >> 8) & 0xFFu;
+#pragma unroll
+      for (int k = 0; k < NPE; k++) {
+        long long t;
+        if constexpr (SC == 3) {
+          const long long m2 = sar_lt32(mul_small(v[k], dyc.c2[__popc(k)]), dl);
+          t = __popc(k) != 0 ? mul_small(v[k], dyc.c1[__popc(k)]) + m2 : m2;
+        } else if constexpr (SC == 1) {
+          t = __popc(k) != 0 ? mul_small(v[k], dyc.c1[__popc(k)]) : 0;
+        } else {
+          t = mul_small(v[k], dyc.c2[__popc(k)]);
+        }
+        v[k] = sar_lt32(t, sl);
+      }
+    }
     wht<DIM, V>(v);
     if constexpr (std::is_same<AR, FixedArith>::value) {
 #pragma unroll
       for (int k = 0; k < NPE; k++) ACC::add(ys, Us, lidx(k), v[k]);
       if (hang) {
-        // transpose of the child-0 interpolation on the unfilled ranks, into the parent nodes
+        // transpose of the child-0 interpolation on the unfilled ranks, into
+        // the parent nodes: parent rank j takes the sum over the supersets k
+        // of j of v[k] / 2^popcount(k)
 #pragma unroll
-        for (int k = 0; k < NPE; k++)
-          if ((fmask >> k) & 1u) v[k] = V(0);
-        transpose_child0<DIM, AR>(v);
+        for (int k = 0; k < NPE; k++) v[k] = ((fmask >> k) & 1u) ? V(0) : (v[k] >> __popc(k));
+        superset_sums<DIM, V>(v);
 #pragma unroll
         for (int k = 0; k < NPE; k++) {
           const uint32_t p = idx16<NPE>(pw, k);
@@ -643,41 +791,59 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const float down = ldexpf(1.0f, e - 23);
     tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
       const int a = reinterpret_cast<const int *>(ys)[u];
-      if (id & TL_EXCL) yq[id & ~TL_EXCL] = (V) a * down;
-      else if (a != 0) atomicAdd(yq + id, (V) a * down);
+      if (id & TL_EXCL) yq[id & TL_ID] = (V) a * down;
+      else if (a != 0) atomicAdd(yq + (id & TL_ID), (V) a * down);
     });
     return;
   }
   __syncthreads();
+  // the tile's sums from its unit (level tau) to each node's (level lam):
+  // a factor 2^(kappa (lam - tau)), lam >= tau for a node only this tile's
+  // finer leaves touch, lam < tau for one that coarser leaves elsewhere touch
+  const int ktau = kappa * tau;
   tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
-    const V a = ACC::get(ys, Us, u);
-    if (id & TL_EXCL) yq[id & ~TL_EXCL] = a;
-    else if (a != V(0)) AR::add(yq + id, a);
+    V a = ACC::get(ys, Us, u);
+    if constexpr (FX) {
+      if (kappa > 0) {
+        const int d = kappa * (int) ((id >> TL_LAM) & 15u) - ktau;
+        a = d >= 0 ? (V) ((unsigned long long) a << d) : (a >> -d);
+      }
+    }
+    if (id & TL_EXCL) yq[id & TL_ID] = a;
+    else if (a != V(0)) AR::add(yq + (id & TL_ID), a);
   });
 }
 
-template <int DIM, int TL, typename AR>
+template <int DIM, int TL, typename AR, int SC>
 static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y,
                          const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
                          cudaStream_t s)
 {
-  auto kfn = k_matvec_q1t<DIM, TL, AR>;
-  const int n_fac = (pl.md + 1) * (1 << DIM);
-  const size_t smem = (size_t) n_fac * sizeof(typename AR::Factor) + (size_t) 2 * (pl.tl_umax + TL_SINKS) * sizeof(typename AR::T);
+  auto kfn = k_matvec_q1t<DIM, TL, AR, SC>;
+  DyConst dyc{};
+  for (int k = 0; k <= DIM; k++) {
+    dyc.c1[k] = (uint32_t) dy_c1(DIM, k);
+    dyc.c2[k] = (uint32_t) dy_c2(DIM, k);
+  }
+  // one row of the per-unit factor table, or the per-level shift words
+  const int n_fac = SC ? pl.md + 1 : (pl.md + 1) * (1 << DIM);
+  const size_t fac_bytes = SC ? (size_t) ((n_fac * 4 + 15) & ~15) : (size_t) n_fac * sizeof(typename AR::Factor);
+  const size_t smem = fac_bytes + (size_t) 2 * (pl.tl_umax + TL_SINKS) * sizeof(typename AR::T);
   ensure_dyn_smem(kfn, smem);
   kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
                                            pl.tl_lstart.p, pl.tl_nodes.p, fm, n_fac, x, y, hzoff, hztab, stv,
                                            pl.conforming ? 1 : 0, skip_stale ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p,
-                                           pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride);
+                                           pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride, dyc, pl.tl_tau.p,
+                                           std::is_same<AR, FixedArith>::value ? pl.fx_kappa : 0);
 }
 
-template <typename AR>
+template <typename AR, int SC>
 static void launch_tiled_dim(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y,
                              const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
                              cudaStream_t s)
 {
 #define DKT_TL_CASE(D, TL) \
-  case (D) * 10000 + (TL): launch_tiled<D, TL, AR>(pl, fm, x, y, hzoff, hztab, stv, skip_stale, s); break;
+  case (D) * 10000 + (TL): launch_tiled<D, TL, AR, SC>(pl, fm, x, y, hzoff, hztab, stv, skip_stale, s); break;
   switch (pl.dim * 10000 + pl.tl_T) {
     DKT_TL_CASE(2, 128) DKT_TL_CASE(2, 256) DKT_TL_CASE(2, 512)
     DKT_TL_CASE(3, 128) DKT_TL_CASE(3, 256) DKT_TL_CASE(3, 512)
@@ -693,14 +859,19 @@ static void launch_tiled_dim(Plan &pl, const void *fm, const typename AR::T *x, 
 // leaves that remain read no stale slot, so they need no look-up of one.
 void tiled_fixed(Plan &pl, bool skip_stale, cudaStream_t s)
 {
-  launch_tiled_dim<FixedArith>(pl, pl.fx_fm.p, pl.xq.p, pl.yq.p,
-                               (pl.st_ready && !skip_stale) ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p,
-                               skip_stale, s);
+  const int32_t *hz = (pl.st_ready && !skip_stale) ? pl.st_hzoff.p : nullptr;
+  switch (pl.fx_scale) {
+#define DKT_SC_CASE(SC, FM) \
+  case SC: launch_tiled_dim<FixedArith, SC>(pl, FM, pl.xq.p, pl.yq.p, hz, pl.st_hztab.p, pl.st_vq.p, skip_stale, s); break;
+    DKT_SC_CASE(0, pl.fx_fm.p) DKT_SC_CASE(1, pl.fx_shift.p) DKT_SC_CASE(2, pl.fx_shift.p) DKT_SC_CASE(3, pl.fx_shift.p)
+#undef DKT_SC_CASE
+    default: throw std::runtime_error("bad fixed-point scaling mode");
+  }
 }
 
 void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
 {
-  launch_tiled_dim<F32Arith>(pl, pl.f32_f.p, x, y, nullptr, nullptr, nullptr, false, s);
+  launch_tiled_dim<F32Arith, 0>(pl, pl.f32_f.p, x, y, nullptr, nullptr, nullptr, false, s);
 }
 
 bool tile_size_supported(int dim, int T)

@@ -365,12 +365,14 @@ def test_conforming_traversal_vs_oracle(dkt, order):
 
 
 @pytest.mark.parametrize("dim", [2, 3, 4])
-def test_tiled_kernel_bitwise_equals_untiled(dkt, dim):
+def test_tiled_kernel_equals_untiled(dkt, dim):
     """The tiled Q1 kernel (every supported tile size) agrees with the
-    per-leaf kernel to a few fixed-point units (it evaluates hanging leaves
-    reflected to child 0, which can move single roundings of the mode
-    scaling by one unit), stale parent reads included; every tile size
-    gives bitwise the same product."""
+    per-leaf kernel to a few fixed-point units, stale parent reads included:
+    the two order their roundings differently (the per-leaf kernel evaluates
+    each leaf in its own level's fixed-point unit and the tiled kernel in its
+    tile's coarsest level's, and the tiled kernel evaluates hanging leaves
+    reflected to child 0).  Each tile size gives bitwise the same product on
+    every run."""
     if dim == 4:
         md = 10
         tc, tl = dkt.moving_ball_tree(max_depth=md, level=5)
@@ -384,14 +386,11 @@ def test_tiled_kernel_bitwise_equals_untiled(dkt, dim):
     x = dkt.uniform_pm1(9, da.n)
     A.set_tile(0)
     y0 = _gpu_mv(A, x)
-    yt = None
     for T in sizes:
         A.set_tile(T)
         y = _gpu_mv(A, x)
         assert _rel(y, y0) <= 1e-13, T
-        if yt is None:
-            yt = y
-        assert np.array_equal(y, yt), T
+        assert np.array_equal(_gpu_mv(A, x), y), T
 
 
 def test_device_sphere_shell_equals_host(dkt):

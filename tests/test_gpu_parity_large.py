@@ -1,0 +1,98 @@
+"""Parity at the benchmarked sizes, through the C ABI.
+
+The moving-ball spacetime meshes of the benchmark (dim 4, max_depth 10,
+shell half-width 2^-L), Laplacian + mass, reference traversal with its
+static-parent-buffer reads:
+  * level 7, Q1 (6.9 M elements, 186,144 stale slot reads per product): the
+    device DA node list bit-exact against the oracle's, and the product of
+    the fixed-point tiled kernel and of the dense FP64 kernel within 1e-12
+    relative (2-norm) of the oracle's restatement of fem::matvec;
+  * level 6, Q2 (0.88 M elements, 278,400 stale slot reads): the
+    sum-factorised kernel within 1e-12 of the oracle;
+  * level 8, Q1 (54.7 M elements, the benchmark's own workload), too large
+    for the oracle to finish in a test: the fixed-point tiled product within
+    1e-12 of the dense FP64 kernel (itself pinned to the oracle above and to
+    the reference's goldens), and the product is linear (A(x + 2z) =
+    Ax + 2Az to 1e-12).
+The oracle runs on the host cores (about a minute and a half at level 7)."""
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+import oracle_port as orc
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+MD = 10
+
+
+@pytest.fixture(scope="module")
+def dkt():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return ge.load_package()
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _mesh(dkt, level, order):
+    tc, tl = dkt.moving_ball_tree(max_depth=MD, level=level, radius=0.2, halfwidth=2.0 ** -level, device=True)
+    return dkt.DA(tc, tl, 4, order=order, max_depth=MD)
+
+
+def _product(A, x, arith):
+    import torch
+    A.set_arithmetic(arith)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    A.matvec(xd, yd)
+    torch.cuda.synchronize()
+    return yd.cpu().numpy()
+
+
+def _oracle(da, order):
+    orc.set_curve(4, MD)
+    orc.set_conforming(0)
+    orc.set_stale_mode(0)
+    sc, sl = da.tree()
+    return orc.DA(sc, sl, 4, order, 2)
+
+
+@pytest.mark.parametrize("level,order", [(7, 1), (6, 2)], ids=["q1_level7", "q2_level6"])
+def test_moving_ball_product_vs_oracle(dkt, level, order):
+    da = _mesh(dkt, level, order)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    st = A.stats()
+    assert st["stale_slots"] > 0
+    ora = _oracle(da, order)
+    nc, nl = da.nodes()
+    assert np.array_equal(nc, ora.node_coords) and np.array_equal(nl, ora.node_levels)
+    assert np.array_equal(da.boundary_ids(), ora.bdry)
+    x = orc.uniform_pm1(2, da.n)
+    yo = ora.matvec(x)
+    assert ora.stats()["stale_reads"] == st["stale_slots"]
+    y_fast = _product(A, x, dkt.ARITH_AUTO)
+    print("level %d order %d: fast kernel vs oracle %.3e" % (level, order, _rel(y_fast, yo)))
+    assert _rel(y_fast, yo) <= TOL
+    if order == 1:
+        y_dense = _product(A, x, dkt.ARITH_FP64)
+        print("level %d: dense FP64 kernel vs oracle %.3e" % (level, _rel(y_dense, yo)))
+        assert _rel(y_dense, yo) <= TOL
+
+
+def test_level8_fixed_point_vs_dense_fp64_and_linearity(dkt):
+    da = _mesh(dkt, 8, 1)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    assert A.stats()["stale_slots"] > 0
+    x = orc.uniform_pm1(2, da.n)
+    z = orc.uniform_pm1(7, da.n)
+    y_fast = _product(A, x, dkt.ARITH_AUTO)
+    y_dense = _product(A, x, dkt.ARITH_FP64)
+    print("level 8: fixed point vs dense FP64 %.3e" % _rel(y_fast, y_dense))
+    assert _rel(y_fast, y_dense) <= TOL
+    y_z = _product(A, z, dkt.ARITH_AUTO)
+    y_sum = _product(A, x + 2.0 * z, dkt.ARITH_AUTO)
+    assert _rel(y_sum, y_fast + 2.0 * y_z) <= TOL
