@@ -362,7 +362,9 @@ def run_batch(a, dkt, dev):
         built = list(ex.map(plan, range(a.batch)))
     B = dkt.Matrix.batch([m for _, m in built])
     t_plan = time.perf_counter() - t0
-    tile, tile_ms = B.autotune()
+    # launch shape for the binary32 product of the mixed solve (the batched
+    # solves' inner operator): tile size and plain grid or persistent launch
+    tile, persist, tile_ms, cand_ms = B.autotune(arith=1)
     off = B.mesh_offsets()
     b = np.empty(B.n)
     for k, (da, _) in enumerate(built):
@@ -375,7 +377,11 @@ def run_batch(a, dkt, dev):
     out = {"workload": "%d 3D Q1 Poisson problems, element targets log-uniform in [1e3, %.0e], 1-4 Gaussian "
                        "clusters (sd 0.05) each; %d elements, %d nodes in one block-diagonal plan"
                        % (a.batch, a.batch_max_elements, n_elem, B.n),
-           "setup_s": {"meshes": t_mesh, "plans": t_plan}, "tile": tile, "tile_product_ms": tile_ms}
+           "setup_s": {"meshes": t_mesh, "plans": t_plan},
+           "launch": {"tile": tile, "persistent": persist, "binary32_product_ms": tile_ms,
+                      "candidates_ms": dict(zip(["untiled", "128", "128_persistent", "256", "256_persistent",
+                                                  "512", "512_persistent"], [float(t) for t in cand_ms])),
+                      "default_ms": float(cand_ms[3])}}
     stream = torch.cuda.current_stream(dev)
     for name, prec, arith in (("fp64_native", dkt.PREC_FP64, dkt.ARITH_FP64), ("fp64", dkt.PREC_FP64, dkt.ARITH_AUTO),
                               ("mixed", dkt.PREC_MIXED, dkt.ARITH_AUTO)):

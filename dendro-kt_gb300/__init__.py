@@ -82,6 +82,7 @@ def load(build_if_missing=True):
         "dkt_plan_num_meshes": ([P, P], I),
         "dkt_plan_mesh_offsets": ([P, P], I),
         "dkt_plan_autotune": ([P, P, P], I),
+        "dkt_plan_autotune_ex": ([P, I, P, P, P, P], I),
         "dkt_plan_stats_ex": ([P, P, I], I),
         "dkt_plan_set_arithmetic": ([P, I], I),
         "dkt_plan_destroy": ([P], None),
@@ -361,11 +362,15 @@ class Matrix:
         _check(load().dkt_plan_mesh_offsets(self._h, _p(o)))
         return o
 
-    def autotune(self):
-        """Keeps the fastest tile size; returns (tile, ms per product)."""
-        t, ms = ctypes.c_int(0), ctypes.c_double(0.0)
-        _check(load().dkt_plan_autotune(self._h, ctypes.byref(t), ctypes.byref(ms)))
-        return t.value, ms.value
+    def autotune(self, arith=0):
+        """Keeps the fastest launch shape for the FP64 (arith 0) or binary32
+        (arith 1) product; returns (tile, persistent, ms per product, times of
+        all candidates: untiled, then per tile size plain and persistent)."""
+        t, p, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+        times = np.zeros(7)
+        _check(load().dkt_plan_autotune_ex(self._h, int(arith), ctypes.byref(t), ctypes.byref(p), ctypes.byref(ms),
+                                           _p(times)))
+        return t.value, bool(p.value), ms.value, times
 
     def matvec_f32(self, x_dev, y_dev, stream=None):
         """Binary32 feMatrix product (Q1 built-in operators)."""

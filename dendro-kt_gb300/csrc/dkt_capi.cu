@@ -37,7 +37,8 @@ void moving_ball_device(int md, int level, double R, double w, const double *c0,
 void unpack_cells_to_host(const DBuf<uint64_t> &keys, int64_t n, int dim, int md, uint32_t *coords, uint8_t *levels,
                           cudaStream_t s);
 void stale_setup(Plan &pl, const std::vector<double> &ip, cudaStream_t s);
-std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s);
+int fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s,
+                            std::string &err);
 int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter, double tol, bool jacobi,
               int *iters, int *refinements, double *relres, cudaStream_t user);
 void q1f32_apply(Plan &pl, const float *x, float *y, bool bc_in, bool bc_out, cudaStream_t s);
@@ -375,8 +376,10 @@ int dkt_fematrix_matvec_noalloc(dkt_plan plan, const double *x_dev, double *y_de
 {
   if (!plan || !x_dev || !y_dev) return fail(DKT_E_ARG, "null argument");
   try {
-    const std::string err = dkt::fematrix_matvec_noalloc(plan->pl, x_dev, y_dev, scale, (cudaStream_t) stream);
-    if (!err.empty()) return fail(err.find("exceed") != std::string::npos ? DKT_E_ARG : DKT_E_CUDA, err);
+    std::string err;
+    const int st = dkt::fematrix_matvec_noalloc(plan->pl, x_dev, y_dev, scale, (cudaStream_t) stream, err);
+    if (st == dkt::NOALLOC_TOO_LARGE) return fail(DKT_E_ARG, err);
+    if (st != dkt::NOALLOC_OK) return fail(DKT_E_CUDA, err);
   } catch (const std::exception &e) {
     return fail(DKT_E_CUDA, e.what());
   }
@@ -530,41 +533,89 @@ int dkt_plan_mesh_offsets(dkt_plan plan, int64_t *offsets)
   return DKT_OK;
 }
 
-int dkt_plan_autotune(dkt_plan plan, int *best_tile, double *best_ms)
+namespace {
+// x_i = uniform[-1,1) from a counter hash (the autotuner's input: every
+// product path, global atomics included, does its real work)
+__global__ void k_fill_pm1(double *__restrict__ x, float *__restrict__ x32, int64_t n)
 {
-  if (!plan) return fail(DKT_E_ARG, "null argument");
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t z = (uint64_t) i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  const double v = 2.0 * ((double) (z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+  x[i] = v;
+  x32[i] = (float) v;
+}
+}  // namespace
+
+int dkt_plan_autotune_ex(dkt_plan plan, int arith, int *best_tile, int *best_persist, double *best_ms,
+                         double *times)
+{
+  if (!plan || arith < 0 || arith > 1) return fail(DKT_E_ARG, "bad argument");
   if (!plan->pl.fx_ready) return fail(DKT_E_UNSUP, "tiles need a Q1 built-in operator");
+  if (arith == 1 && !plan->pl.f32_ready)
+    return fail(DKT_E_UNSUP, "binary32 product needs a plan without stale parent reads");
   return guarded([&]() {
     dkt::Plan &pl = plan->pl;
-    const int cand[4] = {0, pl.dim == 4 ? 64 : 128, pl.dim == 4 ? 128 : 256, pl.dim == 4 ? 256 : 512};
-    dkt::DBuf<double> x(pl.n_nodes), y(pl.n_nodes);
-    DKT_CUDA(cudaMemset(x.p, 0, pl.n_nodes * sizeof(double)));
+    const int sizes[3] = {pl.dim == 4 ? 64 : 128, pl.dim == 4 ? 128 : 256, pl.dim == 4 ? 256 : 512};
+    const int64_t n = pl.n_nodes;
+    dkt::DBuf<double> x(n), y(n);
+    dkt::DBuf<float> x32(n), y32(n);
+    k_fill_pm1<<<dkt::grid_for(n), 256>>>(x.p, x32.p, n);
+    dkt::check_launch("autotune_input");
     cudaEvent_t e0, e1;
     DKT_CUDA(cudaEventCreate(&e0));
     DKT_CUDA(cudaEventCreate(&e1));
-    int best = -1;
-    double bms = 1e300;
     const bool saved = pl.timing;
     pl.timing = false;
-    for (int T : cand) {
-      dkt::tile_setup(pl, T, 0);
-      dkt::fematrix_matvec(pl, x.p, y.p, 1.0, 0);
-      DKT_CUDA(cudaEventRecord(e0, 0));
-      for (int k = 0; k < 5; k++) dkt::fematrix_matvec(pl, x.p, y.p, 1.0, 0);
-      DKT_CUDA(cudaEventRecord(e1, 0));
-      DKT_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      DKT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms / 5 < bms) { bms = ms / 5; best = T; }
+    auto product = [&]() {
+      if (arith == 0) dkt::fematrix_matvec(pl, x.p, y.p, 1.0, 0);
+      else dkt::q1f32_apply(pl, x32.p, y32.p, false, true, 0);
+    };
+    // candidates: the untiled kernel, then per tile size the plain grid and
+    // the persistent launch (dims 2 and 3)
+    struct Cand { int T; bool persist; };
+    std::vector<Cand> cands{{0, false}};
+    for (int T : sizes) {
+      cands.push_back({T, false});
+      cands.push_back({T, true});
+    }
+    int best = 0;
+    double bms = 1e300;
+    for (size_t c = 0; c < cands.size(); c++) {
+      double ms_c = -1.0;
+      if (!(cands[c].persist && pl.dim > 3)) {
+        dkt::tile_setup(pl, cands[c].T, 0);
+        pl.tl_persist = cands[c].persist;
+        product();
+        DKT_CUDA(cudaEventRecord(e0, 0));
+        for (int k = 0; k < 5; k++) product();
+        DKT_CUDA(cudaEventRecord(e1, 0));
+        DKT_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        DKT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms_c = ms / 5;
+        if (ms_c < bms) { bms = ms_c; best = (int) c; }
+      }
+      if (times) times[c] = ms_c;
     }
     pl.timing = saved;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    dkt::tile_setup(pl, best, 0);
-    if (best_tile) *best_tile = best;
+    dkt::tile_setup(pl, cands[best].T, 0);
+    pl.tl_persist = cands[best].persist;
+    if (best_tile) *best_tile = cands[best].T;
+    if (best_persist) *best_persist = cands[best].persist ? 1 : 0;
     if (best_ms) *best_ms = bms;
     return DKT_OK;
   });
+}
+
+int dkt_plan_autotune(dkt_plan plan, int *best_tile, double *best_ms)
+{
+  return dkt_plan_autotune_ex(plan, 0, best_tile, nullptr, best_ms, nullptr);
 }
 
 int dkt_pcg_solve(dkt_plan plan, const double *b_dev, double *x_dev, int precision, int max_iter, double tol,

@@ -230,6 +230,10 @@ struct Plan {
   DBuf<uint32_t> tl_nodes, tl_fm;     // distinct nodes (| exclusive flag); reflected fill masks
   DBuf<uint16_t> tl_e2l, tl_p2l;
   DBuf<uint8_t> tl_tau;              // per tile: coarsest leaf level (its fixed-point unit)
+  // persistent tiled launch (CTAs pull tiles from a counter) instead of one
+  // CTA per tile; chosen by dkt_plan_autotune
+  bool tl_persist = false;
+  DBuf<unsigned long long> tl_counter;
   // Optional CUDA-event timing of the leaf kernel on its launching stream.
   bool timing = false;
   std::vector<cudaEvent_t> ev;       // start/stop pairs of the current window

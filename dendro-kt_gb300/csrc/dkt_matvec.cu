@@ -7,6 +7,7 @@
 // and for hanging leaves zeroes the filled ranks, applies IKD_Child2Parent and
 // adds the result to the parent nodes whose rank is unfilled in the leaf mask
 // (matvec.h:482-522).
+#include <mutex>
 #include <string>
 #include "dkt_internal.cuh"
 
@@ -275,21 +276,24 @@ static __device__ __align__(256) double g_noalloc_xin[NOALLOC_MAX_NODES];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 static double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // device address of the array, per device
+static cudaError_t g_noalloc_err[NOALLOC_MAX_DEVICES];
+static std::once_flag g_noalloc_once[NOALLOC_MAX_DEVICES];
 
 // The array's name is only a host-side handle; its device address is looked
-// up once per device, with that device current.
+// up once per device, with that device current.  Host threads that make
+// their first call on a device at the same time wait for one lookup.
 static cudaError_t noalloc_scratch(double **out)
 {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-  if (!g_noalloc_ptr[dev]) {
+  std::call_once(g_noalloc_once[dev], [dev]() {
     void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_xin);
-    if (e != cudaSuccess) return e;
+    g_noalloc_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_xin);
     g_noalloc_ptr[dev] = static_cast<double *>(p);
-  }
+  });
+  if (g_noalloc_err[dev] != cudaSuccess) return g_noalloc_err[dev];
   *out = g_noalloc_ptr[dev];
   return cudaSuccess;
 }
@@ -315,15 +319,22 @@ static void launch_leaf_noalloc(const Plan &pl, const double *x, double *y, doub
   check_launch("matvec_leaf_noalloc");
 }
 
-// Returns an empty string on success, else the reason of the failure.
-std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s)
+// Returns NOALLOC_OK, NOALLOC_TOO_LARGE (a plan beyond the fixed scratch, or
+// an unsupported shape) or NOALLOC_CUDA, with the reason in err.
+int fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, double scale, cudaStream_t s,
+                            std::string &err)
 {
-  if (pl.n_nodes > NOALLOC_MAX_NODES)
-    return "dkt_fematrix_matvec_noalloc: " + std::to_string(pl.n_nodes) + " nodes exceed its fixed scratch of " +
-           std::to_string(NOALLOC_MAX_NODES) + " nodes";
+  if (pl.n_nodes > NOALLOC_MAX_NODES) {
+    err = "dkt_fematrix_matvec_noalloc: " + std::to_string(pl.n_nodes) + " nodes exceed its fixed scratch of " +
+          std::to_string(NOALLOC_MAX_NODES) + " nodes";
+    return NOALLOC_TOO_LARGE;
+  }
   double *scratch = nullptr;
   cudaError_t e = noalloc_scratch(&scratch);
-  if (e != cudaSuccess) return std::string("dkt_fematrix_matvec_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+  if (e != cudaSuccess) {
+    err = std::string("dkt_fematrix_matvec_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+    return NOALLOC_CUDA;
+  }
   const bool bc = op_has_bc(pl.op.kind);
   const double *xin = x;
   if (bc) {
@@ -346,14 +357,14 @@ std::string fematrix_matvec_noalloc(const Plan &pl, const double *x, double *y, 
       case 32: launch_leaf_noalloc<3, 2>(pl, xin, y, scale, s); break;
       case 41: launch_leaf_noalloc<4, 1>(pl, xin, y, scale, s); break;
       case 42: launch_leaf_noalloc<4, 2>(pl, xin, y, scale, s); break;
-      default: return "dkt_fematrix_matvec_noalloc: unsupported dim/order";
+      default: err = "dkt_fematrix_matvec_noalloc: unsupported dim/order"; return NOALLOC_TOO_LARGE;
     }
   }
   if (bc && pl.n_bdry > 0) {
     k_zero_at<<<grid_for(pl.n_bdry), 256, 0, s>>>(y, pl.bdry.p, pl.n_bdry);
     check_launch("noalloc_zero_out");
   }
-  return std::string();
+  return NOALLOC_OK;
 }
 
 }  // namespace dkt

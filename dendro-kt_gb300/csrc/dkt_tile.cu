@@ -458,21 +458,6 @@ __device__ __forceinline__ uint32_t idx16(const uint32_t (&w)[NPE / 2], int k)
   return (w[k >> 1] >> ((k & 1) * 16)) & 0xFFFFu;
 }
 
-// Transpose of the child-0 interpolation, axes in order (in place).
-template <int DIM, typename AR, typename V>
-__device__ __forceinline__ void transpose_child0(V *v)
-{
-#pragma unroll
-  for (int d = 0; d < DIM; d++)
-#pragma unroll
-    for (int k = 0; k < (1 << DIM); k++)
-      if (!(k & (1 << d))) {
-        const V hb = AR::half(v[k | (1 << d)]);
-        v[k] = v[k] + hb;
-        v[k | (1 << d)] = hb;
-      }
-}
-
 // The integer multiples of the dyadic scaling (6^dim D_L = C1(k) alpha_L +
 // C2(k) beta_L, k the popcount of the mode), passed as a kernel parameter:
 // their loads are constant-bank operands of the multiply-adds.
@@ -609,22 +594,23 @@ __device__ __forceinline__ void tile_scatter(const uint32_t *__restrict__ tile_n
 // tile's unit (fm: the per-unit factor table); 1, 2, 3 = dyadic scaling with
 // the Laplacian term (bit 0) and / or the mass term (bit 1), fm then pointing
 // at the per-level shift words.
+// One tile (one CTA's work); uniform exits only.
 template <int DIM, int T_LEAVES, typename AR, int SC>
-__global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
+__device__ __forceinline__ void q1t_tile(
+    const int64_t tile,
     const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
     const int64_t *__restrict__ tile_hb, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
     const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
     int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
     int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
-    const int *__restrict__ skip_mesh, int skip_stride, const __grid_constant__ DyConst dyc,
+    const int *__restrict__ skip_mesh, int skip_stride, const DyConst &dyc,
     const uint8_t *__restrict__ tile_tau, int kappa)
 {
   using V = typename AR::T;
   using F = typename AR::Factor;
   constexpr int NPE = 1 << DIM;
   extern __shared__ __align__(16) unsigned char smem[];
-  const int64_t tile = blockIdx.x;
   // a batched solve: tiles whose meshes have all converged are not needed
   if (skip_mesh && skip_mesh[(int64_t) tile_mlo[tile] * skip_stride] &&
       skip_mesh[(int64_t) tile_mhi[tile] * skip_stride])
@@ -688,17 +674,12 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
           }
       }
       // parent -> child-0 interpolation: rank k takes the mean of the parent
-      // values on the subsets of k (fixed point: the exact sum, one shift)
-      if constexpr (FX) {
-        subset_sums<DIM, V>(v);
+      // values on the subsets of k (the sum, then one shift or scaling)
+      subset_sums<DIM, V>(v);
 #pragma unroll
-        for (int k = 1; k < NPE; k++) v[k] >>= __popc(k);
-      } else {
-#pragma unroll
-        for (int d = 0; d < DIM; d++)
-#pragma unroll
-          for (int k = 0; k < NPE; k++)
-            if (!(k & (1 << d))) v[k | (1 << d)] = AR::half_sum(v[k], v[k | (1 << d)]);
+      for (int k = 1; k < NPE; k++) {
+        if constexpr (FX) v[k] >>= __popc(k);
+        else v[k] *= 1.0f / (float) (1 << __popc(k));
       }
 #pragma unroll
       for (int k = 0; k < NPE; k++)
@@ -751,14 +732,18 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
       }
     } else {
 #pragma unroll
-      for (int k = 0; k < NPE; k++) zt[k] = ((fmask >> k) & 1u) || !hang ? V(0) : v[k];
-      if (hang) transpose_child0<DIM, AR>(zt);
+      for (int k = 0; k < NPE; k++)
+        zt[k] = ((fmask >> k) & 1u) || !hang ? V(0) : v[k] * (1.0f / (float) (1 << __popc(k)));
+      if (hang) superset_sums<DIM, V>(zt);
     }
   }
   if constexpr (!std::is_same<AR, FixedArith>::value) {
     // binary32: the tile's contributions are quantised against the tile's
-    // largest one (24 bits, a binary32 rounding) and summed with native
-    // integer shared atomics; each node's sum goes out with one float atomic
+    // largest one (22 bits) and summed with native integer shared atomics;
+    // each node's sum goes out with one float atomic.  The rounding to an
+    // integer is one fused multiply-add: v * up + 1.5 * 2^23 lands in
+    // [2^23, 2^24), where binary32 spacing is 1, for |v * up| < 2^22, and its
+    // bits less those of 1.5 * 2^23 are the rounded integer.
     float m = 0.0f;
     if (valid) {
 #pragma unroll
@@ -772,23 +757,24 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     __syncthreads();
     int e = 0;
     frexpf(__uint_as_float(s_max), &e);              // max < 2^e
-    const float up = ldexpf(1.0f, 23 - e);
+    const float up = ldexpf(1.0f, 22 - e);
+    auto quant = [up](float v) { return __float_as_int(fmaf(v, up, 12582912.0f)) - 0x4B400000; };
     if (valid) {
 #pragma unroll
       for (int k = 0; k < NPE; k++) {
-        atomicAdd(reinterpret_cast<int *>(ys) + idx16<NPE>(w, k), __float2int_rn(v[k] * up));
+        atomicAdd(reinterpret_cast<int *>(ys) + idx16<NPE>(w, k), quant(v[k]));
       }
       if (h >= 0) {
 #pragma unroll
         for (int k = 0; k < NPE; k++) {
           const uint32_t p = idx16<NPE>(pw, k);
           if (conforming || !((fmask >> k) & 1u))
-            atomicAdd(reinterpret_cast<int *>(ys) + p, __float2int_rn(zt[k] * up));
+            atomicAdd(reinterpret_cast<int *>(ys) + p, quant(zt[k]));
         }
       }
     }
     __syncthreads();
-    const float down = ldexpf(1.0f, e - 23);
+    const float down = ldexpf(1.0f, e - 22);
     tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
       const int a = reinterpret_cast<const int *>(ys)[u];
       if (id & TL_EXCL) yq[id & TL_ID] = (V) a * down;
@@ -814,12 +800,53 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
   });
 }
 
+// The tiled kernel.  PERSIST false: one CTA per tile (a plain grid of n_tile
+// CTAs).  PERSIST true: a persistent launch, a grid of as many CTAs as fit on
+// the device at once, each pulling the next tile from *counter (zero at
+// launch) until all n_tile are taken; in a batched solve the tiles whose
+// meshes have converged are passed over as they are pulled.
+template <int DIM, int T_LEAVES, typename AR, int SC, bool PERSIST>
+__global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
+    const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
+    const int64_t *__restrict__ tile_hb, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
+    const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
+    int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
+    const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
+    int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
+    const int *__restrict__ skip_mesh, int skip_stride, const __grid_constant__ DyConst dyc,
+    const uint8_t *__restrict__ tile_tau, int kappa, unsigned long long *__restrict__ counter, int64_t n_tile)
+{
+  if constexpr (!PERSIST) {
+    q1t_tile<DIM, T_LEAVES, AR, SC>(blockIdx.x, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm,
+                                    n_fac, xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi,
+                                    skip_mesh, skip_stride, dyc, tile_tau, kappa);
+    return;
+  } else {
+  __shared__ long long s_tile;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (long long) atomicAdd(counter, 1ull);
+    __syncthreads();
+    const int64_t t = s_tile;
+    __syncthreads();                 // every thread has read s_tile
+    if (t >= n_tile) return;
+    q1t_tile<DIM, T_LEAVES, AR, SC>(t, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm, n_fac,
+                                    xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi, skip_mesh,
+                                    skip_stride, dyc, tile_tau, kappa);
+    __syncthreads();                 // the tile's shared memory is free again
+  }
+  }
+}
+
 template <int DIM, int TL, typename AR, int SC>
 static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y,
                          const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
                          cudaStream_t s)
 {
-  auto kfn = k_matvec_q1t<DIM, TL, AR, SC>;
+  // the persistent form is compiled for dims 2 and 3 (the batched meshes);
+  // a 4D plan asking for it runs the plain grid
+  constexpr bool CAN_PERSIST = DIM <= 3;
+  const bool persist = CAN_PERSIST && pl.tl_persist;
+  auto kfn = persist ? k_matvec_q1t<DIM, TL, AR, SC, CAN_PERSIST> : k_matvec_q1t<DIM, TL, AR, SC, false>;
   DyConst dyc{};
   for (int k = 0; k <= DIM; k++) {
     dyc.c1[k] = (uint32_t) dy_c1(DIM, k);
@@ -830,11 +857,24 @@ static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, type
   const size_t fac_bytes = SC ? (size_t) ((n_fac * 4 + 15) & ~15) : (size_t) n_fac * sizeof(typename AR::Factor);
   const size_t smem = fac_bytes + (size_t) 2 * (pl.tl_umax + TL_SINKS) * sizeof(typename AR::T);
   ensure_dyn_smem(kfn, smem);
-  kfn<<<(unsigned) pl.tl_n, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
+  unsigned grid = (unsigned) pl.tl_n;
+  unsigned long long *counter = nullptr;
+  if (persist) {
+    int dev = 0, sms = 0, per_sm = 0;
+    DKT_CUDA(cudaGetDevice(&dev));
+    DKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DKT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, TL, smem));
+    grid = (unsigned) std::max<int64_t>(1, std::min<int64_t>(pl.tl_n, (int64_t) sms * std::max(per_sm, 1)));
+    if (pl.tl_counter.n < 1) pl.tl_counter.alloc(1);
+    counter = pl.tl_counter.p;
+    DKT_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
+  }
+  kfn<<<grid, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
                                            pl.tl_lstart.p, pl.tl_nodes.p, fm, n_fac, x, y, hzoff, hztab, stv,
                                            pl.conforming ? 1 : 0, skip_stale ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p,
                                            pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride, dyc, pl.tl_tau.p,
-                                           std::is_same<AR, FixedArith>::value ? pl.fx_kappa : 0);
+                                           std::is_same<AR, FixedArith>::value ? pl.fx_kappa : 0, counter,
+                                           pl.tl_n);
 }
 
 template <typename AR, int SC>

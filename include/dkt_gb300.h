@@ -159,7 +159,11 @@ int dkt_fematrix_matvec(dkt_plan plan, const double *x_dev, double *y_dev, doubl
  * array's device address (cudaGetSymbolAddress) with that device current;
  * make that first call before any stream capture.  All calls share the array:
  * calls whose work overlaps on the GPU (different streams, or different
- * threads) race on it and must be serialised by the caller. */
+ * threads) race on it and must be serialised by the caller.  A plan with
+ * static-parent-buffer reads (stale slots, see dkt_plan_stats_ex) also keeps
+ * the chain of those reads in buffers of its own, made when the plan was
+ * created, which every product on that plan rewrites: a call on a plan must
+ * not overlap any other product on the same plan either. */
 int dkt_fematrix_matvec_noalloc(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream);
 
 /* Same with host arrays: copies in, computes, copies out, synchronises. */
@@ -247,8 +251,17 @@ int dkt_batch_create(const dkt_plan *plans, int n, dkt_plan *out);
 int dkt_plan_num_meshes(dkt_plan plan, int *n);
 int dkt_plan_mesh_offsets(dkt_plan plan, int64_t *offsets);
 
-/* Times the feMatrix product with every supported tile size (and the
- * untiled kernel) on this plan and keeps the fastest. */
+/* Times the product on this plan (uniform[-1,1] input) for every launch
+ * shape and keeps the fastest: the untiled kernel, then for each supported
+ * tile size (leaves, i.e. elements, per CTA) the plain grid of one CTA per
+ * tile and the persistent launch whose CTAs pull tiles from a counter (dims 2
+ * and 3).  arith: 0 the FP64 feMatrix product, 1 the binary32 product of the
+ * mixed-precision solver.  times (may be NULL): 7 entries, ms per product of
+ * the candidates in that order (untiled; then per tile size, ascending, plain
+ * and persistent), -1 where not available.  No counterpart in the reference. */
+int dkt_plan_autotune_ex(dkt_plan plan, int arith, int *best_tile, int *best_persist, double *best_ms,
+                         double *times);
+/* The same for the FP64 product, without the per-candidate times. */
 int dkt_plan_autotune(dkt_plan plan, int *best_tile, double *best_ms);
 
 /* Binary32 feMatrix product y = A x with the Q1 or Q2 built-in operator of
