@@ -83,6 +83,7 @@ def load(build_if_missing=True):
         "dkt_plan_mesh_offsets": ([P, P], I),
         "dkt_plan_autotune": ([P, P, P], I),
         "dkt_plan_autotune_ex": ([P, I, P, P, P, P], I),
+        "dkt_plan_create_part": ([P, I64, I64, P, I64, P], I),
         "dkt_plan_stats_ex": ([P, P, I], I),
         "dkt_plan_set_arithmetic": ([P, I], I),
         "dkt_plan_destroy": ([P], None),
@@ -602,3 +603,6 @@ def uniform_pm1_coords(seed, coords):
         for d in range(c.shape[1]):
             h = splitmix64(h ^ c[:, d])
     return 2.0 * ((h >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)) - 1.0
+
+
+from . import partition  # noqa: E402  (multi-part meshes: partition maps and ghost exchange)

@@ -1,6 +1,9 @@
 // C ABI (include/dkt_gb300.h): argument checking, error codes, object
 // lifetimes, host<->device movement.  All compute runs in the kernels of
 // dkt_da.cu, dkt_plan.cu and dkt_matvec.cu.
+#include <algorithm>
+#include <climits>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -117,6 +120,22 @@ void setup_operator(dkt::Plan &pl, int op, const double *tables, cudaStream_t s)
   pl.opB.upload(pl.op.B.data(), pl.op.B.size(), s);
   pl.opAlpha.upload(pl.op.alpha.data(), pl.op.alpha.size(), s);
   pl.opBeta.upload(pl.op.beta.data(), pl.op.beta.size(), s);
+}
+
+// out[i] = in[i] >= 0 ? map[in[i]] : -1; a referenced node the map leaves
+// out (-1) raises *bad
+__global__ void k_remap_ids(const int32_t *__restrict__ in, int32_t *__restrict__ out, int64_t n,
+                            const int32_t *__restrict__ map, int *__restrict__ bad)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t v = in[i];
+  int32_t r = -1;
+  if (v >= 0) {
+    r = map[v];
+    if (r < 0) atomicExch(bad, 1);
+  }
+  out[i] = r;
 }
 
 std::vector<double> interp_tables(int p)
@@ -302,6 +321,71 @@ int dkt_plan_create_from_nodes(int dim, int order, int curve, int max_depth, con
     nl.upload(node_levels, (size_t) sz);
     return plan_common(dim, order, curve, max_depth, nx.p, nl.p, sz, nullptr, 0, op, op_tables, out);
   });
+}
+
+int dkt_plan_create_part(dkt_plan full, int64_t leaf_begin, int64_t leaf_end, const int32_t *node_map,
+                         int64_t n_local, dkt_plan *out)
+{
+  if (!full || !node_map || !out || n_local <= 0) return fail(DKT_E_ARG, "null argument or empty part");
+  const dkt::Plan &f = full->pl;
+  if (leaf_begin < 0 || leaf_end <= leaf_begin || leaf_end > f.n_leaf) return fail(DKT_E_ARG, "bad leaf range");
+  if (f.seg.size() >= 2) return fail(DKT_E_UNSUP, "a batch plan is not partitioned");
+  if (f.st_ready && f.st_n_runs > 0)
+    return fail(DKT_E_UNSUP, "a plan that reads stale parent-buffer slots is not partitioned (the buffer is one "
+                             "sequential chain over the whole traversal)");
+  dkt_plan_s *h = new dkt_plan_s();
+  const int rc = guarded([&]() {
+    dkt::Plan &pl = h->pl;
+    cudaStream_t s = 0;
+    const int64_t nl = leaf_end - leaf_begin, npe = f.npe;
+    // the part's hanging records: a contiguous range [h0, h1) of the plan's
+    std::vector<int32_t> hid((size_t) nl);
+    DKT_CUDA(cudaMemcpy(hid.data(), f.hidx.p + leaf_begin, nl * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    int64_t h0 = INT64_MAX, h1 = -1, nh = 0;
+    for (int32_t v : hid)
+      if (v >= 0) { h0 = std::min<int64_t>(h0, v); h1 = std::max<int64_t>(h1, v + 1); nh++; }
+    if (nh == 0) { h0 = 0; h1 = 0; }
+    if (h1 - h0 != nh) throw std::invalid_argument("the leaf range's hanging records are not contiguous");
+    for (int32_t &v : hid) if (v >= 0) v -= (int32_t) h0;
+    pl.dim = f.dim; pl.order = f.order; pl.md = f.md; pl.npe = f.npe; pl.conforming = f.conforming;
+    pl.n_nodes = n_local; pl.n_leaf = nl; pl.n_hang = nh; pl.n_bdry = 0;
+    pl.op = f.op;
+    pl.arith = f.arith;
+    if (f.opA.n) { pl.opA.alloc(f.opA.n); DKT_CUDA(cudaMemcpy(pl.opA.p, f.opA.p, f.opA.n * sizeof(double), cudaMemcpyDeviceToDevice)); }
+    if (f.opB.n) { pl.opB.alloc(f.opB.n); DKT_CUDA(cudaMemcpy(pl.opB.p, f.opB.p, f.opB.n * sizeof(double), cudaMemcpyDeviceToDevice)); }
+    if (f.opAlpha.n) { pl.opAlpha.alloc(f.opAlpha.n); DKT_CUDA(cudaMemcpy(pl.opAlpha.p, f.opAlpha.p, f.opAlpha.n * sizeof(double), cudaMemcpyDeviceToDevice)); }
+    if (f.opBeta.n) { pl.opBeta.alloc(f.opBeta.n); DKT_CUDA(cudaMemcpy(pl.opBeta.p, f.opBeta.p, f.opBeta.n * sizeof(double), cudaMemcpyDeviceToDevice)); }
+    if (f.opTable.n) { pl.opTable.alloc(f.opTable.n); DKT_CUDA(cudaMemcpy(pl.opTable.p, f.opTable.p, f.opTable.n * sizeof(double), cudaMemcpyDeviceToDevice)); }
+    if (f.ip.n) { pl.ip.alloc(f.ip.n); DKT_CUDA(cudaMemcpy(pl.ip.p, f.ip.p, f.ip.n * sizeof(double), cudaMemcpyDeviceToDevice)); }
+    dkt::DBuf<int32_t> map;
+    map.upload(node_map, (size_t) f.n_nodes, s);
+    dkt::DBuf<int> bad(1);
+    DKT_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+    pl.e2n.alloc((size_t) nl * npe);
+    k_remap_ids<<<dkt::grid_for(nl * npe), 256, 0, s>>>(f.e2n.p + leaf_begin * npe, pl.e2n.p, nl * npe, map.p, bad.p);
+    pl.info.alloc(nl);
+    DKT_CUDA(cudaMemcpyAsync(pl.info.p, f.info.p + leaf_begin, nl * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    pl.hidx.upload(hid.data(), hid.size(), s);
+    pl.p2n.alloc((size_t) std::max<int64_t>(nh, 1) * npe);
+    pl.fill.alloc((size_t) std::max<int64_t>(nh, 1) * 3);
+    if (nh) {
+      k_remap_ids<<<dkt::grid_for(nh * npe), 256, 0, s>>>(f.p2n.p + h0 * npe, pl.p2n.p, nh * npe, map.p, bad.p);
+      DKT_CUDA(cudaMemcpyAsync(pl.fill.p, f.fill.p + h0 * 3, nh * 3 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    }
+    dkt::check_launch("part_remap");
+    pl.bdry.alloc(1);
+    int hbad = 0;
+    DKT_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DKT_CUDA(cudaStreamSynchronize(s));
+    if (hbad) throw std::invalid_argument("node_map leaves out a node that the part's leaves touch");
+    if (dkt::q1fx_setup(pl, s)) dkt::tile_setup(pl, f.tl_ready ? f.tl_T : dkt::default_tile(pl.dim), s);
+    dkt::q2sf_setup(pl, s);
+    DKT_CUDA(cudaStreamSynchronize(s));
+    return DKT_OK;
+  });
+  if (rc != DKT_OK) { delete h; return rc; }
+  *out = h;
+  return DKT_OK;
 }
 
 int64_t dkt_plan_num_nodes(dkt_plan plan) { return plan ? plan->pl.n_nodes : -1; }

@@ -585,10 +585,16 @@ std::vector<Cell> sphere_shell_tree(int dim, int md, int level, double R, double
 
 // ---------------------------------------------------------------------------
 // VTU output of an octree: io::vtk::oct2vtu (IO/vtk/include/oct2vtk.h:272-273,
-// IO/vtk/src/oct2vtk.cpp:1530-1760).  One cell per octant with its own 2^dim
-// corner points (integer lattice coordinates, UInt32, z = 0 in 2D), VTK
-// hexahedra in 3D and quads in 2D, inline base64 "binary" data arrays with a
-// UInt32 byte-count header; optionally one Float64 value per cell.
+// IO/vtk/src/oct2vtk.cpp:1530-1800).  The reference's arrays, names and types:
+// one cell per octant with its own 2^dim corner points (integer lattice
+// coordinates, UInt32, x fastest, z = 0 in 2D), UInt64 connectivity and
+// offsets, UInt8 cell types (VTK hexahedra in 3D; quads in 2D, where the
+// reference has no instantiation), and the cell data mpi_rank and cell_level
+// (UInt32; rank 0: one process writes the whole tree); optionally one Float64
+// value per cell after them.  Inline base64 "binary" data arrays with a
+// UInt32 byte-count header (the reference's binary branch repeats the
+// connectivity block once per cell, oct2vtk.cpp:1670-1690, so its ASCII
+// branch is the one these arrays follow).
 // ---------------------------------------------------------------------------
 namespace {
 std::string base64(const std::vector<uint8_t> &in)
@@ -627,7 +633,8 @@ void write_vtu(const char *path, int dim, int md, const uint32_t *coords, const 
   if (n < 0 || (uint64_t) n * (1u << dim) > 0xFFFFFFFFull / 12) throw std::invalid_argument("too many cells for one VTU piece");
   const int nv = 1 << dim;
   std::vector<uint32_t> pts((size_t) n * nv * 3);
-  std::vector<int64_t> conn((size_t) n * nv), offs(n);
+  std::vector<uint64_t> conn((size_t) n * nv), offs(n);
+  std::vector<uint32_t> rank(n, 0u), lev(n);
   std::vector<uint8_t> types(n, (uint8_t) (dim == 3 ? 12 : 9));   // VTK_HEXAHEDRON, VTK_QUAD
   // corner order of the VTK cell types: counter-clockwise in each z-layer
   static const int ci[8] = {0, 1, 3, 2, 4, 5, 7, 6};
@@ -637,8 +644,9 @@ void write_vtu(const char *path, int dim, int md, const uint32_t *coords, const 
     for (int k = 0; k < nv; k++)
       for (int d = 0; d < 3; d++)
         pts[((size_t) e * nv + k) * 3 + d] = d < dim ? coords[e * dim + d] + (((k >> d) & 1) ? len : 0u) : 0u;
-    for (int k = 0; k < nv; k++) conn[(size_t) e * nv + k] = e * nv + ci[k];
-    offs[e] = (int64_t) (e + 1) * nv;
+    for (int k = 0; k < nv; k++) conn[(size_t) e * nv + k] = (uint64_t) (e * nv + ci[k]);
+    offs[e] = (uint64_t) (e + 1) * nv;
+    lev[e] = levels[e];
   }
   std::FILE *fp = std::fopen(path, "w");
   if (!fp) throw std::runtime_error(std::string("cannot open ") + path);
@@ -650,19 +658,27 @@ void write_vtu(const char *path, int dim, int md, const uint32_t *coords, const 
   std::fprintf(fp, "        <DataArray type=\"UInt32\" Name=\"Position\" NumberOfComponents=\"3\" format=\"binary\">\n");
   std::fprintf(fp, "          %s\n        </DataArray>\n      </Points>\n", vtu_block(pts).c_str());
   std::fprintf(fp, "      <Cells>\n");
-  std::fprintf(fp, "        <DataArray type=\"Int64\" Name=\"connectivity\" format=\"binary\">\n");
+  std::fprintf(fp, "        <DataArray type=\"UInt64\" Name=\"connectivity\" format=\"binary\">\n");
   std::fprintf(fp, "          %s\n        </DataArray>\n", vtu_block(conn).c_str());
-  std::fprintf(fp, "        <DataArray type=\"Int64\" Name=\"offsets\" format=\"binary\">\n");
+  std::fprintf(fp, "        <DataArray type=\"UInt64\" Name=\"offsets\" format=\"binary\">\n");
   std::fprintf(fp, "          %s\n        </DataArray>\n", vtu_block(offs).c_str());
   std::fprintf(fp, "        <DataArray type=\"UInt8\" Name=\"types\" format=\"binary\">\n");
   std::fprintf(fp, "          %s\n        </DataArray>\n      </Cells>\n", vtu_block(types).c_str());
+  if (cell_values)
+    std::fprintf(fp, "      <CellData Scalars=\"%s\">\n", cell_values_name ? cell_values_name : "value");
+  else
+    std::fprintf(fp, "      <CellData>\n");
+  std::fprintf(fp, "        <DataArray type=\"UInt32\" Name=\"mpi_rank\" format=\"binary\">\n");
+  std::fprintf(fp, "          %s\n        </DataArray>\n", vtu_block(rank).c_str());
+  std::fprintf(fp, "        <DataArray type=\"UInt32\" Name=\"cell_level\" format=\"binary\">\n");
+  std::fprintf(fp, "          %s\n        </DataArray>\n", vtu_block(lev).c_str());
   if (cell_values) {
     std::vector<double> cv(cell_values, cell_values + n);
-    std::fprintf(fp, "      <CellData Scalars=\"%s\">\n", cell_values_name ? cell_values_name : "value");
     std::fprintf(fp, "        <DataArray type=\"Float64\" Name=\"%s\" format=\"binary\">\n",
                  cell_values_name ? cell_values_name : "value");
-    std::fprintf(fp, "          %s\n        </DataArray>\n      </CellData>\n", vtu_block(cv).c_str());
+    std::fprintf(fp, "          %s\n        </DataArray>\n", vtu_block(cv).c_str());
   }
+  std::fprintf(fp, "      </CellData>\n");
   std::fprintf(fp, "    </Piece>\n  </UnstructuredGrid>\n</VTKFile>\n");
   const bool bad = std::ferror(fp) != 0;
   std::fclose(fp);

@@ -166,6 +166,19 @@ int dkt_fematrix_matvec(dkt_plan plan, const double *x_dev, double *y_dev, doubl
  * not overlap any other product on the same plan either. */
 int dkt_fematrix_matvec_noalloc(dkt_plan plan, const double *x_dev, double *y_dev, double scale, void *stream);
 
+/* One part of a partitioned mesh (the rank-local plan of a multi-rank ot::DA,
+ * src/oda.cpp:52-151 with SFC_NodeSort::dist_countCGNodes,
+ * include/nsort.tcc:492-803): the leaves [leaf_begin, leaf_end) of `full`'s
+ * flattened traversal, their node indices renumbered by node_map (host
+ * array of full's node count: the part's local index of every node its
+ * leaves touch, -1 elsewhere; n_local local nodes, ghosts included).  Its
+ * dkt_matvec is the part's share of fem::matvec (include/matvec.h:231-548) on
+ * the part's ghosted layout; the partition, ownership and ghost exchange
+ * around it are the host's (dendro-kt_gb300/partition.py).  Plans that read
+ * stale parent-buffer slots and batch plans are refused (DKT_E_UNSUP). */
+int dkt_plan_create_part(dkt_plan full, int64_t leaf_begin, int64_t leaf_end, const int32_t *node_map,
+                         int64_t n_local, dkt_plan *out);
+
 /* Same with host arrays: copies in, computes, copies out, synchronises. */
 int dkt_fematrix_matvec_host(dkt_plan plan, const double *x_host, double *y_host, double scale);
 

@@ -79,11 +79,13 @@ int dkt_mesh_sphere_shell_device(int dim, int max_depth, int level, double radiu
                                  const double *centre, int64_t *n_out, uint32_t **coords, uint8_t **levels);
 
 /* io::vtk::oct2vtu (IO/vtk/include/oct2vtk.h:272-273): the tree as a VTK XML
- * unstructured grid, one hexahedron (3D) or quad (2D) per cell with its own
- * corner points in integer lattice coordinates (UInt32, 0..2^max_depth),
- * inline base64 binary arrays.  cell_values (one double per cell, named
- * cell_values_name) may be NULL.  dim 2 or 3, as the reference (VTK has no 4D
- * cells; DKT_E_ARG for other dims). */
+ * unstructured grid with the reference's arrays: one hexahedron (3D) or quad
+ * (2D) per cell with its own corner points in integer lattice coordinates
+ * (Position, UInt32, 0..2^max_depth), UInt64 connectivity and offsets, UInt8
+ * types, and the cell data mpi_rank (0) and cell_level (UInt32), as inline
+ * base64 binary arrays.  cell_values (one double per cell, named
+ * cell_values_name) may be NULL.  The reference instantiates dim 3 only;
+ * dim 2 here as quads; DKT_E_ARG for other dims (VTK has no 4D cells). */
 int dkt_write_vtu(const char *path, int dim, int max_depth, const uint32_t *coords, const uint8_t *levels,
                   int64_t n_cells, const double *cell_values, const char *cell_values_name);
 

@@ -19,6 +19,9 @@
 //             mass right-hand side with boundary zeroing; a 3D operator
 //   * the raw fem::matvec output (FEM/include/matvec.h:231-240), no pre/post
 //   * the RefElement 1D matrices (FEM/src/refel.cpp:75-220)
+//   * op 8 (dim 3): io::vtk::oct2vtu (IO/vtk/src/oct2vtk.cpp:1570-1760) of the
+//     tree in SFC order, written beside the output file as <out>_vtu_0_1.vtu;
+//     the matVec outputs are the identity's (as op 0)
 //   * op 7: HeatEq::HeatMat<dim>::cgSolve (FEM/examples/src/heatMat.cpp:164-325)
 //     from x = 0 on b = the HeatVec<dim> right-hand side of the input vector
 //     (feVector::computeVec, as FEM/examples/src/heatEq.cpp:112-118 builds
@@ -37,6 +40,7 @@
 #include "refel.h"
 #include "heatMat.h"
 #include "heatVec.h"
+#include "oct2vtk.h"
 
 #include <chrono>
 #include <iostream>
@@ -184,13 +188,25 @@ void test_fields(const double *x, double *out, unsigned dim)
   out[1] = 1.0 / s1;
 }
 
+// io::vtk::oct2vtu is defined for dim 3 only (IO/vtk/src/oct2vtk.cpp:1892)
+template <unsigned int dim>
+void write_oct_vtu(const std::vector<ot::TreeNode<unsigned int, dim>> &, const char *)
+{
+}
+template <>
+void write_oct_vtu<3>(const std::vector<ot::TreeNode<unsigned int, 3>> &tree, const char *prefix)
+{
+  io::vtk::oct2vtu<unsigned int, 3>(tree.data(), (unsigned int) tree.size(), prefix, MPI_COMM_WORLD);
+}
+
 double now_s()
 {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
 template <unsigned int dim>
-int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind, int nCalls, uint64_t seed)
+int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind, int nCalls, uint64_t seed,
+        const char *outPath)
 {
   using TN = ot::TreeNode<unsigned int, dim>;
   m_uiMaxDepth = maxDepth;
@@ -263,7 +279,7 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
   heat.setProblemDimensions(pmin, pmax);
   lm.setProblemDimensions(pmin, pmax);
   hv.setProblemDimensions(pmin, pmax);
-  if (op == 0) mv = [&](const double *a, double *b) { idm.matVec(a, b, 1.0); };
+  if (op == 0 || op == 8) mv = [&](const double *a, double *b) { idm.matVec(a, b, 1.0); };
   else if (op == 1 || op == 7) mv = [&](const double *a, double *b) { heat.matVec(a, b, 1.0); };
   else if (op == 6) mv = [&](const double *a, double *b) { hv.computeVec(a, b, 1.0); };
   else mv = [&](const double *a, double *b) { lm.matVec(a, b, 1.0); };
@@ -283,7 +299,7 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
     std::copy(x.begin(), x.end(), xg.begin() + da->getLocalNodeBegin());
     using namespace std::placeholders;
     fem::EleOpT<double> eop;
-    if (op == 0) eop = std::bind(&IdentityMat<dim>::elementalMatVec, &idm, _1, _2, _3, _4);
+    if (op == 0 || op == 8) eop = std::bind(&IdentityMat<dim>::elementalMatVec, &idm, _1, _2, _3, _4);
     else if (op == 1 || op == 7) eop = std::bind(&HeatEq::HeatMat<dim>::elementalMatVec, &heat, _1, _2, _3, _4);
     else if (op == 6) eop = std::bind(&HeatEq::HeatVec<dim>::elementalComputeVec, &hv, _1, _2, _3, _4);
     else eop = std::bind(&LapMassMat<dim>::elementalMatVec, &lm, _1, _2, _3, _4);
@@ -312,6 +328,7 @@ int run(Reader &in, Writer &out, int maxDepth, int order, int op, int inputKind,
   out.arr(re->getQ1d(), M * M);
   out.arr(re->getDg1d(), M * M);
   out.arr(re->getWgq(), M);
+  if (op == 8) write_oct_vtu<dim>(tree, (std::string(outPath) + "_vtu").c_str());
   if (op == 7) {
     // b = HeatVec right-hand side of x; x0 = 0; cgSolve writes its final
     // relative L-infinity residual into tol and prints the iteration at
@@ -359,9 +376,9 @@ int main(int argc, char **argv)
   const int op = in.get<int32_t>(), inputKind = in.get<int32_t>(), nCalls = in.get<int32_t>();
   const uint64_t seed = in.get<uint64_t>();
   int rc = 1;
-  if (dim == 2) rc = run<2>(in, out, maxDepth, order, op, inputKind, nCalls, seed);
-  else if (dim == 3) rc = run<3>(in, out, maxDepth, order, op, inputKind, nCalls, seed);
-  else if (dim == 4) rc = run<4>(in, out, maxDepth, order, op, inputKind, nCalls, seed);
+  if (dim == 2) rc = run<2>(in, out, maxDepth, order, op, inputKind, nCalls, seed, argv[2]);
+  else if (dim == 3) rc = run<3>(in, out, maxDepth, order, op, inputKind, nCalls, seed, argv[2]);
+  else if (dim == 4) rc = run<4>(in, out, maxDepth, order, op, inputKind, nCalls, seed, argv[2]);
   fclose(fi);
   fclose(fo);
   MPI_Finalize();

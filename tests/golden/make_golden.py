@@ -8,7 +8,8 @@ set of small meshes, the reference's own outputs:
   and the RefElement 1D operators; for the driver's op 7 also
   HeatMat<3>::cgSolve from x = 0 on the HeatVec<3> right-hand side of x
   (status, final relative L-infinity residual, iterations, right-hand side,
-  solution).
+  solution); and, under vtu/, io::vtk::oct2vtu of one 3D tree per curve
+  (the driver's op 8: the tree and the written file's arrays).
 Usage:  python tests/golden/make_golden.py [name-substring ...]
         (with arguments, only the fixtures whose names contain one of them)
 """
@@ -82,8 +83,32 @@ def cases():
     return out
 
 
+def vtu_arrays_ascii(path):
+    """The data arrays of an ASCII VTU file (the reference's oct2vtu built
+    with DENDRO_VTU_ASCII), by name."""
+    import xml.etree.ElementTree as ET
+    types = {"UInt32": np.uint32, "UInt64": np.uint64, "UInt8": np.uint8}
+    return {da.get("Name"): np.array(da.text.split(), dtype=types[da.get("type")])
+            for da in ET.parse(path).getroot().iter("DataArray")}
+
+
+def vtu_goldens():
+    """io::vtk::oct2vtu (the driver's op 8) of the Gaussian 300-point 3D tree
+    in both curve orders: the tree as written, and the file's arrays."""
+    os.makedirs(os.path.join(HERE, "vtu"), exist_ok=True)
+    pts = trees.gaussian_points(300, 3, 8, seed=0)
+    for curve in ("morton", "hilbert"):
+        r = run_ref(curve, 3, 8, 1, 8, pts, None, 0, seed=1)
+        a = vtu_arrays_ascii(os.path.join("/tmp", "dkt_golden_out.bin_vtu_0_1.vtu"))
+        np.savez_compressed(os.path.join(HERE, "vtu", f"{curve}_d3_gauss300.npz"), curve=curve, dim=3, md=8,
+                            tree_coords=r["tree_coords"], tree_levels=r["tree_levels"], **a)
+        print("vtu", curve, r["tree_levels"].size, sorted(a))
+
+
 def main(only=()):
     build_ref()
+    if not only or "vtu" in only:
+        vtu_goldens()
     for name, curve, dim, md, order, op, (src, arg) in cases():
         if only and not any(o in name for o in only):
             continue

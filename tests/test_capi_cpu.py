@@ -109,7 +109,7 @@ def test_moving_ball_is_complete(dkt):
 def _vtu_arrays(path):
     import base64
     import xml.etree.ElementTree as ET
-    types = {"UInt32": np.uint32, "Int64": np.int64, "UInt8": np.uint8, "Float64": np.float64}
+    types = {"UInt32": np.uint32, "UInt64": np.uint64, "UInt8": np.uint8, "Float64": np.float64}
     out = {}
     for da in ET.parse(path).getroot().iter("DataArray"):
         raw = base64.b64decode(da.text.strip())
@@ -136,6 +136,8 @@ def test_write_vtu_roundtrip(dkt, tmp_path, dim):
     assert np.array_equal(a["offsets"], nv * np.arange(1, len(l) + 1))
     assert np.all(a["types"] == (12 if dim == 3 else 9))
     assert np.array_equal(a["level"], l.astype(np.float64))
+    assert np.array_equal(a["cell_level"], l.astype(np.uint32))
+    assert np.all(a["mpi_rank"] == 0)
     lens = (1 << (md - l.astype(np.int64)))
     first = P[conn[:, 0]][:, :dim].astype(np.int64)
     assert np.array_equal(first, c.astype(np.int64))
@@ -147,6 +149,20 @@ def test_write_vtu_roundtrip(dkt, tmp_path, dim):
         assert np.array_equal(P[conn[:, 4]][:, 2].astype(np.int64) - first[:, 2], lens)
     else:
         assert np.all(P[:, 2] == 0)
+
+
+@pytest.mark.parametrize("curve", ["morton", "hilbert"])
+def test_write_vtu_matches_reference_oct2vtu(dkt, tmp_path, curve):
+    """The reference's io::vtk::oct2vtu, run on the same tree in the same
+    order (tests/golden/vtu, from its ASCII build): every data array equal."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "vtu", f"{curve}_d3_gauss300.npz"))
+    path = str(tmp_path / "tree.vtu")
+    dkt.write_vtu(path, g["tree_coords"], g["tree_levels"], 3, int(g["md"]))
+    a = _vtu_arrays(path)
+    assert sorted(a) == sorted(["Position", "connectivity", "offsets", "types", "mpi_rank", "cell_level"])
+    for name in a:
+        assert a[name].dtype == g[name].dtype, name
+        assert np.array_equal(a[name], g[name]), name
 
 
 def test_write_vtu_rejects_4d(dkt, tmp_path):
