@@ -137,6 +137,25 @@ __global__ void k_remap_ids(const int32_t *__restrict__ in, int32_t *__restrict_
   }
   out[i] = r;
 }
+// rows[k] of in (width w) to row k of out, node ids through map when given
+template <typename T>
+__global__ void k_gather_rows(const T *__restrict__ in, T *__restrict__ out, const int32_t *__restrict__ rows,
+                              int64_t n_rows, int w, const int32_t *__restrict__ map, int *__restrict__ bad)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_rows * w) return;
+  T v = in[(int64_t) rows[i / w] * w + i % w];
+  if (map) {
+    const int32_t id = (int32_t) v;
+    int32_t r = -1;
+    if (id >= 0) {
+      r = map[id];
+      if (r < 0) atomicExch(bad, 1);
+    }
+    v = (T) r;
+  }
+  out[i] = v;
+}
 
 std::vector<double> interp_tables(int p)
 {
@@ -338,15 +357,15 @@ int dkt_plan_create_part(dkt_plan full, int64_t leaf_begin, int64_t leaf_end, co
     dkt::Plan &pl = h->pl;
     cudaStream_t s = 0;
     const int64_t nl = leaf_end - leaf_begin, npe = f.npe;
-    // the part's hanging records: a contiguous range [h0, h1) of the plan's
-    std::vector<int32_t> hid((size_t) nl);
+    // the part's hanging records, in the order of its leaves
+    std::vector<int32_t> hid((size_t) nl), hrows;
     DKT_CUDA(cudaMemcpy(hid.data(), f.hidx.p + leaf_begin, nl * sizeof(int32_t), cudaMemcpyDeviceToHost));
-    int64_t h0 = INT64_MAX, h1 = -1, nh = 0;
-    for (int32_t v : hid)
-      if (v >= 0) { h0 = std::min<int64_t>(h0, v); h1 = std::max<int64_t>(h1, v + 1); nh++; }
-    if (nh == 0) { h0 = 0; h1 = 0; }
-    if (h1 - h0 != nh) throw std::invalid_argument("the leaf range's hanging records are not contiguous");
-    for (int32_t &v : hid) if (v >= 0) v -= (int32_t) h0;
+    for (int32_t &v : hid)
+      if (v >= 0) {
+        hrows.push_back(v);
+        v = (int32_t) hrows.size() - 1;
+      }
+    const int64_t nh = (int64_t) hrows.size();
     pl.dim = f.dim; pl.order = f.order; pl.md = f.md; pl.npe = f.npe; pl.conforming = f.conforming;
     pl.n_nodes = n_local; pl.n_leaf = nl; pl.n_hang = nh; pl.n_bdry = 0;
     pl.op = f.op;
@@ -368,9 +387,13 @@ int dkt_plan_create_part(dkt_plan full, int64_t leaf_begin, int64_t leaf_end, co
     pl.hidx.upload(hid.data(), hid.size(), s);
     pl.p2n.alloc((size_t) std::max<int64_t>(nh, 1) * npe);
     pl.fill.alloc((size_t) std::max<int64_t>(nh, 1) * 3);
+    dkt::DBuf<int32_t> rows;
     if (nh) {
-      k_remap_ids<<<dkt::grid_for(nh * npe), 256, 0, s>>>(f.p2n.p + h0 * npe, pl.p2n.p, nh * npe, map.p, bad.p);
-      DKT_CUDA(cudaMemcpyAsync(pl.fill.p, f.fill.p + h0 * 3, nh * 3 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+      rows.upload(hrows.data(), hrows.size(), s);
+      k_gather_rows<int32_t><<<dkt::grid_for(nh * npe), 256, 0, s>>>(f.p2n.p, pl.p2n.p, rows.p, nh, (int) npe,
+                                                                     map.p, bad.p);
+      k_gather_rows<uint32_t><<<dkt::grid_for(nh * 3), 256, 0, s>>>(f.fill.p, pl.fill.p, rows.p, nh, 3, nullptr,
+                                                                    bad.p);
     }
     dkt::check_launch("part_remap");
     pl.bdry.alloc(1);
@@ -404,10 +427,11 @@ int dkt_plan_stats_ex(dkt_plan plan, int64_t *out, int n)
 {
   if (!plan || !out || n < 0) return fail(DKT_E_ARG, "bad argument");
   const dkt::Plan &pl = plan->pl;
-  const int64_t v[8] = {pl.n_leaf, pl.n_hang, pl.stale_slots, pl.n_bdry,
-                        pl.st_ready ? pl.st_n_ent : 0, pl.st_ready ? pl.st_n_runs : 0,
-                        pl.st_max_run_groups, pl.st_max_run_ents};
-  for (int k = 0; k < n && k < 8; k++) out[k] = v[k];
+  const int64_t v[10] = {pl.n_leaf, pl.n_hang, pl.stale_slots, pl.n_bdry,
+                         pl.st_ready ? pl.st_n_ent : 0, pl.st_ready ? pl.st_n_runs : 0,
+                         pl.st_max_run_groups, pl.st_max_run_ents,
+                         pl.tl_ready ? pl.tl_n_hs : 0, pl.tl_ready ? pl.tl_n_hleaf : 0};
+  for (int k = 0; k < n && k < 10; k++) out[k] = v[k];
   return DKT_OK;
 }
 
@@ -765,6 +789,16 @@ int dkt_plan_set_tile(dkt_plan plan, int tile_leaves)
   if (tile_leaves > 0 && !plan->pl.fx_ready) return fail(DKT_E_UNSUP, "tiles need a Q1 built-in operator");
   return guarded([&]() {
     dkt::tile_setup(plan->pl, tile_leaves, 0);
+    return DKT_OK;
+  });
+}
+
+int dkt_plan_set_hanging_slots(dkt_plan plan, int enable)
+{
+  if (!plan || (enable != 0 && enable != 1)) return fail(DKT_E_ARG, "bad argument");
+  return guarded([&]() {
+    plan->pl.tl_hns_enable = enable != 0;
+    if (plan->pl.tl_ready) dkt::tile_setup(plan->pl, plan->pl.tl_T, 0);
     return DKT_OK;
   });
 }
