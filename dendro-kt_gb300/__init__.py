@@ -78,7 +78,6 @@ def load(build_if_missing=True):
         "dkt_plan_kernel_timing": ([P, I, P, P], I),
         "dkt_plan_launch_count": ([P, P], I),
         "dkt_plan_set_tile": ([P, I], I),
-        "dkt_plan_set_hanging_slots": ([P, I], I),
         "dkt_batch_create": ([P, I, P], I),
         "dkt_plan_num_meshes": ([P, P], I),
         "dkt_plan_mesh_offsets": ([P, P], I),
@@ -244,11 +243,10 @@ class Matrix:
         return self
 
     def stats(self):
-        s = np.zeros(10, np.int64)
-        _check(load().dkt_plan_stats_ex(self._h, _p(s), 10))
+        s = np.zeros(8, np.int64)
+        _check(load().dkt_plan_stats_ex(self._h, _p(s), 8))
         return dict(zip(["leaves", "hanging_leaves", "stale_slots", "boundary_nodes", "stale_entries",
-                         "stale_runs", "stale_longest_run", "stale_longest_run_entries", "hanging_slots",
-                         "slot_reading_leaves"], s.tolist()))
+                         "stale_runs", "stale_longest_run", "stale_longest_run_entries"], s.tolist()))
 
     def export(self):
         """The flattened traversal as numpy arrays (e2n, info, hidx, p2n, fill)."""
@@ -310,10 +308,6 @@ class Matrix:
     def set_tile(self, tile_leaves):
         """Leaves per tile of the Q1 kernels (0: untiled kernel)."""
         _check(load().dkt_plan_set_tile(self._h, int(tile_leaves)))
-
-    def set_hanging_slots(self, enable):
-        """Hanging-node slots of the tiled Q1 kernel on (default) or off."""
-        _check(load().dkt_plan_set_hanging_slots(self._h, 1 if enable else 0))
 
     def launch_count(self):
         """Kernels launched so far by this matrix's products and solves."""

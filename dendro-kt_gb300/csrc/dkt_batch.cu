@@ -42,8 +42,8 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
 {
   if (in.empty()) throw std::invalid_argument("empty batch");
   const Plan &a = *in[0];
-  int64_t nn = 0, nl = 0, nh = 0, nb = 0, nt = 0, su = 0, ns = 0, nr = 0;
-  uint32_t umax = 0, hmax = 0;
+  int64_t nn = 0, nl = 0, nh = 0, nb = 0, nt = 0, su = 0;
+  uint32_t umax = 0;
   for (const Plan *p : in) {
     if (p->dim != a.dim || p->order != a.order || p->md != a.md || p->op.kind != a.op.kind ||
         p->conforming != a.conforming)
@@ -52,8 +52,7 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
     if (p->st_ready && p->st_n_runs > 0) throw std::invalid_argument("plans with stale parent reads cannot be batched");
     if (p->tl_ready != a.tl_ready || p->tl_T != a.tl_T) throw std::invalid_argument("plans of a batch must share tiling");
     nn += p->n_nodes; nl += p->n_leaf; nh += p->n_hang; nb += p->n_bdry;
-    nt += p->tl_n; su += p->tl_sum_u; ns += p->tl_n_hs; nr += p->tl_n_rest; umax = std::max(umax, p->tl_umax);
-    hmax = std::max(hmax, p->tl_hmax);
+    nt += p->tl_n; su += p->tl_sum_u; umax = std::max(umax, p->tl_umax);
   }
   if (nn >= (int64_t) 0x7FFFFFFF || nh >= (int64_t) 0x7FFFFFFF) throw std::invalid_argument("batch too large");
   const int npe = a.npe;
@@ -74,18 +73,17 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
   if (a.tl_ready) {
     out.tl_off.alloc(nt + 1);
     out.tl_lstart.alloc(nt + 1);
+    out.tl_hb.alloc(nt + 1);
+    out.tl_fm.alloc(std::max<int64_t>(nh, 1));
     out.tl_nodes.alloc(std::max<int64_t>(su, 1));
     out.tl_tau.alloc(std::max<int64_t>(nt, 1));
     out.tl_e2l.alloc((size_t) nl * npe);
-    out.tl_rest.alloc(std::max<int64_t>(nr, 1));
-    out.tl_hs_off.alloc(nt + 1);
-    out.tl_hs_def.alloc((size_t) std::max<int64_t>(ns, 1) * 8);
-    out.tl_hs_p.alloc((size_t) std::max<int64_t>(ns, 1));
+    out.tl_p2l.alloc((size_t) std::max<int64_t>(nh, 1) * npe);
   }
   out.seg.assign(1, 0);
   out.lseg.assign(1, 0);
   std::vector<int32_t> mlo;
-  int64_t bn = 0, bl = 0, bh = 0, bb = 0, bt = 0, bu = 0, bs = 0, br = 0;
+  int64_t bn = 0, bl = 0, bh = 0, bb = 0, bt = 0, bu = 0;
   for (const Plan *p : in) {
     const size_t ne = (size_t) p->n_leaf * npe, np_ = (size_t) p->n_hang * npe;
     if (ne) k_offset_ids<<<grid_for(ne), 256, 0, s>>>(p->e2n.p, out.e2n.p + bl * npe, ne, (int32_t) bn);
@@ -98,30 +96,23 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
     if (a.tl_ready) {
       k_offset_i64<<<grid_for(p->tl_n + 1), 256, 0, s>>>(p->tl_off.p, out.tl_off.p + bt, p->tl_n + 1, bu);
       k_offset_i64<<<grid_for(p->tl_n + 1), 256, 0, s>>>(p->tl_lstart.p, out.tl_lstart.p + bt, p->tl_n + 1, bl);
+      k_offset_i64<<<grid_for(p->tl_n), 256, 0, s>>>(p->tl_hb.p, out.tl_hb.p + bt, p->tl_n, bh);
+      copy_to(out.tl_fm.p + bh, p->tl_fm.p, (size_t) p->n_hang, s);
       if (p->tl_sum_u)
         k_offset_u32<<<grid_for(p->tl_sum_u), 256, 0, s>>>(p->tl_nodes.p, out.tl_nodes.p + bu, p->tl_sum_u,
                                                             (uint32_t) bn, 0xF8000000u);   // keep level + flag bits
       copy_to(out.tl_tau.p + bt, p->tl_tau.p, (size_t) p->tl_n, s);
       copy_to(out.tl_e2l.p + bl * npe, p->tl_e2l.p, ne, s);
-      if (p->tl_n_rest)
-        k_offset_ids<<<grid_for(p->tl_n_rest), 256, 0, s>>>(p->tl_rest.p, out.tl_rest.p + br, p->tl_n_rest,
-                                                            (int32_t) bl);
-      // hanging-node slots: tile-local indices, so only the offsets move
-      k_offset_i64<<<grid_for(p->tl_n + 1), 256, 0, s>>>(p->tl_hs_off.p, out.tl_hs_off.p + bt, p->tl_n + 1, bs);
-      copy_to(out.tl_hs_def.p + bs * 8, p->tl_hs_def.p, (size_t) p->tl_n_hs * 8, s);
-      copy_to(out.tl_hs_p.p + bs, p->tl_hs_p.p, (size_t) p->tl_n_hs, s);
+      copy_to(out.tl_p2l.p + bh * npe, p->tl_p2l.p, np_, s);
     }
     check_launch("batch_combine");
     for (int64_t t = 0; t < p->tl_n; t++) mlo.push_back((int32_t) out.seg.size() - 1);
     bn += p->n_nodes; bl += p->n_leaf; bh += p->n_hang; bb += p->n_bdry; bt += p->tl_n; bu += p->tl_sum_u;
-    bs += p->tl_n_hs; br += p->tl_n_rest;
     out.seg.push_back(bn);
     out.lseg.push_back(bl);
   }
   if (a.tl_ready) {
-    out.tl_T = a.tl_T; out.tl_n = nt; out.tl_sum_u = su; out.tl_umax = umax; out.tl_hmax = hmax; out.tl_n_hs = ns;
-    out.tl_n_rest = nr;
-    out.tl_n_hleaf = nh - nr;
+    out.tl_T = a.tl_T; out.tl_n = nt; out.tl_sum_u = su; out.tl_umax = umax;
     if (mlo.empty()) mlo.push_back(0);
     out.tl_mlo.upload(mlo.data(), mlo.size(), s);
     out.tl_mhi.upload(mlo.data(), mlo.size(), s);   // tiles of one plan never straddle meshes

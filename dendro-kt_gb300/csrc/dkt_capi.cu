@@ -427,11 +427,10 @@ int dkt_plan_stats_ex(dkt_plan plan, int64_t *out, int n)
 {
   if (!plan || !out || n < 0) return fail(DKT_E_ARG, "bad argument");
   const dkt::Plan &pl = plan->pl;
-  const int64_t v[10] = {pl.n_leaf, pl.n_hang, pl.stale_slots, pl.n_bdry,
-                         pl.st_ready ? pl.st_n_ent : 0, pl.st_ready ? pl.st_n_runs : 0,
-                         pl.st_max_run_groups, pl.st_max_run_ents,
-                         pl.tl_ready ? pl.tl_n_hs : 0, pl.tl_ready ? pl.tl_n_hleaf : 0};
-  for (int k = 0; k < n && k < 10; k++) out[k] = v[k];
+  const int64_t v[8] = {pl.n_leaf, pl.n_hang, pl.stale_slots, pl.n_bdry,
+                        pl.st_ready ? pl.st_n_ent : 0, pl.st_ready ? pl.st_n_runs : 0,
+                        pl.st_max_run_groups, pl.st_max_run_ents};
+  for (int k = 0; k < n && k < 8; k++) out[k] = v[k];
   return DKT_OK;
 }
 
@@ -789,16 +788,6 @@ int dkt_plan_set_tile(dkt_plan plan, int tile_leaves)
   if (tile_leaves > 0 && !plan->pl.fx_ready) return fail(DKT_E_UNSUP, "tiles need a Q1 built-in operator");
   return guarded([&]() {
     dkt::tile_setup(plan->pl, tile_leaves, 0);
-    return DKT_OK;
-  });
-}
-
-int dkt_plan_set_hanging_slots(dkt_plan plan, int enable)
-{
-  if (!plan || (enable != 0 && enable != 1)) return fail(DKT_E_ARG, "bad argument");
-  return guarded([&]() {
-    plan->pl.tl_hns_enable = enable != 0;
-    if (plan->pl.tl_ready) dkt::tile_setup(plan->pl, plan->pl.tl_T, 0);
     return DKT_OK;
   });
 }

@@ -160,7 +160,7 @@ struct Plan {
   int64_t n_nodes = 0, n_leaf = 0, n_hang = 0, n_bdry = 0;
   int64_t stale_slots = 0;           // parent slots read unfilled with nonzero weight
   DBuf<int32_t> e2n;                 // [n_leaf][npe]  node index or -1
-  DBuf<uint32_t> info;               // [n_leaf] level | child<<8 | hanging<<16 | rank among the tile's hanging leaves<<17 | reads stale slots<<27 | reads hanging-node slots<<28
+  DBuf<uint32_t> info;               // [n_leaf] level | child<<8 | hanging<<16 | rank among the tile's hanging leaves<<17 | reads stale slots<<27
   DBuf<int32_t> hidx;                // [n_leaf] index into hanging arrays or -1
   DBuf<int32_t> p2n;                 // [n_hang][npe] parent node index (level L-1) or -1
   DBuf<uint32_t> fill;               // [n_hang][3] filled-rank bitmask of the leaf
@@ -225,25 +225,11 @@ struct Plan {
   bool tl_ready = false;
   int tl_T = 0;
   int64_t tl_n = 0, tl_sum_u = 0;
-  uint32_t tl_umax = 0, tl_hmax = 0;
-  DBuf<int64_t> tl_off, tl_lstart;   // per tile: node-list offset, first leaf
-  DBuf<uint32_t> tl_nodes;            // distinct nodes (| exclusive flag | unit level)
-  DBuf<uint16_t> tl_e2l;              // tile-local element maps (reflected for hanging leaves)
-  // hanging leaves that read no hanging-node slots (info bit 28 clear): done
-  // by the per-leaf kernel after the tiled one
-  DBuf<int32_t> tl_rest;
-  int64_t tl_n_rest = 0;
+  uint32_t tl_umax = 0;
+  DBuf<int64_t> tl_off, tl_lstart, tl_hb;   // per tile: node-list offset, first leaf, first hanging index
+  DBuf<uint32_t> tl_nodes, tl_fm;     // distinct nodes (| exclusive flag); reflected fill masks
+  DBuf<uint16_t> tl_e2l, tl_p2l;
   DBuf<uint8_t> tl_tau;              // per tile: coarsest leaf level (its fixed-point unit)
-  // Hanging-node slots (dkt_tile.cu): per tile the distinct hanging points
-  // of its slot-reading hanging leaves (info bit 28), each the centre of a
-  // parent face with 2^p corners; slot s of tile t sits at tile-local index
-  // U_t + s, its corners in tl_hs_def[8 (tl_hs_off[t] + s) ...] (tile-local
-  // node indices) and p in tl_hs_p.
-  bool tl_hns_enable = true;
-  int64_t tl_n_hs = 0, tl_n_hleaf = 0;
-  DBuf<int64_t> tl_hs_off;           // [n_tile + 1]
-  DBuf<uint16_t> tl_hs_def;          // [n_hs][8]
-  DBuf<uint8_t> tl_hs_p;             // [n_hs]
   // persistent tiled launch (CTAs pull tiles from a counter) instead of one
   // CTA per tile; chosen by dkt_plan_autotune
   bool tl_persist = false;

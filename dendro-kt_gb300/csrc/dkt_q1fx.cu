@@ -584,28 +584,24 @@ bool q1fx_setup(Plan &pl, cudaStream_t s)
   return true;
 }
 
-void tiled_fixed(Plan &pl, cudaStream_t s);
+void tiled_fixed(Plan &pl, bool skip_stale, cudaStream_t s);
 void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s);
 
-// The hanging leaves that read no hanging-node slots (among them every leaf
-// that reads stale slots), after the tiled kernel and the chain: the
-// per-leaf kernel over pl.tl_rest.
+// The leaves that read stale slots, after the chain (per-leaf kernel).
 template <int DIM>
-static void launch_q1fx_rest(Plan &pl, cudaStream_t s)
+static void launch_q1fx_stale_leaves(Plan &pl, cudaStream_t s)
 {
   const unsigned threads = 256;
-  k_matvec_q1<DIM, FixedArith><<<grid_for(pl.tl_n_rest * ((1 << DIM) / 4), threads), threads, 0, s>>>(
+  k_matvec_q1<DIM, FixedArith><<<grid_for(pl.st_n_hleaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p, pl.xq.p,
-      pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0,
-      pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr, pl.fx_kappa, pl.md + 1, pl.tl_rest.p, pl.tl_n_rest);
-  check_launch("matvec_q1fx_rest");
+      pl.yq.p, pl.st_hzoff.p, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0,
+      pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr, pl.fx_kappa, pl.md + 1, pl.st_hleaves.p, pl.st_n_hleaf);
+  check_launch("matvec_q1fx_stale_leaves");
   pl.n_launch++;
 }
 
-// split: the stale-buffer chain runs on the side stream; the leaves that
-// read it wait for its join.  The timed window covers every leaf launch.
 template <int DIM>
-static void launch_q1fx(Plan &pl, bool split, cudaStream_t s)
+static void launch_q1fx(Plan &pl, bool skip_stale, cudaStream_t s)
 {
   const unsigned threads = 256;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -614,11 +610,8 @@ static void launch_q1fx(Plan &pl, bool split, cudaStream_t s)
     DKT_CUDA(cudaEventCreate(&e1));
     DKT_CUDA(cudaEventRecord(e0, s));
   }
-  if (pl.tl_ready) {
-    tiled_fixed(pl, s);
-    if (split) DKT_CUDA(cudaStreamWaitEvent(s, pl.st_join, 0));
-    if (pl.tl_n_rest > 0) launch_q1fx_rest<DIM>(pl, s);
-  } else k_matvec_q1<DIM, FixedArith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
+  if (pl.tl_ready) tiled_fixed(pl, skip_stale, s);
+  else k_matvec_q1<DIM, FixedArith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.fx_fm.p,
       pl.xq.p, pl.yq.p, pl.st_ready ? pl.st_hzoff.p : nullptr, pl.st_hztab.p, pl.st_vq.p, pl.conforming ? 1 : 0,
       pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr, pl.fx_kappa, pl.md + 1);
@@ -638,17 +631,7 @@ template <int DIM>
 static void launch_q1f32(Plan &pl, const float *x, float *y, cudaStream_t s)
 {
   const unsigned threads = 256;
-  if (pl.tl_ready) {
-    tiled_f32(pl, x, y, s);
-    if (pl.tl_n_rest > 0) {
-      k_matvec_q1<DIM, F32Arith><<<grid_for(pl.tl_n_rest * ((1 << DIM) / 4), threads), threads, 0, s>>>(
-          pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.f32_f.p, x, y, nullptr,
-          nullptr, nullptr, pl.conforming ? 1 : 0, nullptr, 0, pl.md + 1, pl.tl_rest.p, pl.tl_n_rest);
-      check_launch("matvec_q1f32_rest");
-      pl.n_launch++;
-    }
-    return;
-  }
+  if (pl.tl_ready) { tiled_f32(pl, x, y, s); return; }
   k_matvec_q1<DIM, F32Arith><<<grid_for(pl.n_leaf * ((1 << DIM) / 4), threads), threads, 0, s>>>(
       pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, pl.n_hang, pl.f32_f.p, x, y,
       nullptr, nullptr, nullptr, pl.conforming ? 1 : 0, nullptr, 0, pl.md + 1);
@@ -758,6 +741,14 @@ void q1fx_matvec(Plan &pl, const double *x, double *y, double scale, bool bc, cu
     case 3: launch_q1fx<3>(pl, split, s); break;
     case 4: launch_q1fx<4>(pl, split, s); break;
     default: throw std::runtime_error("unsupported dim");
+  }
+  if (split) {
+    DKT_CUDA(cudaStreamWaitEvent(s, pl.st_join, 0));
+    switch (pl.dim) {
+      case 2: launch_q1fx_stale_leaves<2>(pl, s); break;
+      case 3: launch_q1fx_stale_leaves<3>(pl, s); break;
+      case 4: launch_q1fx_stale_leaves<4>(pl, s); break;
+    }
   }
   const uint8_t *lam = pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr;
   switch (pl.fx_div) {

@@ -40,8 +40,6 @@ constexpr uint32_t TL_EXCL = 0x80000000u;
 constexpr uint32_t TL_ID = 0x07FFFFFFu;
 constexpr int TL_LAM = 27;
 constexpr int TL_SINKS = 32;   // sink entries past a tile's nodes, one per lane
-// info bit 28: a hanging leaf whose unfilled ranks read hanging-node slots
-constexpr uint32_t INFO_HNS = 1u << 28;
 
 // ---------------------------------------------------------------------------
 // Plan-time tile build: one CTA per tile sorts the tile's (node, slot) pairs
@@ -70,15 +68,12 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(
   for (int s = threadIdx.x; s < cap; s += TB_THREADS) {
     int32_t node = -1;
     const int half = T * npe;
-    // hanging leaves that read no hanging-node slots are the per-leaf
-    // kernel's: nothing of theirs goes into the tile
     if (s < half) {
       const int j = s / npe;
-      if (j < nl && !(((info[l0 + j] >> 16) & 1u) && !(info[l0 + j] & INFO_HNS)))
-        node = e2n[(l0 + j) * npe + s % npe];
+      if (j < nl) node = e2n[(l0 + j) * npe + s % npe];
     } else {
       const int j = (s - half) / npe;
-      if (j < nl && (info[l0 + j] & INFO_HNS)) node = p2n[(int64_t) hidx[l0 + j] * npe + (s - half) % npe];
+      if (j < nl && ((info[l0 + j] >> 16) & 1u)) node = p2n[(int64_t) hidx[l0 + j] * npe + (s - half) % npe];
     }
     key[s] = node >= 0 ? (((uint64_t) (uint32_t) node << 32) | (uint32_t) s) : ~0ull;
   }
@@ -148,82 +143,35 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(
   }
 }
 
-// Which hanging leaves read hanging-node slots (info bit 28; the others go
-// to the per-leaf kernel).  In the reflected frame (rank k of the leaf, parent
-// rank k, at position k ^ c of the maps), with U the unfilled ranks:
-//   * the leaf reads no stale parent slot (info bit 27);
-//   * rank 0 is filled, and no unfilled rank spans every axis (a face of at
-//     most 2^(dim-1) corners);
-//   * every unfilled rank's face has two opposite corners that are nodes
-//     (they name the face; a corner with no node reads 0 in both forms);
-//   * reference traversal only: U is closed under removing an axis (down to
-//     rank 0), and rank 0 is the parent's rank-0 node.  Then the parent ranks
-//     the reference transpose reaches (unfilled ones) are exactly the corners
-//     of the unfilled ranks' faces other than rank 0, and the slot form sends
-//     to every corner and takes rank 0's share back.
-__global__ void k_hns_flag(const int32_t *__restrict__ e2n, uint32_t *__restrict__ info,
-                           const int32_t *__restrict__ hidx, const int32_t *__restrict__ p2n,
-                           const uint32_t *__restrict__ fill, int64_t n_leaf, int npe, int dim, int conforming,
-                           int enable)
-{
-  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_leaf) return;
-  uint32_t inf = info[i] & ~INFO_HNS;
-  if (enable && ((inf >> 16) & 1u) && !((inf >> 27) & 1u)) {
-    const int c = (int) ((inf >> 8) & 0xFFu);
-    const int64_t h = hidx[i];
-    const uint32_t f = fill[h * 3];
-    const int32_t *pr = p2n + h * npe, *er = e2n + i * npe;
-    uint32_t um = 0;
-    for (int k = 0; k < npe; k++) um |= (((f >> (k ^ c)) & 1u) ^ 1u) << k;
-    bool ok = !(um & 1u) && (conforming || (er[c] >= 0 && er[c] == pr[c]));
-    for (int k = 1; k < npe && ok; k++) {
-      if (!((um >> k) & 1u)) continue;
-      if (__popc(k) >= dim) ok = false;
-      if (!conforming)
-        for (int d = 0; d < dim; d++)
-          if (((k >> d) & 1) && k != (1 << d) && !((um >> (k ^ (1 << d))) & 1u)) ok = false;
-      bool pair = false;
-      for (int q = 0; q < npe; q++)
-        if (!(q & ~k) && pr[q ^ c] >= 0 && pr[(q ^ k) ^ c] >= 0) pair = true;
-      ok = ok && pair;
-    }
-    if (ok) inf |= INFO_HNS;
-  }
-  info[i] = inf;
-}
-
-// Within every tile (stable): slot-reading hanging leaves, then non-hanging
-// leaves, then the hanging leaves left to the per-leaf kernel (idle here).
-// The warps of a tile then mostly run one code path.  Leaf order does not
-// matter to the product (integer sums); the hanging records stay indexed by
-// hidx.
+// Within every tile, hanging leaves first (stable): the warps of a tile then
+// run mostly one code path (a hanging leaf does the interpolation and its
+// transpose, about half again the work).  Leaf order does not matter to the
+// product (integer sums); the hanging records stay indexed by h.
 __global__ void k_tile_partition(const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info,
                                  const int32_t *__restrict__ hidx, int32_t *__restrict__ e2n_o,
                                  uint32_t *__restrict__ info_o, int32_t *__restrict__ hidx_o, int64_t n_leaf, int T,
                                  int npe)
 {
-  __shared__ uint32_t wc[3][32];
+  __shared__ uint32_t wc[32];
   const int64_t l0 = (int64_t) blockIdx.x * T;
   const int64_t i = l0 + threadIdx.x;
   const bool valid = i < n_leaf;
-  const uint32_t inf = valid ? info[i] : 0u;
-  const int cls = !valid ? 3 : ((inf >> 16) & 1u) ? ((inf & INFO_HNS) ? 0 : 2) : 1;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (int) (blockDim.x >> 5);
-  unsigned m[3];
-  for (int q = 0; q < 3; q++) {
-    m[q] = __ballot_sync(0xffffffffu, cls == q);
-    if (lane == 0) wc[q][w] = __popc(m[q]);
-  }
+  const int nl = (int) (n_leaf - l0 < T ? n_leaf - l0 : T);
+  const bool hang = valid && ((info[i] >> 16) & 1u);
+  const unsigned m = __ballot_sync(0xffffffffu, hang);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wc[w] = __popc(m);
   __syncthreads();
+  uint32_t before = __popc(m & ((1u << lane) - 1u)), total = 0;
+  for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
+    if (k < w) before += wc[k];
+    total += wc[k];
+  }
   if (!valid) return;
-  uint32_t pos = __popc(m[cls] & ((1u << lane) - 1u));
-  for (int q = 0; q < 3; q++)
-    for (int k = 0; k < nw; k++)
-      if (q < cls || (q == cls && k < w)) pos += wc[q][k];
-  const int64_t j = l0 + pos;
+  const int64_t j = l0 + (hang ? (int64_t) before : (int64_t) total + (threadIdx.x - before));
+  (void) nl;
   for (int k = 0; k < npe; k++) e2n_o[j * npe + k] = e2n[i * npe + k];
-  info_o[j] = inf;
+  info_o[j] = info[i];
   hidx_o[j] = hidx[i];
 }
 __global__ void k_flag27(const uint32_t *__restrict__ info, uint32_t *__restrict__ f, int64_t n)
@@ -231,16 +179,55 @@ __global__ void k_flag27(const uint32_t *__restrict__ info, uint32_t *__restrict
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) f[i] = (info[i] >> 27) & 1u;
 }
-// hanging leaves that read no hanging-node slots
-__global__ void k_flag_rest(const uint32_t *__restrict__ info, uint32_t *__restrict__ f, int64_t n)
-{
-  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) f[i] = ((info[i] >> 16) & 1u) && !(info[i] & INFO_HNS) ? 1u : 0u;
-}
 __global__ void k_iota_i32(int32_t *__restrict__ v, int64_t n)
 {
   const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) v[i] = (int32_t) i;
+}
+
+// Reflected fill masks: bit k = fill bit (k ^ c) of hanging leaf h (Q1: nPe <= 16).
+__global__ void k_tile_fmask(const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+                             const uint32_t *__restrict__ fill, int64_t n_leaf, int npe, uint32_t *__restrict__ fm)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_leaf) return;
+  const uint32_t inf = info[i];
+  if (!((inf >> 16) & 1u)) return;
+  const int c = (int) ((inf >> 8) & 0xFFu);
+  const int64_t h = hidx[i];
+  const uint32_t f = fill[h * 3];
+  uint32_t m = 0;
+  for (int k = 0; k < npe; k++) m |= ((f >> (k ^ c)) & 1u) << k;
+  fm[h] = m;
+}
+// Per tile: the hanging index of its first hanging leaf (hb), and in bits
+// 17..26 of every hanging leaf's info word its rank among the tile's hanging
+// leaves, so the kernel finds a leaf's hanging records without reading hidx.
+// One CTA of `T` threads per tile.
+__global__ void k_tile_ranks(uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+                             const int64_t *__restrict__ ls, int64_t *__restrict__ hb)
+{
+  __shared__ uint32_t wc[32];
+  const int64_t t = blockIdx.x;
+  const int64_t i = ls[t] + threadIdx.x;
+  const bool valid = i < ls[t + 1];
+  uint32_t inf = valid ? info[i] : 0u;
+  const bool hang = valid && ((inf >> 16) & 1u);
+  const unsigned m = __ballot_sync(0xffffffffu, hang);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wc[w] = __popc(m);
+  __syncthreads();
+  uint32_t r = __popc(m & ((1u << lane) - 1u));
+  for (int k = 0; k < w; k++) r += wc[k];
+  if (threadIdx.x == 0) hb[t] = 0;
+  __syncthreads();
+  constexpr uint32_t RANK = 0x3FFu << 17;
+  if (hang) {
+    info[i] = (inf & ~RANK) | (r << 17);
+    if (r == 0) hb[t] = hidx[i];
+  } else if (valid) {
+    info[i] = inf & ~RANK;
+  }
 }
 
 // tau[t] = the coarsest leaf level of tile t (its fixed-point unit)
@@ -263,137 +250,23 @@ __global__ void k_tile_lstart(int64_t *__restrict__ ls, int64_t n_tile, int64_t 
 }
 
 // Slots with no node (TL_NONE) are pointed at one of TL_SINKS per-lane sink
-// entries past the tile's U nodes and H hanging-node slots (U + H + lane):
-// the leaf kernel reads 0 there and adds into a sink that is never written
-// out, with no test per slot.  Lanes of one warp have distinct sinks.  One
-// CTA of `T` threads per tile.
-__global__ void k_tile_sinks(uint16_t *__restrict__ e2l, const int64_t *__restrict__ ls,
-                             const int64_t *__restrict__ off, const int64_t *__restrict__ hs_off, int npe)
+// entries past the tile's U nodes (U + lane): the leaf kernel reads 0 there
+// and adds into a sink that is never written out, with no test per slot.
+// Lanes of one warp have distinct sinks.  One CTA of `T` threads per tile.
+__global__ void k_tile_sinks(uint16_t *__restrict__ e2l, uint16_t *__restrict__ p2l,
+                             const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx,
+                             const int64_t *__restrict__ ls, const int64_t *__restrict__ off, int npe)
 {
   const int64_t t = blockIdx.x;
   const int64_t i = ls[t] + threadIdx.x;
   if (i >= ls[t + 1]) return;
-  const uint16_t sink = (uint16_t) (off[t + 1] - off[t] + (hs_off[t + 1] - hs_off[t]) + (threadIdx.x & (TL_SINKS - 1)));
+  const uint16_t sink = (uint16_t) (off[t + 1] - off[t] + (threadIdx.x & (TL_SINKS - 1)));
   for (int k = 0; k < npe; k++)
     if (e2l[i * npe + k] == TL_NONE) e2l[i * npe + k] = sink;
-}
-
-// ---------------------------------------------------------------------------
-// Hanging-node slots.  In the reflected (child-0) frame an unfilled rank k of
-// a hanging leaf is the centre of the parent face spanned by the axes of k,
-// and its interpolated value is the mean of the parent nodes on the subsets
-// of k -- the face's 2^popcount(k) corners.  The value depends on the point
-// only, so the leaves of a tile that meet at one hanging point share one
-// slot: its value is computed once per tile from the face's corners, and the
-// leaves read and add into it like a node.  The transpose then sends each
-// slot's sum to every corner of its face once per tile; in the reference
-// traversal a leaf's transpose leaves out the parent corner it shares (rank
-// 0), so the leaf takes its own share back at its rank-0 node (k_hns_flag
-// has the conditions).  Integer sums: the fixed-point product is the same as
-// interpolating and transposing per leaf in the same tile.
-//
-// A face is named by the corner with the smallest local index among those
-// whose opposite corner is also a node, and that opposite corner (two
-// opposite corners fix an axis-aligned box).  One CTA of HB_THREADS per tile
-// sorts the (face, leaf, rank) keys of its slot-reading leaves in shared
-// memory:
-//   mode 0: count the faces;
-//   mode 1: write the slots (corners, p) and point the leaves' unfilled
-//           ranks at them (U + slot).
-// Key: p (bits 62-63), first corner (46-61), opposite corner (30-45), leaf
-// within the tile (4-13), rank (0-3); a tile's slots come sorted by p.
-// A corner with no node is written as the tile's first sink (U + H), which
-// reads 0 and is never written out.
-// ---------------------------------------------------------------------------
-constexpr int HB_THREADS = 256;
-
-template <int NPE>
-__global__ void __launch_bounds__(HB_THREADS) k_hns_build(
-    int mode, const uint32_t *__restrict__ info, const int32_t *__restrict__ hidx, const int64_t *__restrict__ ls,
-    const int64_t *__restrict__ off, uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, int cap,
-    uint32_t *__restrict__ cnt, const int64_t *__restrict__ hs_off, uint16_t *__restrict__ hs_def,
-    uint8_t *__restrict__ hs_p, int *__restrict__ err)
-{
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t *key = reinterpret_cast<uint64_t *>(smem);            // [cap]
-  __shared__ uint32_t part[HB_THREADS];
-  const int64_t t = blockIdx.x;
-  const int64_t l0 = ls[t];
-  const int nl = (int) (ls[t + 1] - l0);
-  const uint32_t U = (uint32_t) (off[t + 1] - off[t]);
-  for (int s = threadIdx.x; s < cap; s += HB_THREADS) key[s] = ~0ull;
-  __syncthreads();
-  for (int j = threadIdx.x; j < nl; j += HB_THREADS) {
-    const int64_t i = l0 + j;
-    if (!(info[i] & INFO_HNS)) continue;
-    const uint16_t *er = e2l + i * NPE, *pr = p2l + (int64_t) hidx[i] * NPE;
-    for (int k = 1; k < NPE; k++) {
-      if (er[k] != TL_NONE) continue;                    // filled
-      uint32_t a = 0xFFFFu;
-      int qa = -1;
-      for (int q = 0; q < NPE; q++)
-        if (!(q & ~k) && pr[q] < U && pr[q ^ k] < U && pr[q] < a) { a = pr[q]; qa = q; }
-      if (qa < 0) { atomicOr(err, 1); continue; }       // excluded by k_hns_flag
-      const uint32_t b = pr[qa ^ k];
-      key[j * (NPE - 1) + (k - 1)] = ((uint64_t) __popc(k) << 62) | ((uint64_t) a << 46) | ((uint64_t) b << 30) |
-                                     (uint64_t) ((j << 4) | k);
-    }
-  }
-  __syncthreads();
-  // bitonic sort, ascending
-  for (int k = 2; k <= cap; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < cap; i += HB_THREADS) {
-        const int p = i ^ j;
-        if (p > i) {
-          const uint64_t a = key[i], b = key[p];
-          const bool up = (i & k) == 0;
-          if ((a > b) == up) { key[i] = b; key[p] = a; }
-        }
-      }
-      __syncthreads();
-    }
-  }
-  // distinct faces (key >> 30): each thread owns a contiguous run of keys
-  const int per = cap / HB_THREADS;   // cap is a multiple of HB_THREADS
-  const int b0 = threadIdx.x * per;
-  uint32_t c = 0;
-  for (int k = b0; k < b0 + per; k++) {
-    const uint64_t a = key[k];
-    if (a != ~0ull && (k == 0 || (key[k - 1] >> 30) != (a >> 30))) c++;
-  }
-  part[threadIdx.x] = c;
-  __syncthreads();
-  for (int o = 1; o < HB_THREADS; o <<= 1) {
-    const uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
-    __syncthreads();
-    part[threadIdx.x] += v;
-    __syncthreads();
-  }
-  if (mode == 0) {
-    if (threadIdx.x == 0) cnt[t] = part[HB_THREADS - 1];
-    return;
-  }
-  uint32_t rank = part[threadIdx.x] - c;
-  const int64_t base = hs_off[t];
-  const uint16_t sink = (uint16_t) (U + (hs_off[t + 1] - base));
-  for (int k = b0; k < b0 + per; k++) {
-    const uint64_t a = key[k];
-    if (a == ~0ull) break;
-    const bool head = (k == 0 || (key[k - 1] >> 30) != (a >> 30));
-    if (head) rank++;
-    const int j = (int) ((a >> 4) & 0x3FFu), r = (int) (a & 15u);
-    const int64_t i = l0 + j;
-    e2l[i * NPE + r] = (uint16_t) (U + rank - 1);
-    if (head) {
-      const uint16_t *pr = p2l + (int64_t) hidx[i] * NPE;
-      uint16_t *row = hs_def + (base + rank - 1) * 8;
-      int n = 0;
-      for (int q = 0; q < NPE; q++)
-        if (!(q & ~r)) row[n++] = pr[q] < U ? pr[q] : sink;
-      for (; n < 8; n++) row[n] = sink;
-      hs_p[base + rank - 1] = (uint8_t) __popc(r);
-    }
+  if ((info[i] >> 16) & 1u) {
+    const int64_t h = hidx[i];
+    for (int k = 0; k < npe; k++)
+      if (p2l[h * npe + k] == TL_NONE) p2l[h * npe + k] = sink;
   }
 }
 
@@ -404,22 +277,14 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   if (pl.order != 1 || pl.n_leaf == 0 || T <= 0) return;
   if (T < 32 || T > 1024 || (T & (T - 1))) throw std::invalid_argument("tile size must be a power of two in [32, 1024]");
   const int npe = pl.npe;
-  if (npe != 4 && npe != 8 && npe != 16) throw std::invalid_argument("tiles need a Q1 plan");
   int cap = 1;
   while (cap < 2 * T * npe) cap <<= 1;
   cap = std::max(cap, TB_THREADS);
   if (cap > 65536) throw std::invalid_argument("tile too large");   // 16-bit local indices
   if (pl.n_nodes > (int64_t) TL_ID + 1) throw std::invalid_argument("too many nodes for tiles");
   const int64_t n_tile = (pl.n_leaf + T - 1) / T;
-  // slot keys per tile: T (npe - 1) (leaf, rank) pairs
-  int hcap = HB_THREADS;
-  while (hcap < T * (npe - 1)) hcap <<= 1;
-  const bool hns = pl.tl_hns_enable && (size_t) hcap * sizeof(uint64_t) <= 128 * 1024;
-  k_hns_flag<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.fill.p, pl.n_leaf, npe,
-                                                 pl.dim, pl.conforming ? 1 : 0, hns ? 1 : 0);
-  check_launch("hns_flag");
   if (pl.seg.empty()) {
-    // a single mesh: every tile's leaves in three runs (a batch keeps the
+    // hanging leaves first within each tile (a single mesh: a batch keeps the
     // concatenated order of its meshes)
     DBuf<int32_t> e2n_o((size_t) pl.n_leaf * npe), hidx_o(pl.n_leaf);
     DBuf<uint32_t> info_o(pl.n_leaf);
@@ -443,19 +308,6 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
       if (nh != pl.st_n_hleaf) throw std::runtime_error("stale leaf list changed size");
     }
   }
-  {
-    // the hanging leaves left to the per-leaf kernel
-    DBuf<uint32_t> f(pl.n_leaf), pos(pl.n_leaf);
-    DBuf<int32_t> iota(pl.n_leaf);
-    k_flag_rest<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.info.p, f.p, pl.n_leaf);
-    k_iota_i32<<<grid_for(pl.n_leaf), 256, 0, s>>>(iota.p, pl.n_leaf);
-    pl.tl_n_rest = (int64_t) exclusive_scan_total<uint32_t>(f.p, pos.p, pl.n_leaf, s);
-    pl.tl_rest.alloc(std::max<int64_t>(pl.tl_n_rest, 1));
-    scatter_if_kernel<int32_t><<<grid_for(pl.n_leaf), 256, 0, s>>>(iota.p, f.p, pos.p, pl.tl_rest.p, pl.n_leaf);
-    check_launch("rest_leaves");
-    DKT_CUDA(cudaStreamSynchronize(s));
-    pl.tl_n_hleaf = pl.n_hang - pl.tl_n_rest;
-  }
   DBuf<uint32_t> node_tiles(pl.n_nodes), cnt(n_tile);
   DKT_CUDA(cudaMemsetAsync(node_tiles.p, 0, pl.n_nodes * sizeof(uint32_t), s));
   const size_t smem = (size_t) cap * sizeof(uint64_t);
@@ -464,63 +316,36 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
                                                           npe, T, cap, node_tiles.p, cnt.p, nullptr, nullptr,
                                                           nullptr, nullptr, nullptr);
   check_launch("tile_count");
-  // offsets (host scan: one value per tile)
+  // offsets (host scan: one value per tile) and the largest tile
   std::vector<uint32_t> hc(n_tile);
   DKT_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_tile * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   DKT_CUDA(cudaStreamSynchronize(s));
   std::vector<int64_t> ho(n_tile + 1, 0);
-  for (int64_t t = 0; t < n_tile; t++) ho[t + 1] = ho[t] + hc[t];
+  uint32_t umax = 0;
+  for (int64_t t = 0; t < n_tile; t++) {
+    ho[t + 1] = ho[t] + hc[t];
+    umax = std::max(umax, hc[t]);
+  }
   pl.tl_off.upload(ho.data(), ho.size(), s);
   pl.tl_nodes.alloc(std::max<int64_t>(ho[n_tile], 1));
   pl.tl_e2l.alloc((size_t) pl.n_leaf * npe);
-  // tile-local parent maps: only for building the slots
-  DBuf<uint16_t> p2l((size_t) std::max<int64_t>(pl.n_hang, 1) * npe);
+  pl.tl_p2l.alloc((size_t) std::max<int64_t>(pl.n_hang, 1) * npe);
   DKT_CUDA(cudaMemsetAsync(pl.tl_e2l.p, 0xFF, (size_t) pl.n_leaf * npe * sizeof(uint16_t), s));
-  DKT_CUDA(cudaMemsetAsync(p2l.p, 0xFF, (size_t) std::max<int64_t>(pl.n_hang, 1) * npe * sizeof(uint16_t), s));
+  DKT_CUDA(cudaMemsetAsync(pl.tl_p2l.p, 0xFF, (size_t) std::max<int64_t>(pl.n_hang, 1) * npe * sizeof(uint16_t), s));
   k_tile_build<<<(unsigned) n_tile, TB_THREADS, smem, s>>>(1, pl.e2n.p, pl.info.p, pl.hidx.p, pl.p2n.p, pl.n_leaf,
                                                           npe, T, cap, node_tiles.p, cnt.p, pl.tl_off.p,
-                                                          pl.tl_nodes.p, pl.tl_e2l.p, p2l.p,
+                                                          pl.tl_nodes.p, pl.tl_e2l.p, pl.tl_p2l.p,
                                                           pl.fx_kappa > 0 ? pl.fx_lam.p : nullptr);
   check_launch("tile_fill");
+  pl.tl_fm.alloc(std::max<int64_t>(pl.n_hang, 1));
+  k_tile_fmask<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.info.p, pl.hidx.p, pl.fill.p, pl.n_leaf, npe, pl.tl_fm.p);
   pl.tl_lstart.alloc(n_tile + 1);
   k_tile_lstart<<<grid_for(n_tile + 1), 256, 0, s>>>(pl.tl_lstart.p, n_tile, T, pl.n_leaf);
-  // hanging-node slots
-  std::vector<int64_t> hso(n_tile + 1, 0);
-  DBuf<int> err(1);
-  DKT_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-  auto kb = npe == 16 ? k_hns_build<16> : npe == 8 ? k_hns_build<8> : k_hns_build<4>;
-  const size_t hsm = (size_t) hcap * sizeof(uint64_t);
-  if (hns && pl.tl_n_hleaf > 0) {
-    ensure_dyn_smem(kb, hsm);
-    kb<<<(unsigned) n_tile, HB_THREADS, hsm, s>>>(0, pl.info.p, pl.hidx.p, pl.tl_lstart.p, pl.tl_off.p, pl.tl_e2l.p,
-                                                   p2l.p, hcap, cnt.p, nullptr, nullptr, nullptr, err.p);
-    check_launch("hns_count");
-    DKT_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_tile * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    DKT_CUDA(cudaStreamSynchronize(s));
-    for (int64_t t = 0; t < n_tile; t++) hso[t + 1] = hso[t] + hc[t];
-  }
-  uint32_t umax = 0, hmax = 0;
-  for (int64_t t = 0; t < n_tile; t++) {
-    umax = std::max<uint32_t>(umax, (uint32_t) (ho[t + 1] - ho[t] + hso[t + 1] - hso[t]));
-    hmax = std::max<uint32_t>(hmax, (uint32_t) (hso[t + 1] - hso[t]));
-  }
-  // U + H + TL_SINKS below TL_NONE keeps every local index clear of it
-  if ((int64_t) umax + TL_SINKS >= (int64_t) TL_NONE) throw std::invalid_argument("tile too large");
-  pl.tl_hs_off.upload(hso.data(), hso.size(), s);
-  pl.tl_n_hs = hso[n_tile];
-  pl.tl_hs_def.alloc((size_t) std::max<int64_t>(pl.tl_n_hs, 1) * 8);
-  pl.tl_hs_p.alloc((size_t) std::max<int64_t>(pl.tl_n_hs, 1));
-  if (pl.tl_n_hs > 0) {
-    kb<<<(unsigned) n_tile, HB_THREADS, hsm, s>>>(1, pl.info.p, pl.hidx.p, pl.tl_lstart.p, pl.tl_off.p, pl.tl_e2l.p,
-                                                   p2l.p, hcap, cnt.p, pl.tl_hs_off.p, pl.tl_hs_def.p, pl.tl_hs_p.p,
-                                                   err.p);
-    check_launch("hns_fill");
-  }
-  int herr = 0;
-  DKT_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  DKT_CUDA(cudaStreamSynchronize(s));
-  if (herr) throw std::runtime_error("hanging-node slot build: a face without two opposite nodes");
-  k_tile_sinks<<<(unsigned) n_tile, T, 0, s>>>(pl.tl_e2l.p, pl.tl_lstart.p, pl.tl_off.p, pl.tl_hs_off.p, npe);
+  pl.tl_hb.alloc(n_tile + 1);
+  k_tile_ranks<<<(unsigned) n_tile, T, 0, s>>>(pl.info.p, pl.hidx.p, pl.tl_lstart.p, pl.tl_hb.p);
+  // U <= 2 T npe <= 32768 (T <= 1024, npe <= 16), so U + TL_SINKS stays clear of TL_NONE
+  k_tile_sinks<<<(unsigned) n_tile, T, 0, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.hidx.p, pl.tl_lstart.p,
+                                               pl.tl_off.p, npe);
   pl.tl_tau.alloc(n_tile);
   k_tile_tau<<<(unsigned) n_tile, T, 0, s>>>(pl.info.p, pl.tl_lstart.p, pl.tl_tau.p);
   check_launch("tile_masks");
@@ -539,7 +364,6 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   pl.tl_T = T;
   pl.tl_n = n_tile;
   pl.tl_umax = umax;
-  pl.tl_hmax = hmax;
   pl.tl_sum_u = ho[n_tile];
   pl.tl_ready = true;
 }
@@ -666,28 +490,66 @@ __device__ __forceinline__ long long sar_lt32(long long v, uint32_t s)
   return (long long) (((unsigned long long) rhi << 32) | rlo);
 }
 
+// v[k] <- sum over the subsets j of k of v[j] (integers; two axes per pass,
+// each output of a pass at most one three-input sum)
+template <int DIM, typename T>
+__device__ __forceinline__ void subset_sums(T (&v)[1 << DIM])
+{
+  constexpr int D2 = DIM / 2 * 2;
+#pragma unroll
+  for (int d = 0; d < D2; d += 2)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (3 << d))) {
+        const int i1 = 1 << d, i2 = 2 << d;
+        const T a = v[k], b = v[k | i1], c = v[k | i2], e = v[k | i1 | i2];
+        const T t = a + b;
+        v[k | i1] = t;
+        v[k | i2] = a + c;
+        v[k | i1 | i2] = t + c + e;
+      }
+#pragma unroll
+  for (int d = D2; d < DIM; d++)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (1 << d))) v[k | (1 << d)] += v[k];
+}
+// v[j] <- sum over the supersets k of j of v[k]
+template <int DIM, typename T>
+__device__ __forceinline__ void superset_sums(T (&v)[1 << DIM])
+{
+  constexpr int D2 = DIM / 2 * 2;
+#pragma unroll
+  for (int d = 0; d < D2; d += 2)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (3 << d))) {
+        const int i1 = 1 << d, i2 = 2 << d;
+        const T a = v[k], b = v[k | i1], c = v[k | i2], e = v[k | i1 | i2];
+        const T t = b + e;
+        v[k | i1] = t;
+        v[k | i2] = c + e;
+        v[k] = t + a + c;
+      }
+#pragma unroll
+  for (int d = D2; d < DIM; d++)
+#pragma unroll
+    for (int k = 0; k < (1 << DIM); k++)
+      if (!(k & (1 << d))) v[k] += v[k | (1 << d)];
+}
+
 // A thread's node slots of the tile are visited in groups of four, the four
 // id loads issued before anything that depends on them: one global round trip
 // per group for the ids and one for the values, instead of two per slot.
 constexpr int TILE_G = 4;
 
-// The tile's node values into shared memory (and its node entries into sid
-// for the flush), its slot definitions into srow / sp (loads issued first,
-// independent of the node loads), sums zeroed.
 template <int T_LEAVES, typename V, typename ACC>
-__device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, int H,
-                                            int Us, const V *__restrict__ xq, V *xs, uint32_t *ys, uint32_t *sid,
-                                            int64_t hs0, const uint16_t *__restrict__ hs_def,
-                                            const uint8_t *__restrict__ hs_p, uint4 *srow, uint8_t *sp)
+__device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, int Us,
+                                            const V *__restrict__ xq, V *xs, uint32_t *ys)
 {
-  for (int q = threadIdx.x; q < H; q += T_LEAVES) {
-    srow[q] = __ldg(reinterpret_cast<const uint4 *>(hs_def) + hs0 + q);
-    sp[q] = hs_p[hs0 + q];
-  }
-  // the hanging-node slots and the sinks: sums zeroed, sinks read 0
-  for (int u = U + threadIdx.x; u < Us; u += T_LEAVES) {
-    if (u >= U + H) xs[u] = V(0);
-    ACC::zero(ys, Us, u);
+  if (threadIdx.x < TL_SINKS) {
+    xs[U + threadIdx.x] = V(0);
+    ACC::zero(ys, Us, U + threadIdx.x);
   }
   for (int b = threadIdx.x; b < U; b += TILE_G * T_LEAVES) {
     uint32_t id[TILE_G];
@@ -695,16 +557,15 @@ __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_no
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) {
       const int u = b + j * T_LEAVES;
-      id[j] = u < U ? __ldg(tile_nodes + u0 + u) : 0u;
+      id[j] = u < U ? __ldg(tile_nodes + u0 + u) & TL_ID : 0u;
     }
 #pragma unroll
-    for (int j = 0; j < TILE_G; j++) xv[j] = b + j * T_LEAVES < U ? __ldg(xq + (id[j] & TL_ID)) : V(0);
+    for (int j = 0; j < TILE_G; j++) xv[j] = b + j * T_LEAVES < U ? __ldg(xq + id[j]) : V(0);
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) {
       const int u = b + j * T_LEAVES;
       if (u < U) {
         xs[u] = xv[j];
-        sid[u] = id[j];
         ACC::zero(ys, Us, u);
       }
     }
@@ -712,57 +573,20 @@ __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_no
 }
 
 // The tile's sums out: stored where the tile is the node's only toucher,
-// added atomically elsewhere.  put(id, u) writes slot u to node id (the
-// node entries staged in sid by the gather).
+// added atomically elsewhere.  put(id, u) writes slot u to node id.
 template <int T_LEAVES, typename PUT>
-__device__ __forceinline__ void tile_scatter(const uint32_t *sid, int U, PUT put)
+__device__ __forceinline__ void tile_scatter(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, PUT put)
 {
-  for (int u = threadIdx.x; u < U; u += T_LEAVES) put(sid[u], u);
-}
-
-// The 2^p corners of a slot (local indices packed two to a word), one
-// unrolled body per p: a tile's slots come sorted by p, so the warps of a
-// slot phase mostly take one branch.
-template <int P, typename F>
-__device__ __forceinline__ void for_corners(const uint32_t (&cw)[4], F f)
-{
+  for (int b = threadIdx.x; b < U; b += TILE_G * T_LEAVES) {
+    uint32_t id[TILE_G];
 #pragma unroll
-  for (int c = 0; c < (1 << P); c++) f((cw[c >> 1] >> ((c & 1) * 16)) & 0xFFFFu);
-}
-template <int DIM, typename F>
-__device__ __forceinline__ void corners_of(int p, const uint32_t (&cw)[4], F f)
-{
-  if (p == 1) for_corners<1>(cw, f);
-  if constexpr (DIM >= 3) if (p == 2) for_corners<2>(cw, f);
-  if constexpr (DIM >= 4) if (p == 3) for_corners<3>(cw, f);
-}
-
-// Hanging-node slot values: the mean of each slot's face corners (2^p of
-// them, 1 <= p < DIM; a corner with no node is a sink and reads 0).  The
-// slot definitions are staged in shared memory (srow, sp) by the gather.
-template <int DIM, int T_LEAVES, bool FX, typename V>
-__device__ __forceinline__ void slot_means(V *xs, int U, int H, const uint4 *srow, const uint8_t *sp)
-{
-  for (int q = threadIdx.x; q < H; q += T_LEAVES) {
-    const int p = sp[q];
-    const uint4 rw = srow[q];
-    const uint32_t cw[4] = {rw.x, rw.y, rw.z, rw.w};
-    V acc = V(0);
-    corners_of<DIM>(p, cw, [&](uint32_t c) { acc += xs[c]; });
-    if constexpr (FX) xs[U + q] = acc >> p;
-    else xs[U + q] = acc * (1.0f / (float) (1 << p));
-  }
-}
-
-// Each slot's sum to every corner of its face (the transposed interpolation).
-template <int DIM, int T_LEAVES, typename ADD>
-__device__ __forceinline__ void slot_sums_out(int U, int H, const uint4 *srow, const uint8_t *sp, ADD add)
-{
-  for (int q = threadIdx.x; q < H; q += T_LEAVES) {
-    const int p = sp[q];
-    const uint4 rw = srow[q];
-    const uint32_t cw[4] = {rw.x, rw.y, rw.z, rw.w};
-    add(U + q, [&](auto put) { corners_of<DIM>(p, cw, put); });
+    for (int j = 0; j < TILE_G; j++) {
+      const int u = b + j * T_LEAVES;
+      id[j] = u < U ? __ldg(tile_nodes + u0 + u) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < TILE_G; j++)
+      if (b + j * T_LEAVES < U) put(id[j], b + j * T_LEAVES);
   }
 }
 
@@ -770,26 +594,22 @@ __device__ __forceinline__ void slot_sums_out(int U, int H, const uint4 *srow, c
 // tile's unit (fm: the per-unit factor table); 1, 2, 3 = dyadic scaling with
 // the Laplacian term (bit 0) and / or the mass term (bit 1), fm then pointing
 // at the per-level shift words.
-// One tile (one CTA's work); uniform exits only.  Every hanging leaf handled
-// here reads hanging-node slots; the other hanging leaves (info bit 28 clear)
-// are the per-leaf kernel's, and their threads idle.
+// One tile (one CTA's work); uniform exits only.
 template <int DIM, int T_LEAVES, typename AR, int SC>
 __device__ __forceinline__ void q1t_tile(
-    const int64_t tile, const uint16_t *__restrict__ e2l, const uint32_t *__restrict__ info,
-    const int64_t *__restrict__ tile_off, const int64_t *__restrict__ tile_ls,
-    const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm, int n_fac,
-    const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq, int conforming,
-    const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi, const int *__restrict__ skip_mesh,
-    int skip_stride, const DyConst &dyc, const uint8_t *__restrict__ tile_tau, int kappa,
-    const int64_t *__restrict__ hs_off, const uint16_t *__restrict__ hs_def, const uint8_t *__restrict__ hs_p,
-    int smax, int hmax)
+    const int64_t tile,
+    const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
+    const int64_t *__restrict__ tile_hb, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
+    const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
+    int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
+    const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
+    int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
+    const int *__restrict__ skip_mesh, int skip_stride, const DyConst &dyc,
+    const uint8_t *__restrict__ tile_tau, int kappa)
 {
   using V = typename AR::T;
   using F = typename AR::Factor;
   constexpr int NPE = 1 << DIM;
-  constexpr bool FX = std::is_same<AR, FixedArith>::value;
-  static_assert(FX || SC == 0, "dyadic scaling is a fixed-point form");
-  using ACC = TileAcc<AR>;
   extern __shared__ __align__(16) unsigned char smem[];
   // a batched solve: tiles whose meshes have all converged are not needed
   if (skip_mesh && skip_mesh[(int64_t) tile_mlo[tile] * skip_stride] &&
@@ -797,50 +617,77 @@ __device__ __forceinline__ void q1t_tile(
     return;
   const int64_t u0 = tile_off[tile];
   const int U = (int) (tile_off[tile + 1] - u0);
-  const int64_t hs0 = hs_off[tile];
-  const int H = (int) (hs_off[tile + 1] - hs0);
   const int64_t i = tile_ls[tile] + threadIdx.x;
   bool valid = i < tile_ls[tile + 1];
   // the leaf's records first, so their latency overlaps the node gather
-  uint32_t inf = 0;
-  uint32_t w[NPE / 2];
+  uint32_t inf = 0, fmask = 0xFFFFFFFFu;
+  uint32_t w[NPE / 2], pw[NPE / 2];
+  int64_t h = -1;
   if (valid) {
     inf = __ldg(info + i);
-    if (((inf >> 16) & 1u) && !(inf & INFO_HNS)) valid = false;
+    if (skip_stale && ((inf >> 27) & 1u)) valid = false;   // done after the stale chain
   }
-  if (valid) load_row16<NPE>(e2l + i * NPE, w);
-  const bool hang = valid && ((inf >> 16) & 1u);
+  if (valid) {
+    load_row16<NPE>(e2l + i * NPE, w);
+    if ((inf >> 16) & 1u) {
+      h = tile_hb[tile] + ((inf >> 17) & 0x3FFu);
+      fmask = __ldg(fmask_r + h);
+      load_row16<NPE>(p2l + h * NPE, pw);
+    }
+  }
+  using ACC = TileAcc<AR>;
+  constexpr bool FX = std::is_same<AR, FixedArith>::value;
+  static_assert(FX || SC == 0, "dyadic scaling is a fixed-point form");
   F *fac = reinterpret_cast<F *>(smem);
   uint32_t *fsh = reinterpret_cast<uint32_t *>(smem);     // SC != 0: per-level shift words
-  const int Us = U + H + TL_SINKS;                        // the tile's nodes, its slots, the sinks
+  const int Us = U + TL_SINKS;                            // the tile's nodes, then the sinks
   const int fac_bytes = SC ? ((n_fac * 4 + 15) & ~15) : n_fac * (int) sizeof(F);
   V *xs = reinterpret_cast<V *>(smem + fac_bytes);
   uint32_t *ys = reinterpret_cast<uint32_t *>(xs + Us);  // ACC::WORDS words per entry
-  // staged slot definitions, past the largest tile's node and slot sums
-  uint4 *srow = reinterpret_cast<uint4 *>(smem + ((fac_bytes + (size_t) 2 * smax * sizeof(V) + 15) & ~(size_t) 15));
-  uint32_t *sid = reinterpret_cast<uint32_t *>(srow + hmax);   // the tile's node entries
-  uint8_t *sp = reinterpret_cast<uint8_t *>(sid + smax);
   // the tile's fixed-point unit: its coarsest leaf level (factor table row)
   const int tau = FX ? (int) tile_tau[tile] : 0;
   for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) {
     if constexpr (SC != 0) fsh[k] = static_cast<const uint32_t *>(fm)[k];
     else fac[k] = AR::load_factor(fm, tau * n_fac + k);
   }
-  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, H, Us, xq, xs, ys, sid, hs0, hs_def, hs_p, srow, sp);
+  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, Us, xq, xs, ys);
   __shared__ uint32_t s_max;
   if (threadIdx.x == 0) s_max = 0u;
   __syncthreads();
-  if (H > 0) {
-    slot_means<DIM, T_LEAVES, FX, V>(xs, U, H, srow, sp);
-    __syncthreads();
-  }
-  auto lidx = [&](int k) -> uint32_t { return idx16<NPE>(w, k); };
-  V v[NPE];
+  V v[NPE], zt[std::is_same<AR, FixedArith>::value ? 1 : NPE];
   if (valid) {
     const int L = inf & 0xFFu;
-    // a hanging leaf's unfilled ranks read their slots (the parent-face means)
+    const bool hang = h >= 0;
+    auto lidx = [&](int k) -> uint32_t { return idx16<NPE>(w, k); };
+    if (hang) {
+      const int c = (int) ((inf >> 8) & 0xFFu);
+      const int32_t hz = hzoff ? __ldg(hzoff + h) : -1;
 #pragma unroll
-    for (int k = 0; k < NPE; k++) v[k] = xs[lidx(k)];
+      for (int k = 0; k < NPE; k++) v[k] = xs[idx16<NPE>(pw, k)];   // a sink reads 0
+      if (hz >= 0) {
+        // the parent slots with no node read the emulated static buffer
+#pragma unroll
+        for (int k = 0; k < NPE; k++)
+          if (idx16<NPE>(pw, k) >= (uint32_t) U) {
+            const int32_t id = __ldg(hztab + (int64_t) hz * NPE + (k ^ c));
+            if (id >= 0) v[k] = __ldg(stvq + id);
+          }
+      }
+      // parent -> child-0 interpolation: rank k takes the mean of the parent
+      // values on the subsets of k (the sum, then one shift or scaling)
+      subset_sums<DIM, V>(v);
+#pragma unroll
+      for (int k = 1; k < NPE; k++) {
+        if constexpr (FX) v[k] >>= __popc(k);
+        else v[k] *= 1.0f / (float) (1 << __popc(k));
+      }
+#pragma unroll
+      for (int k = 0; k < NPE; k++)
+        if ((fmask >> k) & 1u) v[k] = xs[lidx(k)];
+    } else {
+#pragma unroll
+      for (int k = 0; k < NPE; k++) v[k] = xs[lidx(k)];
+    }
     wht<DIM, V>(v);
     if constexpr (SC == 0) {
 #pragma unroll
@@ -867,30 +714,30 @@ __device__ __forceinline__ void q1t_tile(
       }
     }
     wht<DIM, V>(v);
-    // a hanging leaf's unfilled ranks (their local index is a slot's): the
-    // transposed interpolation weight 2^-popcount, into the slot
-    if constexpr (FX) {
-      // the reference transpose leaves out the shared parent corner (rank 0
-      // is always filled), which the slots' sums reach: the leaf's share is
-      // taken back at its rank-0 node, the same corner, added last
-      const bool back_out = hang && !conforming;
-      V back = V(0);
+    if constexpr (std::is_same<AR, FixedArith>::value) {
 #pragma unroll
-      for (int k = 1; k < NPE; k++) {
-        if (hang && lidx(k) >= (uint32_t) U) {
-          v[k] >>= __popc(k);
-          if (back_out) back += v[k];
+      for (int k = 0; k < NPE; k++) ACC::add(ys, Us, lidx(k), v[k]);
+      if (hang) {
+        // transpose of the child-0 interpolation on the unfilled ranks, into
+        // the parent nodes: parent rank j takes the sum over the supersets k
+        // of j of v[k] / 2^popcount(k)
+#pragma unroll
+        for (int k = 0; k < NPE; k++) v[k] = ((fmask >> k) & 1u) ? V(0) : (v[k] >> __popc(k));
+        superset_sums<DIM, V>(v);
+#pragma unroll
+        for (int k = 0; k < NPE; k++) {
+          const uint32_t p = idx16<NPE>(pw, k);
+          if (conforming || !((fmask >> k) & 1u)) ACC::add(ys, Us, p, v[k]);
         }
-        ACC::add(ys, Us, lidx(k), v[k]);
       }
-      ACC::add(ys, Us, lidx(0), v[0] - back);
-    } else if (hang) {
+    } else {
 #pragma unroll
-      for (int k = 1; k < NPE; k++)
-        if (lidx(k) >= (uint32_t) U) v[k] *= 1.0f / (float) (1 << __popc(k));
+      for (int k = 0; k < NPE; k++)
+        zt[k] = ((fmask >> k) & 1u) || !hang ? V(0) : v[k] * (1.0f / (float) (1 << __popc(k)));
+      if (hang) superset_sums<DIM, V>(zt);
     }
   }
-  if constexpr (!FX) {
+  if constexpr (!std::is_same<AR, FixedArith>::value) {
     // binary32: the tile's contributions are quantised against the tile's
     // largest one (22 bits) and summed with native integer shared atomics;
     // each node's sum goes out with one float atomic.  The rounding to an
@@ -900,8 +747,10 @@ __device__ __forceinline__ void q1t_tile(
     float m = 0.0f;
     if (valid) {
 #pragma unroll
-      for (int k = 0; k < NPE; k++)
-        if (lidx(k) < (uint32_t) (U + H)) m = fmaxf(m, fabsf(v[k]));
+      for (int k = 0; k < NPE; k++) {
+        if (idx16<NPE>(w, k) < (uint32_t) U) m = fmaxf(m, fabsf(v[k]));
+        m = fmaxf(m, fabsf(zt[k]));
+      }
     }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(&s_max, __float_as_uint(m));
@@ -911,32 +760,22 @@ __device__ __forceinline__ void q1t_tile(
     const float up = ldexpf(1.0f, 22 - e);
     auto quant = [up](float v) { return __float_as_int(fmaf(v, up, 12582912.0f)) - 0x4B400000; };
     if (valid) {
-      // the shared parent corner's share taken back at rank 0 (reference
-      // traversal), in integers
-      const bool back_out = hang && !conforming;
-      int back = 0, q0 = 0;
 #pragma unroll
       for (int k = 0; k < NPE; k++) {
-        const int qv = quant(v[k]);
-        if (k == 0) {
-          q0 = qv;
-        } else {
-          if (back_out && lidx(k) >= (uint32_t) U) back += qv;
-          atomicAdd(reinterpret_cast<int *>(ys) + lidx(k), qv);
+        atomicAdd(reinterpret_cast<int *>(ys) + idx16<NPE>(w, k), quant(v[k]));
+      }
+      if (h >= 0) {
+#pragma unroll
+        for (int k = 0; k < NPE; k++) {
+          const uint32_t p = idx16<NPE>(pw, k);
+          if (conforming || !((fmask >> k) & 1u))
+            atomicAdd(reinterpret_cast<int *>(ys) + p, quant(zt[k]));
         }
       }
-      atomicAdd(reinterpret_cast<int *>(ys) + lidx(0), q0 - back);
     }
     __syncthreads();
-    if (H > 0) {
-      slot_sums_out<DIM, T_LEAVES>(U, H, srow, sp, [&](int u, auto each) {
-        const int a = reinterpret_cast<const int *>(ys)[u];
-        if (a != 0) each([&](uint32_t c) { atomicAdd(reinterpret_cast<int *>(ys) + c, a); });
-      });
-      __syncthreads();
-    }
     const float down = ldexpf(1.0f, e - 22);
-    tile_scatter<T_LEAVES>(sid, U, [&](uint32_t id, int u) {
+    tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
       const int a = reinterpret_cast<const int *>(ys)[u];
       if (id & TL_EXCL) yq[id & TL_ID] = (V) a * down;
       else if (a != 0) atomicAdd(yq + (id & TL_ID), (V) a * down);
@@ -944,18 +783,11 @@ __device__ __forceinline__ void q1t_tile(
     return;
   }
   __syncthreads();
-  if (H > 0) {
-    slot_sums_out<DIM, T_LEAVES>(U, H, srow, sp, [&](int u, auto each) {
-      const V a = ACC::get(ys, Us, u);
-      if (a != V(0)) each([&](uint32_t c) { ACC::add(ys, Us, c, a); });
-    });
-    __syncthreads();
-  }
   // the tile's sums from its unit (level tau) to each node's (level lam):
   // a factor 2^(kappa (lam - tau)), lam >= tau for a node only this tile's
   // finer leaves touch, lam < tau for one that coarser leaves elsewhere touch
   const int ktau = kappa * tau;
-  tile_scatter<T_LEAVES>(sid, U, [&](uint32_t id, int u) {
+  tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
     V a = ACC::get(ys, Us, u);
     if constexpr (FX) {
       if (kappa > 0) {
@@ -975,18 +807,19 @@ __device__ __forceinline__ void q1t_tile(
 // meshes have converged are passed over as they are pulled.
 template <int DIM, int T_LEAVES, typename AR, int SC, bool PERSIST>
 __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
-    const uint16_t *__restrict__ e2l, const uint32_t *__restrict__ info, const int64_t *__restrict__ tile_off,
+    const uint16_t *__restrict__ e2l, const uint16_t *__restrict__ p2l, const uint32_t *__restrict__ info,
+    const int64_t *__restrict__ tile_hb, const uint32_t *__restrict__ fmask_r, const int64_t *__restrict__ tile_off,
     const int64_t *__restrict__ tile_ls, const uint32_t *__restrict__ tile_nodes, const void *__restrict__ fm,
-    int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq, int conforming,
-    const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi, const int *__restrict__ skip_mesh,
-    int skip_stride, const __grid_constant__ DyConst dyc, const uint8_t *__restrict__ tile_tau, int kappa,
-    unsigned long long *__restrict__ counter, int64_t n_tile, const int64_t *__restrict__ hs_off,
-    const uint16_t *__restrict__ hs_def, const uint8_t *__restrict__ hs_p, int smax, int hmax)
+    int n_fac, const typename AR::T *__restrict__ xq, typename AR::T *__restrict__ yq,
+    const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
+    int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
+    const int *__restrict__ skip_mesh, int skip_stride, const __grid_constant__ DyConst dyc,
+    const uint8_t *__restrict__ tile_tau, int kappa, unsigned long long *__restrict__ counter, int64_t n_tile)
 {
   if constexpr (!PERSIST) {
-    q1t_tile<DIM, T_LEAVES, AR, SC>(blockIdx.x, e2l, info, tile_off, tile_ls, tile_nodes, fm, n_fac, xq, yq,
-                                    conforming, tile_mlo, tile_mhi, skip_mesh, skip_stride, dyc, tile_tau, kappa,
-                                    hs_off, hs_def, hs_p, smax, hmax);
+    q1t_tile<DIM, T_LEAVES, AR, SC>(blockIdx.x, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm,
+                                    n_fac, xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi,
+                                    skip_mesh, skip_stride, dyc, tile_tau, kappa);
     return;
   } else {
   __shared__ long long s_tile;
@@ -996,16 +829,18 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const int64_t t = s_tile;
     __syncthreads();                 // every thread has read s_tile
     if (t >= n_tile) return;
-    q1t_tile<DIM, T_LEAVES, AR, SC>(t, e2l, info, tile_off, tile_ls, tile_nodes, fm, n_fac, xq, yq, conforming,
-                                    tile_mlo, tile_mhi, skip_mesh, skip_stride, dyc, tile_tau, kappa, hs_off,
-                                    hs_def, hs_p, smax, hmax);
+    q1t_tile<DIM, T_LEAVES, AR, SC>(t, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm, n_fac,
+                                    xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi, skip_mesh,
+                                    skip_stride, dyc, tile_tau, kappa);
     __syncthreads();                 // the tile's shared memory is free again
   }
   }
 }
 
 template <int DIM, int TL, typename AR, int SC>
-static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y, cudaStream_t s)
+static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y,
+                         const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
+                         cudaStream_t s)
 {
   // the persistent form is compiled for dims 2 and 3 (the batched meshes);
   // a 4D plan asking for it runs the plain grid
@@ -1020,11 +855,7 @@ static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, type
   // one row of the per-unit factor table, or the per-level shift words
   const int n_fac = SC ? pl.md + 1 : (pl.md + 1) * (1 << DIM);
   const size_t fac_bytes = SC ? (size_t) ((n_fac * 4 + 15) & ~15) : (size_t) n_fac * sizeof(typename AR::Factor);
-  // tl_umax: the largest U + H of a tile; then the staged slot definitions
-  // (16 + 1 bytes per slot of the tile with most) and node entries (4 bytes)
-  const int smax = (int) pl.tl_umax + TL_SINKS, hmax = (int) pl.tl_hmax;
-  const size_t smem = ((fac_bytes + (size_t) 2 * smax * sizeof(typename AR::T) + 15) & ~(size_t) 15) +
-                      (size_t) hmax * 17 + (size_t) smax * 4;
+  const size_t smem = fac_bytes + (size_t) 2 * (pl.tl_umax + TL_SINKS) * sizeof(typename AR::T);
   ensure_dyn_smem(kfn, smem);
   unsigned grid = (unsigned) pl.tl_n;
   unsigned long long *counter = nullptr;
@@ -1038,18 +869,21 @@ static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, type
     counter = pl.tl_counter.p;
     DKT_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
   }
-  kfn<<<grid, TL, smem, s>>>(pl.tl_e2l.p, pl.info.p, pl.tl_off.p, pl.tl_lstart.p, pl.tl_nodes.p, fm, n_fac, x, y,
-                             pl.conforming ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p, pl.tl_mlo.p ? pl.skip_mesh : nullptr,
-                             pl.skip_stride, dyc, pl.tl_tau.p,
-                             std::is_same<AR, FixedArith>::value ? pl.fx_kappa : 0, counter, pl.tl_n,
-                             pl.tl_hs_off.p, pl.tl_hs_def.p, pl.tl_hs_p.p, smax, hmax);
+  kfn<<<grid, TL, smem, s>>>(pl.tl_e2l.p, pl.tl_p2l.p, pl.info.p, pl.tl_hb.p, pl.tl_fm.p, pl.tl_off.p,
+                                           pl.tl_lstart.p, pl.tl_nodes.p, fm, n_fac, x, y, hzoff, hztab, stv,
+                                           pl.conforming ? 1 : 0, skip_stale ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p,
+                                           pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride, dyc, pl.tl_tau.p,
+                                           std::is_same<AR, FixedArith>::value ? pl.fx_kappa : 0, counter,
+                                           pl.tl_n);
 }
 
 template <typename AR, int SC>
-static void launch_tiled_dim(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y, cudaStream_t s)
+static void launch_tiled_dim(Plan &pl, const void *fm, const typename AR::T *x, typename AR::T *y,
+                             const int32_t *hzoff, const int32_t *hztab, const typename AR::T *stv, bool skip_stale,
+                             cudaStream_t s)
 {
 #define DKT_TL_CASE(D, TL) \
-  case (D) * 10000 + (TL): launch_tiled<D, TL, AR, SC>(pl, fm, x, y, s); break;
+  case (D) * 10000 + (TL): launch_tiled<D, TL, AR, SC>(pl, fm, x, y, hzoff, hztab, stv, skip_stale, s); break;
   switch (pl.dim * 10000 + pl.tl_T) {
     DKT_TL_CASE(2, 128) DKT_TL_CASE(2, 256) DKT_TL_CASE(2, 512)
     DKT_TL_CASE(3, 128) DKT_TL_CASE(3, 256) DKT_TL_CASE(3, 512)
@@ -1061,12 +895,14 @@ static void launch_tiled_dim(Plan &pl, const void *fm, const typename AR::T *x, 
   pl.n_launch++;
 }
 
-// Every leaf but the hanging leaves that read no hanging-node slots (the
-// per-leaf kernel's, over pl.tl_rest).
-void tiled_fixed(Plan &pl, cudaStream_t s)
+// skip_stale: leave the leaves that read stale slots to a later launch.  The
+// leaves that remain read no stale slot, so they need no look-up of one.
+void tiled_fixed(Plan &pl, bool skip_stale, cudaStream_t s)
 {
+  const int32_t *hz = (pl.st_ready && !skip_stale) ? pl.st_hzoff.p : nullptr;
   switch (pl.fx_scale) {
-#define DKT_SC_CASE(SC, FM) case SC: launch_tiled_dim<FixedArith, SC>(pl, FM, pl.xq.p, pl.yq.p, s); break;
+#define DKT_SC_CASE(SC, FM) \
+  case SC: launch_tiled_dim<FixedArith, SC>(pl, FM, pl.xq.p, pl.yq.p, hz, pl.st_hztab.p, pl.st_vq.p, skip_stale, s); break;
     DKT_SC_CASE(0, pl.fx_fm.p) DKT_SC_CASE(1, pl.fx_shift.p) DKT_SC_CASE(2, pl.fx_shift.p) DKT_SC_CASE(3, pl.fx_shift.p)
 #undef DKT_SC_CASE
     default: throw std::runtime_error("bad fixed-point scaling mode");
@@ -1075,7 +911,7 @@ void tiled_fixed(Plan &pl, cudaStream_t s)
 
 void tiled_f32(Plan &pl, const float *x, float *y, cudaStream_t s)
 {
-  launch_tiled_dim<F32Arith, 0>(pl, pl.f32_f.p, x, y, s);
+  launch_tiled_dim<F32Arith, 0>(pl, pl.f32_f.p, x, y, nullptr, nullptr, nullptr, false, s);
 }
 
 bool tile_size_supported(int dim, int T)

@@ -126,8 +126,7 @@ int dkt_plan_stats(dkt_plan plan, int64_t *out4);
 
 /* Extended counts, up to n of: leaves, hanging leaves, stale slots, boundary
  * nodes, stale-chain entries, stale-chain runs, longest run (hanging leaves),
- * longest run (entries), hanging-node slots of the tiles, hanging leaves that
- * read them.  Instrumentation, no reference counterpart. */
+ * longest run (entries).  Instrumentation, no reference counterpart. */
 int dkt_plan_stats_ex(dkt_plan plan, int64_t *out, int n);
 
 /* Host copy of the flattened traversal (for inspection and tests):
@@ -308,17 +307,6 @@ int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t 
  * result does not depend on it (fixed point: bitwise).  A tuning knob with no
  * reference counterpart; plans start with 256. */
 int dkt_plan_set_tile(dkt_plan plan, int tile_leaves);
-
-/* Hanging-node slots of the tiled Q1 kernel (enable = 1, the default): the
- * hanging leaves of a tile that meet at one hanging point read one shared
- * slot holding the parent-face mean, and the transposed interpolation is
- * sent from each slot to the face's corners once per tile, instead of every
- * leaf interpolating from and transposing into its parent's nodes.  Hanging
- * leaves that cannot use slots (those that read stale parent slots, among
- * others), and with enable = 0 every hanging leaf, run in the per-leaf
- * kernel after the tiled one.  The products agree to rounding.  A tuning
- * knob with no reference counterpart. */
-int dkt_plan_set_hanging_slots(dkt_plan plan, int enable);
 
 /* Number of kernels this plan's matrix-vector products and solves have
  * launched so far (cumulative; every kernel of the library, not only the
