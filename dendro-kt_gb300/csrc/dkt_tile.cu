@@ -543,9 +543,11 @@ __device__ __forceinline__ void superset_sums(T (&v)[1 << DIM])
 // per group for the ids and one for the values, instead of two per slot.
 constexpr int TILE_G = 4;
 
+// The tile's node values into shared memory, and its node entries into sid
+// for the flush; sums zeroed.
 template <int T_LEAVES, typename V, typename ACC>
 __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, int Us,
-                                            const V *__restrict__ xq, V *xs, uint32_t *ys)
+                                            const V *__restrict__ xq, V *xs, uint32_t *ys, uint32_t *sid)
 {
   if (threadIdx.x < TL_SINKS) {
     xs[U + threadIdx.x] = V(0);
@@ -557,15 +559,16 @@ __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_no
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) {
       const int u = b + j * T_LEAVES;
-      id[j] = u < U ? __ldg(tile_nodes + u0 + u) & TL_ID : 0u;
+      id[j] = u < U ? __ldg(tile_nodes + u0 + u) : 0u;
     }
 #pragma unroll
-    for (int j = 0; j < TILE_G; j++) xv[j] = b + j * T_LEAVES < U ? __ldg(xq + id[j]) : V(0);
+    for (int j = 0; j < TILE_G; j++) xv[j] = b + j * T_LEAVES < U ? __ldg(xq + (id[j] & TL_ID)) : V(0);
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) {
       const int u = b + j * T_LEAVES;
       if (u < U) {
         xs[u] = xv[j];
+        sid[u] = id[j];
         ACC::zero(ys, Us, u);
       }
     }
@@ -573,21 +576,12 @@ __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_no
 }
 
 // The tile's sums out: stored where the tile is the node's only toucher,
-// added atomically elsewhere.  put(id, u) writes slot u to node id.
+// added atomically elsewhere.  put(id, u) writes slot u to node id (the node
+// entries staged in sid by the gather).
 template <int T_LEAVES, typename PUT>
-__device__ __forceinline__ void tile_scatter(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, PUT put)
+__device__ __forceinline__ void tile_scatter(const uint32_t *sid, int U, PUT put)
 {
-  for (int b = threadIdx.x; b < U; b += TILE_G * T_LEAVES) {
-    uint32_t id[TILE_G];
-#pragma unroll
-    for (int j = 0; j < TILE_G; j++) {
-      const int u = b + j * T_LEAVES;
-      id[j] = u < U ? __ldg(tile_nodes + u0 + u) : 0u;
-    }
-#pragma unroll
-    for (int j = 0; j < TILE_G; j++)
-      if (b + j * T_LEAVES < U) put(id[j], b + j * T_LEAVES);
-  }
+  for (int u = threadIdx.x; u < U; u += T_LEAVES) put(sid[u], u);
 }
 
 // SC (fixed point only): 0 = per-(level, mode) multiply-high factors of the
@@ -605,7 +599,7 @@ __device__ __forceinline__ void q1t_tile(
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
     int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
     const int *__restrict__ skip_mesh, int skip_stride, const DyConst &dyc,
-    const uint8_t *__restrict__ tile_tau, int kappa)
+    const uint8_t *__restrict__ tile_tau, int kappa, int smax)
 {
   using V = typename AR::T;
   using F = typename AR::Factor;
@@ -644,13 +638,15 @@ __device__ __forceinline__ void q1t_tile(
   const int fac_bytes = SC ? ((n_fac * 4 + 15) & ~15) : n_fac * (int) sizeof(F);
   V *xs = reinterpret_cast<V *>(smem + fac_bytes);
   uint32_t *ys = reinterpret_cast<uint32_t *>(xs + Us);  // ACC::WORDS words per entry
+  // the tile's node entries, past the largest tile's values and sums
+  uint32_t *sid = reinterpret_cast<uint32_t *>(smem + fac_bytes + (size_t) 2 * smax * sizeof(V));
   // the tile's fixed-point unit: its coarsest leaf level (factor table row)
   const int tau = FX ? (int) tile_tau[tile] : 0;
   for (int k = threadIdx.x; k < n_fac; k += T_LEAVES) {
     if constexpr (SC != 0) fsh[k] = static_cast<const uint32_t *>(fm)[k];
     else fac[k] = AR::load_factor(fm, tau * n_fac + k);
   }
-  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, Us, xq, xs, ys);
+  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, Us, xq, xs, ys, sid);
   __shared__ uint32_t s_max;
   if (threadIdx.x == 0) s_max = 0u;
   __syncthreads();
@@ -775,7 +771,7 @@ __device__ __forceinline__ void q1t_tile(
     }
     __syncthreads();
     const float down = ldexpf(1.0f, e - 22);
-    tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
+    tile_scatter<T_LEAVES>(sid, U, [&](uint32_t id, int u) {
       const int a = reinterpret_cast<const int *>(ys)[u];
       if (id & TL_EXCL) yq[id & TL_ID] = (V) a * down;
       else if (a != 0) atomicAdd(yq + (id & TL_ID), (V) a * down);
@@ -787,7 +783,7 @@ __device__ __forceinline__ void q1t_tile(
   // a factor 2^(kappa (lam - tau)), lam >= tau for a node only this tile's
   // finer leaves touch, lam < tau for one that coarser leaves elsewhere touch
   const int ktau = kappa * tau;
-  tile_scatter<T_LEAVES>(tile_nodes, u0, U, [&](uint32_t id, int u) {
+  tile_scatter<T_LEAVES>(sid, U, [&](uint32_t id, int u) {
     V a = ACC::get(ys, Us, u);
     if constexpr (FX) {
       if (kappa > 0) {
@@ -814,12 +810,13 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
     int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
     const int *__restrict__ skip_mesh, int skip_stride, const __grid_constant__ DyConst dyc,
-    const uint8_t *__restrict__ tile_tau, int kappa, unsigned long long *__restrict__ counter, int64_t n_tile)
+    const uint8_t *__restrict__ tile_tau, int kappa, unsigned long long *__restrict__ counter, int64_t n_tile,
+    int smax)
 {
   if constexpr (!PERSIST) {
     q1t_tile<DIM, T_LEAVES, AR, SC>(blockIdx.x, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm,
                                     n_fac, xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi,
-                                    skip_mesh, skip_stride, dyc, tile_tau, kappa);
+                                    skip_mesh, skip_stride, dyc, tile_tau, kappa, smax);
     return;
   } else {
   __shared__ long long s_tile;
@@ -831,7 +828,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     if (t >= n_tile) return;
     q1t_tile<DIM, T_LEAVES, AR, SC>(t, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm, n_fac,
                                     xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi, skip_mesh,
-                                    skip_stride, dyc, tile_tau, kappa);
+                                    skip_stride, dyc, tile_tau, kappa, smax);
     __syncthreads();                 // the tile's shared memory is free again
   }
   }
@@ -855,7 +852,9 @@ static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, type
   // one row of the per-unit factor table, or the per-level shift words
   const int n_fac = SC ? pl.md + 1 : (pl.md + 1) * (1 << DIM);
   const size_t fac_bytes = SC ? (size_t) ((n_fac * 4 + 15) & ~15) : (size_t) n_fac * sizeof(typename AR::Factor);
-  const size_t smem = fac_bytes + (size_t) 2 * (pl.tl_umax + TL_SINKS) * sizeof(typename AR::T);
+  // values and sums of the largest tile (plus sinks), then its node entries
+  const int smax = (int) pl.tl_umax + TL_SINKS;
+  const size_t smem = fac_bytes + (size_t) 2 * smax * sizeof(typename AR::T) + (size_t) smax * sizeof(uint32_t);
   ensure_dyn_smem(kfn, smem);
   unsigned grid = (unsigned) pl.tl_n;
   unsigned long long *counter = nullptr;
@@ -874,7 +873,7 @@ static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, type
                                            pl.conforming ? 1 : 0, skip_stale ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p,
                                            pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride, dyc, pl.tl_tau.p,
                                            std::is_same<AR, FixedArith>::value ? pl.fx_kappa : 0, counter,
-                                           pl.tl_n);
+                                           pl.tl_n, smax);
 }
 
 template <typename AR, int SC>
