@@ -9,6 +9,9 @@ static-parent-buffer reads:
     relative (2-norm) of the oracle's restatement of fem::matvec;
   * level 6, Q2 (0.88 M elements, 278,400 stale slot reads): the
     sum-factorised kernel within 1e-12 of the oracle;
+  * level 6, Q1, on the Hilbert curve (the tree, the DA node order and the
+    stale-slot chain all follow the curve): DA and product against the
+    oracle run on the same curve tables;
   * level 8, Q1 (54.7 M elements, the benchmark's own workload), too large
     for the oracle to finish in a test: the fixed-point tiled product within
     1e-12 of the dense FP64 kernel (itself pinned to the oracle above and to
@@ -38,9 +41,11 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def _mesh(dkt, level, order):
+def _mesh(dkt, level, order, curve=None):
     tc, tl = dkt.moving_ball_tree(max_depth=MD, level=level, radius=0.2, halfwidth=2.0 ** -level, device=True)
-    return dkt.DA(tc, tl, 4, order=order, max_depth=MD)
+    if curve is None:
+        return dkt.DA(tc, tl, 4, order=order, max_depth=MD)
+    return dkt.DA(tc, tl, 4, order=order, max_depth=MD, curve=curve)
 
 
 def _product(A, x, arith):
@@ -53,8 +58,11 @@ def _product(A, x, arith):
     return yd.cpu().numpy()
 
 
-def _oracle(da, order):
-    orc.set_curve(4, MD)
+def _oracle(da, order, tables=None):
+    if tables is None:
+        orc.set_curve(4, MD)
+    else:
+        orc.set_curve(4, MD, *tables)
     orc.set_conforming(0)
     orc.set_stale_mode(0)
     sc, sl = da.tree()
@@ -81,6 +89,28 @@ def test_moving_ball_product_vs_oracle(dkt, level, order):
         y_dense = _product(A, x, dkt.ARITH_FP64)
         print("level %d: dense FP64 kernel vs oracle %.3e" % (level, _rel(y_dense, yo)))
         assert _rel(y_dense, yo) <= TOL
+
+
+def test_hilbert_moving_ball_product_vs_oracle(dkt):
+    da = _mesh(dkt, 6, 1, curve=dkt.CURVE_HILBERT)
+    A = dkt.Matrix(da, op=dkt.OP_LAPMASS)
+    st = A.stats()
+    assert st["stale_slots"] > 0
+    ora = _oracle(da, 1, tables=dkt.curve_tables(dkt.CURVE_HILBERT, 4))
+    try:
+        nc, nl = da.nodes()
+        assert np.array_equal(nc, ora.node_coords) and np.array_equal(nl, ora.node_levels)
+        assert np.array_equal(da.boundary_ids(), ora.bdry)
+        x = orc.uniform_pm1(3, da.n)
+        yo = ora.matvec(x)
+        assert ora.stats()["stale_reads"] == st["stale_slots"]
+    finally:
+        orc.set_curve(4, MD)
+    y_fast = _product(A, x, dkt.ARITH_AUTO)
+    y_dense = _product(A, x, dkt.ARITH_FP64)
+    print("hilbert level 6: fast %.3e dense %.3e" % (_rel(y_fast, yo), _rel(y_dense, yo)))
+    assert _rel(y_fast, yo) <= TOL
+    assert _rel(y_dense, yo) <= TOL
 
 
 def test_level8_fixed_point_vs_dense_fp64_and_linearity(dkt):
