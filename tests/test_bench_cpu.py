@@ -25,6 +25,10 @@ def _check(line):
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 2
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    # one product of the whole mesh is the step it times; the requested
+    # counts are echoed, not claimed
+    assert line["steps"] == 1 and line["warmup"] == 0
+    assert line["requested_steps"] == 1 and line["requested_warmup"] == 1
 
 
 def test_reference_arm_single_process():
