@@ -13,6 +13,7 @@
 namespace dkt {
 
 bool q1fx_setup(Plan &pl, cudaStream_t s);
+void tile_pad(Plan &pl, cudaStream_t s);
 bool q2sf_setup(Plan &pl, cudaStream_t s);
 
 __global__ void k_offset_ids(const int32_t *__restrict__ in, int32_t *__restrict__ out, int64_t n, int32_t base)
@@ -113,6 +114,8 @@ void batch_combine(const std::vector<const Plan *> &in, Plan &out, cudaStream_t 
   }
   if (a.tl_ready) {
     out.tl_T = a.tl_T; out.tl_n = nt; out.tl_sum_u = su; out.tl_umax = umax;
+    out.tl_ls_direct = false;
+    tile_pad(out, s);
     if (mlo.empty()) mlo.push_back(0);
     out.tl_mlo.upload(mlo.data(), mlo.size(), s);
     out.tl_mhi.upload(mlo.data(), mlo.size(), s);   // tiles of one plan never straddle meshes

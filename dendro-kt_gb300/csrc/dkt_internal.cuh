@@ -230,6 +230,13 @@ struct Plan {
   DBuf<uint32_t> tl_nodes, tl_fm;     // distinct nodes (| exclusive flag); reflected fill masks
   DBuf<uint16_t> tl_e2l, tl_p2l;
   DBuf<uint8_t> tl_tau;              // per tile: coarsest leaf level (its fixed-point unit)
+  // the node entries again at fixed stride tl_cap per tile (padded with node
+  // 0), and each tile's count: the leaf kernel reads a tile's entries without
+  // first reading its offset (one dependent global load fewer per tile)
+  DBuf<uint32_t> tl_pad;
+  DBuf<int32_t> tl_ucnt;
+  int tl_cap = 0;
+  bool tl_ls_direct = false;         // tile t's leaves start at t * tl_T (false: tl_lstart, a batch)
   // persistent tiled launch (CTAs pull tiles from a counter) instead of one
   // CTA per tile; chosen by dkt_plan_autotune
   bool tl_persist = false;

@@ -270,6 +270,27 @@ __global__ void k_tile_sinks(uint16_t *__restrict__ e2l, uint16_t *__restrict__ 
   }
 }
 
+// Tile t's node entries at t * cap (then node 0 up to cap) and its count.
+// One CTA per tile.
+__global__ void k_tile_pad(const int64_t *__restrict__ off, const uint32_t *__restrict__ nodes,
+                           uint32_t *__restrict__ pad, int32_t *__restrict__ ucnt, int cap)
+{
+  const int64_t t = blockIdx.x;
+  const int U = (int) (off[t + 1] - off[t]);
+  if (threadIdx.x == 0) ucnt[t] = U;
+  for (int u = threadIdx.x; u < cap; u += blockDim.x) pad[t * cap + u] = u < U ? nodes[off[t] + u] : 0u;
+}
+
+void tile_pad(Plan &pl, cudaStream_t s)
+{
+  const int cap = ((int) pl.tl_umax + 3) & ~3;
+  pl.tl_cap = cap;
+  pl.tl_pad.alloc((size_t) std::max<int64_t>(pl.tl_n, 1) * cap);
+  pl.tl_ucnt.alloc(std::max<int64_t>(pl.tl_n, 1));
+  if (pl.tl_n) k_tile_pad<<<(unsigned) pl.tl_n, 256, 0, s>>>(pl.tl_off.p, pl.tl_nodes.p, pl.tl_pad.p, pl.tl_ucnt.p, cap);
+  check_launch("tile_pad");
+}
+
 void tile_setup(Plan &pl, int T, cudaStream_t s)
 {
   pl.tl_ready = false;
@@ -364,6 +385,9 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   pl.tl_T = T;
   pl.tl_n = n_tile;
   pl.tl_umax = umax;
+  pl.tl_ls_direct = true;
+  tile_pad(pl, s);
+  DKT_CUDA(cudaStreamSynchronize(s));
   pl.tl_sum_u = ho[n_tile];
   pl.tl_ready = true;
 }
@@ -547,19 +571,21 @@ constexpr int TILE_G = 4;
 // for the flush; sums zeroed.
 template <int T_LEAVES, typename V, typename ACC>
 __device__ __forceinline__ void tile_gather(const uint32_t *__restrict__ tile_nodes, int64_t u0, int U, int Us,
-                                            const V *__restrict__ xq, V *xs, uint32_t *ys, uint32_t *sid)
+                                            const V *__restrict__ xq, V *xs, uint32_t *ys, uint32_t *sid, int cap)
 {
   if (threadIdx.x < TL_SINKS) {
     xs[U + threadIdx.x] = V(0);
     ACC::zero(ys, Us, U + threadIdx.x);
   }
-  for (int b = threadIdx.x; b < U; b += TILE_G * T_LEAVES) {
+  // the first round's entry loads stay within the tile's padded block
+  // (cap entries) and need not wait for U
+  for (int b = threadIdx.x; b < U || b == (int) threadIdx.x; b += TILE_G * T_LEAVES) {
     uint32_t id[TILE_G];
     V xv[TILE_G];
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) {
       const int u = b + j * T_LEAVES;
-      id[j] = u < U ? __ldg(tile_nodes + u0 + u) : 0u;
+      id[j] = u < cap ? __ldg(tile_nodes + u0 + u) : 0u;
     }
 #pragma unroll
     for (int j = 0; j < TILE_G; j++) xv[j] = b + j * T_LEAVES < U ? __ldg(xq + (id[j] & TL_ID)) : V(0);
@@ -599,7 +625,8 @@ __device__ __forceinline__ void q1t_tile(
     const int32_t *__restrict__ hzoff, const int32_t *__restrict__ hztab, const typename AR::T *__restrict__ stvq,
     int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
     const int *__restrict__ skip_mesh, int skip_stride, const DyConst &dyc,
-    const uint8_t *__restrict__ tile_tau, int kappa, int smax)
+    const uint8_t *__restrict__ tile_tau, int kappa, int smax, const uint32_t *__restrict__ pad,
+    const int32_t *__restrict__ ucnt, int cap, int64_t n_leaf, int ls_direct)
 {
   using V = typename AR::T;
   using F = typename AR::Factor;
@@ -609,10 +636,13 @@ __device__ __forceinline__ void q1t_tile(
   if (skip_mesh && skip_mesh[(int64_t) tile_mlo[tile] * skip_stride] &&
       skip_mesh[(int64_t) tile_mhi[tile] * skip_stride])
     return;
-  const int64_t u0 = tile_off[tile];
-  const int U = (int) (tile_off[tile + 1] - u0);
-  const int64_t i = tile_ls[tile] + threadIdx.x;
-  bool valid = i < tile_ls[tile + 1];
+  // the tile's node entries at tile * cap, its count beside them; its leaves
+  // at tile * T unless the plan is a batch (concatenated tiles)
+  (void) tile_off;
+  const int64_t u0 = tile * (int64_t) cap;
+  const int U = ucnt[tile];
+  const int64_t i = (ls_direct ? tile * (int64_t) T_LEAVES : tile_ls[tile]) + threadIdx.x;
+  bool valid = ls_direct ? i < n_leaf : i < tile_ls[tile + 1];
   // the leaf's records first, so their latency overlaps the node gather
   uint32_t inf = 0, fmask = 0xFFFFFFFFu;
   uint32_t w[NPE / 2], pw[NPE / 2];
@@ -646,7 +676,7 @@ __device__ __forceinline__ void q1t_tile(
     if constexpr (SC != 0) fsh[k] = static_cast<const uint32_t *>(fm)[k];
     else fac[k] = AR::load_factor(fm, tau * n_fac + k);
   }
-  tile_gather<T_LEAVES, V, ACC>(tile_nodes, u0, U, Us, xq, xs, ys, sid);
+  tile_gather<T_LEAVES, V, ACC>(pad, u0, U, Us, xq, xs, ys, sid, cap);
   __shared__ uint32_t s_max;
   if (threadIdx.x == 0) s_max = 0u;
   __syncthreads();
@@ -811,12 +841,14 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     int conforming, int skip_stale, const int32_t *__restrict__ tile_mlo, const int32_t *__restrict__ tile_mhi,
     const int *__restrict__ skip_mesh, int skip_stride, const __grid_constant__ DyConst dyc,
     const uint8_t *__restrict__ tile_tau, int kappa, unsigned long long *__restrict__ counter, int64_t n_tile,
-    int smax)
+    int smax, const uint32_t *__restrict__ pad, const int32_t *__restrict__ ucnt, int cap, int64_t n_leaf,
+    int ls_direct)
 {
   if constexpr (!PERSIST) {
     q1t_tile<DIM, T_LEAVES, AR, SC>(blockIdx.x, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm,
                                     n_fac, xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi,
-                                    skip_mesh, skip_stride, dyc, tile_tau, kappa, smax);
+                                    skip_mesh, skip_stride, dyc, tile_tau, kappa, smax, pad, ucnt, cap, n_leaf,
+                                    ls_direct);
     return;
   } else {
   __shared__ long long s_tile;
@@ -828,7 +860,7 @@ __global__ void __launch_bounds__(T_LEAVES, 1024 / T_LEAVES) k_matvec_q1t(
     if (t >= n_tile) return;
     q1t_tile<DIM, T_LEAVES, AR, SC>(t, e2l, p2l, info, tile_hb, fmask_r, tile_off, tile_ls, tile_nodes, fm, n_fac,
                                     xq, yq, hzoff, hztab, stvq, conforming, skip_stale, tile_mlo, tile_mhi, skip_mesh,
-                                    skip_stride, dyc, tile_tau, kappa, smax);
+                                    skip_stride, dyc, tile_tau, kappa, smax, pad, ucnt, cap, n_leaf, ls_direct);
     __syncthreads();                 // the tile's shared memory is free again
   }
   }
@@ -873,7 +905,8 @@ static void launch_tiled(Plan &pl, const void *fm, const typename AR::T *x, type
                                            pl.conforming ? 1 : 0, skip_stale ? 1 : 0, pl.tl_mlo.p, pl.tl_mhi.p,
                                            pl.tl_mlo.p ? pl.skip_mesh : nullptr, pl.skip_stride, dyc, pl.tl_tau.p,
                                            std::is_same<AR, FixedArith>::value ? pl.fx_kappa : 0, counter,
-                                           pl.tl_n, smax);
+                                           pl.tl_n, smax, pl.tl_pad.p, pl.tl_ucnt.p, pl.tl_cap, pl.n_leaf,
+                                           pl.tl_ls_direct ? 1 : 0);
 }
 
 template <typename AR, int SC>
