@@ -237,6 +237,7 @@ struct Plan {
   DBuf<int32_t> tl_ucnt;
   int tl_cap = 0;
   bool tl_ls_direct = false;         // tile t's leaves start at t * tl_T (false: tl_lstart, a batch)
+  DBuf<int32_t> leaf_sfc;            // position in the traversal's (SFC) order of each leaf record, once tiled
   // persistent tiled launch (CTAs pull tiles from a counter) instead of one
   // CTA per tile; chosen by dkt_plan_autotune
   bool tl_persist = false;

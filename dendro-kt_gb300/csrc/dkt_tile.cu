@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(TB_THREADS) k_tile_build(
 __global__ void k_tile_partition(const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info,
                                  const int32_t *__restrict__ hidx, int32_t *__restrict__ e2n_o,
                                  uint32_t *__restrict__ info_o, int32_t *__restrict__ hidx_o, int64_t n_leaf, int T,
-                                 int npe)
+                                 int npe, int32_t *__restrict__ sfc_o)
 {
   __shared__ uint32_t wc[32];
   const int64_t l0 = (int64_t) blockIdx.x * T;
@@ -170,6 +170,22 @@ __global__ void k_tile_partition(const int32_t *__restrict__ e2n, const uint32_t
   if (!valid) return;
   const int64_t j = l0 + (hang ? (int64_t) before : (int64_t) total + (threadIdx.x - before));
   (void) nl;
+  for (int k = 0; k < npe; k++) e2n_o[j * npe + k] = e2n[i * npe + k];
+  info_o[j] = info[i];
+  hidx_o[j] = hidx[i];
+  sfc_o[j] = (int32_t) i;   // the input is in traversal order
+}
+// Leaf records back to the traversal order (record i to position sfc[i]),
+// so that a plan tiled again is partitioned from that order: tiles then hold
+// consecutive leaves whatever tile sizes were tried before.
+__global__ void k_leaf_restore(const int32_t *__restrict__ e2n, const uint32_t *__restrict__ info,
+                               const int32_t *__restrict__ hidx, const int32_t *__restrict__ sfc,
+                               int32_t *__restrict__ e2n_o, uint32_t *__restrict__ info_o,
+                               int32_t *__restrict__ hidx_o, int64_t n_leaf, int npe)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_leaf) return;
+  const int64_t j = sfc[i];
   for (int k = 0; k < npe; k++) e2n_o[j * npe + k] = e2n[i * npe + k];
   info_o[j] = info[i];
   hidx_o[j] = hidx[i];
@@ -307,15 +323,26 @@ void tile_setup(Plan &pl, int T, cudaStream_t s)
   if (pl.seg.empty()) {
     // hanging leaves first within each tile (a single mesh: a batch keeps the
     // concatenated order of its meshes)
-    DBuf<int32_t> e2n_o((size_t) pl.n_leaf * npe), hidx_o(pl.n_leaf);
+    DBuf<int32_t> e2n_o((size_t) pl.n_leaf * npe), hidx_o(pl.n_leaf), sfc_o(pl.n_leaf);
     DBuf<uint32_t> info_o(pl.n_leaf);
+    if (pl.leaf_sfc.n == (size_t) pl.n_leaf) {
+      // tiled before: back to the traversal order first
+      k_leaf_restore<<<grid_for(pl.n_leaf), 256, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, pl.leaf_sfc.p, e2n_o.p,
+                                                         info_o.p, hidx_o.p, pl.n_leaf, npe);
+      check_launch("leaf_restore");
+      DKT_CUDA(cudaStreamSynchronize(s));
+      std::swap(pl.e2n, e2n_o);
+      std::swap(pl.info, info_o);
+      std::swap(pl.hidx, hidx_o);
+    }
     k_tile_partition<<<(unsigned) n_tile, T, 0, s>>>(pl.e2n.p, pl.info.p, pl.hidx.p, e2n_o.p, info_o.p, hidx_o.p,
-                                                     pl.n_leaf, T, npe);
+                                                     pl.n_leaf, T, npe, sfc_o.p);
     check_launch("tile_partition");
     DKT_CUDA(cudaStreamSynchronize(s));
     pl.e2n = std::move(e2n_o);
     pl.info = std::move(info_o);
     pl.hidx = std::move(hidx_o);
+    pl.leaf_sfc = std::move(sfc_o);
     if (pl.st_n_hleaf > 0) {
       // the leaves that read stale slots, renumbered
       DBuf<uint32_t> f(pl.n_leaf), pos(pl.n_leaf);

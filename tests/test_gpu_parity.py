@@ -386,11 +386,18 @@ def test_tiled_kernel_equals_untiled(dkt, dim):
     x = dkt.uniform_pm1(9, da.n)
     A.set_tile(0)
     y0 = _gpu_mv(A, x)
+    first = {}
     for T in sizes:
         A.set_tile(T)
         y = _gpu_mv(A, x)
         assert _rel(y, y0) <= 1e-13, T
         assert np.array_equal(_gpu_mv(A, x), y), T
+        first[T] = y
+    # re-tiling starts from the traversal order again: the same tiles, so
+    # bitwise the same product as the first time, whatever came in between
+    for T in reversed(sizes):
+        A.set_tile(T)
+        assert np.array_equal(_gpu_mv(A, x), first[T]), T
 
 
 def test_device_sphere_shell_equals_host(dkt):
