@@ -305,7 +305,7 @@ int dkt_plan_kernel_timing(dkt_plan plan, int enable, double *total_ms, int64_t 
  * (64/128/256 in 4D, 128/256/512 in 2D/3D) share one CTA, a per-tile list of
  * distinct nodes and 16-bit local maps; 0 selects the untiled kernel.  The
  * result does not depend on it (fixed point: bitwise).  A tuning knob with no
- * reference counterpart; plans start with 256. */
+ * reference counterpart; plans start with 128 in 4D and 256 in 2D and 3D. */
 int dkt_plan_set_tile(dkt_plan plan, int tile_leaves);
 
 /* Number of kernels this plan's matrix-vector products and solves have
