@@ -398,6 +398,7 @@ def run_batch(a, dkt, dev):
         x = torch.zeros_like(bd)
         B.pcg(bd, x, precision=prec, tol=1e-10, max_iter=32)       # warm-up
         x.zero_()
+        fin0 = B.stats()["fp64_finishes"]
         torch.cuda.synchronize(dev)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -411,6 +412,8 @@ def run_batch(a, dkt, dev):
                      "iterations_max": int(np.max(it))}
         if prec == dkt.PREC_MIXED:
             out[name]["refinements_max"] = int(np.max(ref))
+            out[name]["refinements_p50"] = float(np.percentile(ref, 50))
+            out[name]["fp64_finish"] = bool(B.stats()["fp64_finishes"] > fin0)
     out["mixed_over_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
     out["mixed_over_fp64_dense"] = out["fp64_dense"]["ms"] / out["mixed"]["ms"]
     return out

@@ -243,10 +243,11 @@ class Matrix:
         return self
 
     def stats(self):
-        s = np.zeros(8, np.int64)
-        _check(load().dkt_plan_stats_ex(self._h, _p(s), 8))
+        s = np.zeros(9, np.int64)
+        _check(load().dkt_plan_stats_ex(self._h, _p(s), 9))
         return dict(zip(["leaves", "hanging_leaves", "stale_slots", "boundary_nodes", "stale_entries",
-                         "stale_runs", "stale_longest_run", "stale_longest_run_entries"], s.tolist()))
+                         "stale_runs", "stale_longest_run", "stale_longest_run_entries", "fp64_finishes"],
+                        s.tolist()))
 
     def export(self):
         """The flattened traversal as numpy arrays (e2n, info, hidx, p2n, fill)."""

@@ -429,10 +429,10 @@ int dkt_plan_stats_ex(dkt_plan plan, int64_t *out, int n)
 {
   if (!plan || !out || n < 0) return fail(DKT_E_ARG, "bad argument");
   const dkt::Plan &pl = plan->pl;
-  const int64_t v[8] = {pl.n_leaf, pl.n_hang, pl.stale_slots, pl.n_bdry,
+  const int64_t v[9] = {pl.n_leaf, pl.n_hang, pl.stale_slots, pl.n_bdry,
                         pl.st_ready ? pl.st_n_ent : 0, pl.st_ready ? pl.st_n_runs : 0,
-                        pl.st_max_run_groups, pl.st_max_run_ents};
-  for (int k = 0; k < n && k < 8; k++) out[k] = v[k];
+                        pl.st_max_run_groups, pl.st_max_run_ents, pl.fallbacks};
+  for (int k = 0; k < n && k < 9; k++) out[k] = v[k];
   return DKT_OK;
 }
 

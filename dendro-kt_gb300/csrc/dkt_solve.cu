@@ -24,9 +24,12 @@
 // fixed-point product) and replaces the binary32 one, and the search
 // direction is rescaled -- the Krylov space is kept, so the iteration count
 // stays that of FP64 PCG.  Convergence is only ever declared on the FP64
-// residual.  If an update finds the true residual no longer falling (the
-// system is beyond binary32, condition number near 1/eps32), the solve
-// finishes with FP64 PCG from the current x.
+// residual.  Each mesh of a batch is judged on its own: one whose true
+// residual stopped falling while its recursion says it fell (the system is
+// beyond binary32, condition number near 1/eps32) is frozen in the binary32
+// sequence and finished with FP64 PCG from its current x once the others are
+// done; a search-direction restart likewise touches only the meshes that
+// need it.
 #include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
@@ -408,6 +411,13 @@ __global__ void k_rescale(const double *__restrict__ r, float *__restrict__ r32,
     p[i] *= ps;
   }
 }
+// p = z (a fresh search direction) on the meshes flagged
+__global__ void k_restart(float *__restrict__ p, const float *__restrict__ z, const int64_t *__restrict__ lo,
+                          const int64_t *__restrict__ hi, const int32_t *__restrict__ prob, const int *__restrict__ flag)
+{
+  if (!flag[prob[blockIdx.x]]) return;
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) p[i] = z[i];
+}
 // per mesh: finished meshes freeze (done), the others take alpha = 0 for the
 // z / r.z refresh that follows
 __global__ void k_mark(CgScal *__restrict__ sc, const int *__restrict__ active, int P)
@@ -478,7 +488,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
       DKT_CUDA(cudaStreamSynchronize(s));
       int above = 0;
       for (int p = 0; p < P; p++) {
-        rel[p] = hr[p] / hb[p];
+        rel[p] = hr[p] == 0.0 ? 0.0 : hr[p] / hb[p];   // b = 0: x = 0 is exact
         above += rel[p] > tol ? 1 : 0;
       }
       return above;
@@ -521,8 +531,11 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
       Cg<float> cg(pl, ch);
       DBuf<float> xc(n), r32(n);
       DBuf<double> r(n), sig(P), signew(P);
-      DBuf<int> act(P), fold_ok(P);
+      DBuf<int> act(P), fold_ok(P), rflag(P);
       std::vector<double> hsig(P, 0.0);
+      // meshes whose true residual stopped following their binary32
+      // recursion: frozen in the binary32 sequence, finished by FP64 PCG
+      std::vector<int> beyond(P, 0);
       const double delta = 1e-2;      // update once the recursive residual fell by this much
       int since = 0, updates = 0;
       DKT_CUDA(cudaMemsetAsync(xc.p, 0, n * sizeof(float), s));
@@ -534,14 +547,14 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
         pl.n_launch += 3;
         DKT_CUDA(cudaMemcpyAsync(hr.data(), signew.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
         DKT_CUDA(cudaStreamSynchronize(s));
-        int n_active = 0;
+        int n_above = 0;
         for (int p = 0; p < P; p++) {
-          rel[p] = hr[p] / hb[p];
-          h_active[p] = rel[p] > tol ? 1 : 0;
-          n_active += h_active[p];
+          rel[p] = hr[p] == 0.0 ? 0.0 : hr[p] / hb[p];   // b = 0: x = 0 is exact
+          n_above += rel[p] > tol ? 1 : 0;
+          h_active[p] = rel[p] > tol && !beyond[p] ? 1 : 0;
         }
         act.upload(h_active.data(), P, s);
-        return n_active;
+        return n_above;
       };
       if (true_residual() == 0) {
         rc = 0;
@@ -572,7 +585,6 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           for (int p = 0; p < P; p++) {
             if (!h_active[p]) continue;
             const double rr = cg.hsc[p].rr;   // |r32|^2, |r32| = 1 at the last update
-            if (!(rr == rr)) restart = true;
             if (rr <= delta * delta || std::sqrt(rr) * hsig[p] <= tol * hb[p] || !(rr == rr)) upd = true;
           }
           if (!upd) continue;
@@ -590,6 +602,22 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           since = 0;
           for (int p = 0; p < P; p++) outer[p] += h_active[p];
           if (true_residual() == 0) { rc = 0; break; }
+          // per mesh: a true residual that stopped falling while the
+          // recursion says it fell (or a recursion gone NaN) is beyond
+          // binary32; the other meshes of a batch carry on, whatever
+          // stage of their convergence this update finds them at
+          int n_mixed = 0;
+          bool newly = false;
+          for (int p = 0; p < P; p++) {
+            if (h_active[p] && (!(rec[p] == rec[p]) || (rec[p] <= 0.1 * hsig[p] && hr[p] > 0.5 * hsig[p]))) {
+              beyond[p] = 1;
+              h_active[p] = 0;
+              newly = true;
+            }
+            n_mixed += h_active[p];
+          }
+          if (newly) act.upload(h_active.data(), P, s);
+          if (n_mixed == 0) break;
           k_rescale<<<nb, ST, 0, s>>>(r.p, r32.p, cg.p.p, ch.lo.p, ch.hi.p, ch.prob.p, sig.p, signew.p, act.p);
           DKT_CUDA(cudaMemcpyAsync(sig.p, signew.p, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
           k_mark<<<pgrid(P), 128, 0, s>>>(cg.sc.p, act.p, P);
@@ -599,19 +627,17 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           pl.n_launch += 4;
           // the kept direction only fits a residual that the recursion still
           // tracks; where the true residual is far above the recursive one
-          // (binary32 round-off has taken over), restart from p = z
+          // (binary32 round-off has taken over), that mesh restarts from p = z
+          std::vector<int> rs(P, 0);
+          bool any = false;
           for (int p = 0; p < P; p++)
-            if (h_active[p] && !(hr[p] <= 10.0 * rec[p])) restart = true;
-          if (restart) {
-            k_pupd<float><<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, 1);
+            if (h_active[p] && (restart || !(hr[p] <= 10.0 * rec[p]))) rs[p] = 1, any = true;
+          if (any) {
+            rflag.upload(rs.data(), P, s);
+            k_restart<<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, rflag.p);
             pl.n_launch++;
           }
-          // a mesh whose true residual stopped falling is beyond binary32
-          bool stalled = false;
-          for (int p = 0; p < P; p++)
-            if (h_active[p] && hr[p] > 0.5 * hsig[p]) stalled = true;
           hsig = hr;
-          if (stalled) break;
         }
       }
       if (rc != 0 && used < max_iter) {

@@ -659,10 +659,14 @@ __device__ __forceinline__ void q1t_tile(
   using F = typename AR::Factor;
   constexpr int NPE = 1 << DIM;
   extern __shared__ __align__(16) unsigned char smem[];
-  // a batched solve: tiles whose meshes have all converged are not needed
-  if (skip_mesh && skip_mesh[(int64_t) tile_mlo[tile] * skip_stride] &&
-      skip_mesh[(int64_t) tile_mhi[tile] * skip_stride])
-    return;
+  // a batched solve: tiles whose meshes have all converged are not needed (a
+  // tile of small meshes covers several; every one of them is checked)
+  if (skip_mesh) {
+    bool all_done = true;
+    for (int32_t m = tile_mlo[tile], me = tile_mhi[tile]; m <= me && all_done; m++)
+      all_done = skip_mesh[(int64_t) m * skip_stride] != 0;
+    if (all_done) return;
+  }
   // the tile's node entries at tile * cap, its count beside them; its leaves
   // at tile * T unless the plan is a batch (concatenated tiles)
   (void) tile_off;

@@ -126,7 +126,9 @@ int dkt_plan_stats(dkt_plan plan, int64_t *out4);
 
 /* Extended counts, up to n of: leaves, hanging leaves, stale slots, boundary
  * nodes, stale-chain entries, stale-chain runs, longest run (hanging leaves),
- * longest run (entries).  Instrumentation, no reference counterpart. */
+ * longest run (entries), mixed-precision solves on the plan that finished
+ * some mesh with FP64 PCG (its binary32 recursion had stopped tracking the
+ * true residual).  Instrumentation, no reference counterpart. */
 int dkt_plan_stats_ex(dkt_plan plan, int64_t *out, int n);
 
 /* Host copy of the flattened traversal (for inspection and tests):

@@ -69,6 +69,10 @@ def test_batched_pcg_per_mesh_convergence(dkt, precision, order):
     xd = torch.zeros_like(bd)
     it, ref, rr, ok = B.pcg(bd, xd, precision=precision, tol=1e-10)
     assert ok and len(it) == 5 and np.all(rr <= 1e-10), (it, ref, rr)
+    if precision == 1:
+        # well-conditioned meshes at different stages of convergence at each
+        # reliable update: every one stays in the binary32 sequence
+        assert B.stats()["fp64_finishes"] == 0 and np.all(ref >= 1), ref
     x = xd.cpu().numpy()
     for k, (A, d) in enumerate(zip(mats, das)):
         xk = x[off[k]:off[k + 1]]
@@ -102,3 +106,39 @@ def test_autotune_keeps_result(dkt):
     C = dkt.Matrix(d, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING)
     T32, p32, ms32, t32 = C.autotune(arith=1)
     assert ms32 > 0 and T32 in (0, 128, 256, 512) and ms32 == min(t for t in t32 if t > 0)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_pcg_tiles_spanning_small_meshes(dkt, precision):
+    """Forty small 2D meshes (7-60 leaves), re-tiled over the whole batch so
+    that each tile covers several of them; three in four have a zero
+    right-hand side and converge at once.  A tile whose first and last meshes
+    are done still holds live meshes between them, whose products must go on;
+    the zero meshes keep x = 0."""
+    import torch
+    das = []
+    for k in range(40):
+        c, l = dkt.tree_from_points(dkt.cluster_points(3, 2, 8, seed=k), 2, 8)
+        das.append(dkt.DA(c, l, 2, order=1, max_depth=8))
+    mats = [dkt.Matrix(d, op=dkt.OP_LAPLACE, traversal=dkt.TRAVERSAL_CONFORMING) for d in das]
+    B = dkt.Matrix.batch(mats)
+    B.set_tile(256)
+    off = B.mesh_offsets()
+    bs = []
+    for k, d in enumerate(das):
+        b = dkt.uniform_pm1(50 + k, d.n) if k % 4 == 1 else np.zeros(d.n)
+        b[d.boundary_ids()] = 0.0
+        bs.append(b)
+    bd = torch.from_numpy(np.concatenate(bs)).cuda()
+    xd = torch.zeros_like(bd)
+    it, ref, rr, ok = B.pcg(bd, xd, precision=precision, tol=1e-10)
+    assert ok and np.all(rr <= 1e-10), (it, rr)
+    x = xd.cpu().numpy()
+    for k, (A, d) in enumerate(zip(mats, das)):
+        xk = x[off[k]:off[k + 1]]
+        if k % 4 != 1:
+            assert not np.any(xk), k
+            assert it[k] == 0, (k, it[k])
+            continue
+        r = bs[k] - _mv(A, xk)
+        assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(bs[k]), k
