@@ -5,8 +5,8 @@
 //
 // The vectors are cut into chunks that never straddle two meshes; one CTA
 // per chunk does the vector work and writes per-chunk partial sums, and a
-// one-warp-per-mesh kernel adds each mesh's partials in a fixed order (lane
-// sums over a fixed stride, then a fixed shuffle tree), so every dot product
+// one-block-per-mesh kernel adds each mesh's partials in a fixed order (thread
+// sums over a fixed stride, then a fixed reduction tree), so every dot product
 // accumulates in FP64 and is bitwise reproducible.  Chunks are small (2048
 // nodes, eight per thread) because FP64 additions are long-latency on this
 // part: a thread's chain of dependent FP64 accumulations must stay short.  All
@@ -19,17 +19,18 @@
 // Mixed precision (reliable updates): one Jacobi-PCG sequence runs on
 // binary32 vectors with the binary32 Q1 product, in units of the FP64
 // residual norm at the last update.  Whenever a mesh's recursive residual has
-// fallen 1000x (or claims convergence), the accumulated correction is added
-// to x in FP64, the residual is recomputed exactly (b - A x with the FP64
-// fixed-point product) and replaces the binary32 one, and the search
-// direction is rescaled -- the Krylov space is kept, so the iteration count
-// stays that of FP64 PCG.  Convergence is only ever declared on the FP64
-// residual.  Each mesh of a batch is judged on its own: one whose true
-// residual stopped falling while its recursion says it fell (the system is
-// beyond binary32, condition number near 1/eps32) is frozen in the binary32
-// sequence and finished with FP64 PCG from its current x once the others are
-// done; a search-direction restart likewise touches only the meshes that
-// need it.
+// fallen 100x (or claims convergence), or 512 iterations passed without that,
+// the accumulated correction is added to x in FP64, the residual is
+// recomputed exactly (b - A x with the FP64 fixed-point product) and replaces
+// the binary32 one, and the search direction is rescaled -- the Krylov space
+// is kept, so the iteration count stays near that of FP64 PCG.  Only a mesh
+// whose true residual is far above its recursive one (binary32 round-off has
+// taken over) restarts its direction.  Convergence is only ever declared on
+// the FP64 residual.  Each mesh of a batch is judged on its own: one whose
+// true residual stopped falling while its recursion says it fell, or that 512
+// iterations did not move (the system is beyond binary32, condition number
+// near 1/eps32), is frozen in the binary32 sequence and finished with FP64
+// PCG from its current x once the others are done.
 #include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
@@ -132,30 +133,33 @@ __global__ void __launch_bounds__(ST) k_dot(const T *__restrict__ a, const T *__
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// Per mesh (one warp): sum of its chunks' partials in a fixed order -- lane l
-// adds chunks c0 + l, c0 + l + 32, ... in turn, then a fixed shuffle tree.
-// Every lane returns the total.
-__device__ __forceinline__ double mesh_sum(const double *part, int stride, int off, int c0, int c1, int lane)
+// Per mesh (one block of FIN threads): sum of its chunks' partials in a fixed
+// order -- thread t adds chunks c0 + t, c0 + t + FIN, ... in turn, then the
+// fixed shuffle and shared-memory tree of block_sum.  A block, not a warp:
+// FP64 additions are long-latency on this part, and a warp would add about
+// 80 partials in one dependent chain per lane on a 5 M-node mesh.  Thread 0
+// returns the total.
+constexpr int FIN = 256;
+__device__ __forceinline__ double mesh_sum(const double *part, int stride, int off, int c0, int c1, double *sh)
 {
   double s = 0.0;
-#pragma unroll 8
-  for (int c = c0 + lane; c < c1; c += 32) s += part[(int64_t) c * stride + off];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  return s;
+#pragma unroll 4
+  for (int c = c0 + (int) threadIdx.x; c < c1; c += FIN) s += part[(int64_t) c * stride + off];
+  return block_sum(s, sh);
 }
-// one warp per mesh in the finalisers (the whole warp returns together)
-#define MESH_OF_WARP(P)                                                      \
-  const int lane = threadIdx.x & 31;                                         \
-  const int p = (int) ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);        \
+// one block per mesh in the finalisers
+#define MESH_OF_BLOCK(P)                                                     \
+  __shared__ double sh_fin[FIN / 32];                                        \
+  const int p = (int) blockIdx.x;                                            \
   if (p >= (P)) return;
 
 // alpha = r.z / p.q (0 once converged or on breakdown)
 __global__ void k_fin_alpha(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
                             CgScal *__restrict__ sc)
 {
-  MESH_OF_WARP(P)
-  const double pq = mesh_sum(part, 1, 0, first[p], first[p + 1], lane);
-  if (lane != 0) return;
+  MESH_OF_BLOCK(P)
+  const double pq = mesh_sum(part, 1, 0, first[p], first[p + 1], sh_fin);
+  if (threadIdx.x != 0) return;
   CgScal &q = sc[p];
   q.pq = pq;
   q.alpha = (q.done || !(pq != 0.0)) ? 0.0 : q.rz / pq;
@@ -199,10 +203,10 @@ __global__ void __launch_bounds__(ST) k_update(T *__restrict__ x, T *__restrict_
 __global__ void k_fin_beta(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
                            CgScal *__restrict__ sc, int count, int *__restrict__ n_done)
 {
-  MESH_OF_WARP(P)
-  const double a = mesh_sum(part, 2, 0, first[p], first[p + 1], lane);
-  const double b = mesh_sum(part, 2, 1, first[p], first[p + 1], lane);
-  if (lane != 0) return;
+  MESH_OF_BLOCK(P)
+  const double a = mesh_sum(part, 2, 0, first[p], first[p + 1], sh_fin);
+  const double b = mesh_sum(part, 2, 1, first[p], first[p + 1], sh_fin);
+  if (threadIdx.x != 0) return;
   CgScal &q = sc[p];
   if (!q.done) {
     if (count) q.it++;
@@ -240,9 +244,9 @@ __global__ void k_residual(const double *__restrict__ b, const double *__restric
 __global__ void k_norms(const double *__restrict__ part, const int32_t *__restrict__ first, int P,
                         double *__restrict__ nrm)
 {
-  MESH_OF_WARP(P)
-  const double v = sqrt(mesh_sum(part, 1, 0, first[p], first[p + 1], lane));
-  if (lane == 0) nrm[p] = v;
+  MESH_OF_BLOCK(P)
+  const double v = mesh_sum(part, 1, 0, first[p], first[p + 1], sh_fin);
+  if (threadIdx.x == 0) nrm[p] = sqrt(v);
 }
 
 __global__ void k_invert(const double *__restrict__ d, double *__restrict__ o64, float *__restrict__ o32, int64_t n)
@@ -278,7 +282,7 @@ template <> struct CgOp<float> {
 };
 
 inline unsigned pgrid(int P) { return (unsigned) ((P + 127) / 128); }
-inline unsigned wgrid(int P) { return (unsigned) ((P + 3) / 4); }   // blocks of 128 threads, a warp per mesh
+inline unsigned wgrid(int P) { return (unsigned) std::max(P, 1); }   // finalisers: a block of FIN threads per mesh
 
 // Jacobi-PCG on all meshes of the plan, in type T (FP64 dots).  r must hold
 // b - A x on entry.
@@ -315,9 +319,9 @@ struct Cg {
     CgOp<T>::apply(pl, p.p, q.p, s);
     k_dot<T><<<nb, ST, 0, s>>>(p.p, q.p, ch.lo.p, ch.hi.p, part.p, &sc.p[0].done, ch.prob.p,
                                (int) (sizeof(CgScal) / sizeof(int)));
-    k_fin_alpha<<<wgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p);
+    k_fin_alpha<<<wgrid(ch.P), FIN, 0, s>>>(part.p, ch.first.p, ch.P, sc.p);
     k_update<T><<<nb, ST, 0, s>>>(x, r, z.p, p.p, q.p, dinv, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, part.p);
-    k_fin_beta<<<wgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 1, n_done.p);
+    k_fin_beta<<<wgrid(ch.P), FIN, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 1, n_done.p);
     k_pupd<T><<<nb, ST, 0, s>>>(p.p, z.p, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, 0);
     check_launch("cg_iteration");
     pl.n_launch += 5;
@@ -332,7 +336,7 @@ struct Cg {
     k_init_scal<<<pgrid(ch.P), 128, 0, s>>>(sc.p, ch.P, rr_stop_dev, rr_stop, n_done.p);
     // z = dinv r, r.z, r.r (alpha = 0 leaves x and r unchanged), p = z
     k_update<T><<<nb, ST, 0, s>>>(x, r, z.p, p.p, q.p, dinv, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, part.p);
-    k_fin_beta<<<wgrid(ch.P), 128, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 0, n_done.p);
+    k_fin_beta<<<wgrid(ch.P), FIN, 0, s>>>(part.p, ch.first.p, ch.P, sc.p, 0, n_done.p);
     k_pupd<T><<<nb, ST, 0, s>>>(p.p, z.p, ch.lo.p, ch.hi.p, ch.prob.p, sc.p, 1);
     check_launch("cg_start");
     pl.n_launch += 4;
@@ -467,7 +471,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
     }
     // per-mesh ||b||
     k_dot<double><<<nb, ST, 0, s>>>(b, b, ch.lo.p, ch.hi.p, part.p);
-    k_norms<<<wgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, bnrm.p);
+    k_norms<<<wgrid(P), FIN, 0, s>>>(part.p, ch.first.p, P, bnrm.p);
     pl.n_launch += 2;
     DKT_CUDA(cudaMemcpyAsync(hb.data(), bnrm.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
     DKT_CUDA(cudaStreamSynchronize(s));
@@ -482,7 +486,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
       fematrix_matvec(pl, x, ax.p, 1.0, s);
       k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
       k_dot<double><<<nb, ST, 0, s>>>(r.p, r.p, ch.lo.p, ch.hi.p, part.p);
-      k_norms<<<wgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, rnrm.p);
+      k_norms<<<wgrid(P), FIN, 0, s>>>(part.p, ch.first.p, P, rnrm.p);
       pl.n_launch += 4;
       DKT_CUDA(cudaMemcpyAsync(hr.data(), rnrm.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
       DKT_CUDA(cudaStreamSynchronize(s));
@@ -543,7 +547,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
         fematrix_matvec(pl, x, ax.p, 1.0, s);
         k_residual<<<608, ST, 0, s>>>(b, ax.p, r.p, n);
         k_dot<double><<<nb, ST, 0, s>>>(r.p, r.p, ch.lo.p, ch.hi.p, part.p);
-        k_norms<<<wgrid(P), 128, 0, s>>>(part.p, ch.first.p, P, signew.p);
+        k_norms<<<wgrid(P), FIN, 0, s>>>(part.p, ch.first.p, P, signew.p);
         pl.n_launch += 3;
         DKT_CUDA(cudaMemcpyAsync(hr.data(), signew.p, P * sizeof(double), cudaMemcpyDeviceToHost, s));
         DKT_CUDA(cudaStreamSynchronize(s));
@@ -566,7 +570,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
         k_mark<<<pgrid(P), 128, 0, s>>>(cg.sc.p, act.p, P);
         k_update<float><<<nb, ST, 0, s>>>(xc.p, r32.p, cg.z.p, cg.p.p, cg.q.p, dinv32.p ? dinv32.p : nullptr,
                                           ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, cg.part.p);
-        k_fin_beta<<<wgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
+        k_fin_beta<<<wgrid(P), FIN, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
         k_pupd<float><<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, 1);
         pl.n_launch += 6;
         hsig = hr;
@@ -581,7 +585,8 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           DKT_CUDA(cudaStreamSynchronize(s));
           // update when some active mesh's recursive residual fell by delta or
           // claims convergence, or after 512 iterations without one
-          bool upd = since >= 512, restart = since >= 512;
+          const bool long_run = since >= 512;
+          bool upd = long_run;
           for (int p = 0; p < P; p++) {
             if (!h_active[p]) continue;
             const double rr = cg.hsc[p].rr;   // |r32|^2, |r32| = 1 at the last update
@@ -603,13 +608,15 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           for (int p = 0; p < P; p++) outer[p] += h_active[p];
           if (true_residual() == 0) { rc = 0; break; }
           // per mesh: a true residual that stopped falling while the
-          // recursion says it fell (or a recursion gone NaN) is beyond
-          // binary32; the other meshes of a batch carry on, whatever
-          // stage of their convergence this update finds them at
+          // recursion says it fell, one that 512 binary32 iterations did not
+          // lower by a tenth, or a recursion gone NaN, is beyond binary32;
+          // the other meshes of a batch carry on, whatever stage of their
+          // convergence this update finds them at
           int n_mixed = 0;
           bool newly = false;
           for (int p = 0; p < P; p++) {
-            if (h_active[p] && (!(rec[p] == rec[p]) || (rec[p] <= 0.1 * hsig[p] && hr[p] > 0.5 * hsig[p]))) {
+            if (h_active[p] && (!(rec[p] == rec[p]) || (rec[p] <= 0.1 * hsig[p] && hr[p] > 0.5 * hsig[p]) ||
+                                (long_run && hr[p] > 0.9 * hsig[p]))) {
               beyond[p] = 1;
               h_active[p] = 0;
               newly = true;
@@ -623,15 +630,19 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           k_mark<<<pgrid(P), 128, 0, s>>>(cg.sc.p, act.p, P);
           k_update<float><<<nb, ST, 0, s>>>(xc.p, r32.p, cg.z.p, cg.p.p, cg.q.p, jacobi ? dinv32.p : nullptr,
                                             ch.lo.p, ch.hi.p, ch.prob.p, cg.sc.p, cg.part.p);
-          k_fin_beta<<<wgrid(P), 128, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
+          k_fin_beta<<<wgrid(P), FIN, 0, s>>>(cg.part.p, ch.first.p, P, cg.sc.p, 0, cg.n_done.p);
           pl.n_launch += 4;
           // the kept direction only fits a residual that the recursion still
           // tracks; where the true residual is far above the recursive one
-          // (binary32 round-off has taken over), that mesh restarts from p = z
+          // (binary32 round-off has taken over), that mesh restarts from p = z.
+          // A mesh whose recursion still tracks keeps its direction however
+          // long the run was: ill-conditioned meshes (2D at depth 14) need
+          // thousands of iterations, and a restart every 512 would turn CG
+          // into a much slower restarted method.
           std::vector<int> rs(P, 0);
           bool any = false;
           for (int p = 0; p < P; p++)
-            if (h_active[p] && (restart || !(hr[p] <= 10.0 * rec[p]))) rs[p] = 1, any = true;
+            if (h_active[p] && !(hr[p] <= 10.0 * rec[p])) rs[p] = 1, any = true;
           if (any) {
             rflag.upload(rs.data(), P, s);
             k_restart<<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, rflag.p);

@@ -787,11 +787,10 @@ __device__ __forceinline__ void q1t_tile(
           if (conforming || !((fmask >> k) & 1u)) ACC::add(ys, Us, p, v[k]);
         }
       }
-    } else {
+    } else if (hang) {
 #pragma unroll
-      for (int k = 0; k < NPE; k++)
-        zt[k] = ((fmask >> k) & 1u) || !hang ? V(0) : v[k] * (1.0f / (float) (1 << __popc(k)));
-      if (hang) superset_sums<DIM, V>(zt);
+      for (int k = 0; k < NPE; k++) zt[k] = ((fmask >> k) & 1u) ? V(0) : v[k] * (1.0f / (float) (1 << __popc(k)));
+      superset_sums<DIM, V>(zt);
     }
   }
   if constexpr (!std::is_same<AR, FixedArith>::value) {
@@ -801,12 +800,16 @@ __device__ __forceinline__ void q1t_tile(
     // integer is one fused multiply-add: v * up + 1.5 * 2^23 lands in
     // [2^23, 2^24), where binary32 spacing is 1, for |v * up| < 2^22, and its
     // bits less those of 1.5 * 2^23 are the rounded integer.
+    // The largest contribution bounds the scale.  The outputs of unfilled
+    // ranks, which go to sinks, count too: they are element outputs like the
+    // others, and leaving them out would cost a test per rank.
     float m = 0.0f;
     if (valid) {
 #pragma unroll
-      for (int k = 0; k < NPE; k++) {
-        if (idx16<NPE>(w, k) < (uint32_t) U) m = fmaxf(m, fabsf(v[k]));
-        m = fmaxf(m, fabsf(zt[k]));
+      for (int k = 0; k < NPE; k++) m = fmaxf(m, fabsf(v[k]));
+      if (h >= 0) {
+#pragma unroll
+        for (int k = 0; k < NPE; k++) m = fmaxf(m, fabsf(zt[k]));
       }
     }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));

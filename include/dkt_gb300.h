@@ -241,8 +241,11 @@ int dkt_cg_solve_host(dkt_plan plan, const double *b_host, double *x_host, int m
  * in FP64.  DKT_PREC_MIXED: Jacobi-PCG on binary32 vectors with the binary32
  * product and reliable updates -- the correction is folded into x in FP64
  * and the residual recomputed with the FP64 product (b - A x) each
- * time the binary32 residual has fallen 1000x -- until ||b - A x||_2 <=
- * tol ||b||_2 (FP64 residual); refinements counts the updates.  Dot products
+ * time the binary32 residual has fallen 100x, or after 512 binary32
+ * iterations without that, the search direction kept while the binary32
+ * recursion still tracks b - A x -- until ||b - A x||_2 <= tol ||b||_2
+ * (FP64 residual); refinements counts the updates.  A mesh on which binary32
+ * stops making progress is finished by FP64 PCG from its x.  Dot products
  * accumulate in FP64 in both.  Mixed needs a Q1 or Q2 built-in operator without
  * stale parent reads (a conforming plan, or a mesh without them); it is the
  * solver of HeatMat::cgSolve (FEM/examples/src/heatMat.cpp:164-325) with the
