@@ -442,19 +442,22 @@ __global__ void __launch_bounds__(TP_THREADS) k_stale_chain_tp(
   }
 }
 
-// Blocks of a chain launch: at most four per SM, each taking runs in turn
+// Blocks of a chain launch: at most eight per SM, each taking runs in turn
 // from the list (longest first).  One block per run would fill the SMs'
 // block slots with short-lived chain blocks at the start of the product and
 // hold back the leaf kernel it overlaps (level-8 moving ball: 3.93 ms for the
-// leaf kernel beside a one-block-per-run chain, 3.76 ms beside this one, 3.60
-// ms alone); one block per SM makes the chain outlast the leaf kernel on
-// smaller meshes (level 7: product step 0.82 ms against 0.65 ms).
+// leaf kernel beside a one-block-per-run chain, 3.76 ms beside four blocks
+// per SM, with an earlier leaf kernel).  On the current leaf kernel the
+// level-8 product does not depend on the chain's width (step 3.43 ms with
+// two, four or eight blocks per SM), while on smaller meshes the chain is the
+// longer of the two and more walkers shorten it (level 7: step 0.680 ms with
+// two per SM, 0.630 with four, 0.598 with eight).
 static unsigned chain_blocks(int64_t n_runs)
 {
   int dev = 0, sms = 0;
   DKT_CUDA(cudaGetDevice(&dev));
   DKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  return (unsigned) std::max<int64_t>(1, std::min<int64_t>(n_runs, (int64_t) 4 * std::max(sms, 1)));
+  return (unsigned) std::max<int64_t>(1, std::min<int64_t>(n_runs, (int64_t) 8 * std::max(sms, 1)));
 }
 
 void stale_eval(Plan &pl, const double *x, const long long *xq, cudaStream_t s)

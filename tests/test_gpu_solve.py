@@ -168,9 +168,10 @@ def test_mixed_keeps_krylov_space_on_ill_conditioned_2d_mesh(dkt):
     iterations.  Reliable updates come every 512 binary32 iterations there
     (the recursion does not fall 100x sooner), and the search direction must
     survive them while the recursion tracks the true residual: the mixed
-    solve stays within 1.5x of the FP64 iteration count (restarting the
-    direction at each such update took it to about 2x, and to 8x on the
-    largest 2D meshes), and both reach 1e-10 on b - A x."""
+    solve stays within 1.35x of the FP64 iteration count (2,464 against
+    2,022; restarting the direction at each such update took it to 3,088, and
+    to 8x the FP64 count on the largest 2D meshes), and both reach 1e-10 on
+    b - A x."""
     import torch
     level, (c, l) = 2, dkt.sphere_shell_tree(2, 14, 2, (0.4997, 0.4342), 0.245)
     while len(l) < 240000 and level < 14:
@@ -189,4 +190,4 @@ def test_mixed_keeps_krylov_space_on_ill_conditioned_2d_mesh(dkt):
         assert ok and np.linalg.norm(b - ax.cpu().numpy()) <= 1e-10 * np.linalg.norm(b), (prec, it, ref, rr)
         its[prec] = it
     assert its[dkt.PREC_FP64] >= 1000, its
-    assert its[dkt.PREC_MIXED] <= 1.5 * its[dkt.PREC_FP64], its
+    assert its[dkt.PREC_MIXED] <= 1.35 * its[dkt.PREC_FP64], its
