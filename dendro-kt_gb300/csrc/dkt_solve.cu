@@ -7,7 +7,8 @@
 // per chunk does the vector work and writes per-chunk partial sums, and a
 // one-block-per-mesh kernel adds each mesh's partials in a fixed order (thread
 // sums over a fixed stride, then a fixed reduction tree), so every dot product
-// accumulates in FP64 and is bitwise reproducible.  Chunks are small (2048
+// accumulates in FP64 across threads and is bitwise reproducible (a thread's
+// eight terms of a binary32 vector are first added in binary32).  Chunks are small (2048
 // nodes, eight per thread) because FP64 additions are long-latency on this
 // part: a thread's chain of dependent FP64 accumulations must stay short.  All
 // scalars (alpha, beta, r.z, r.r, a converged flag) stay on the device, so a
@@ -114,7 +115,7 @@ __device__ __forceinline__ double widen(float f)
 }
 __device__ __forceinline__ double widen(double d) { return d; }
 
-// part[c] = sum over chunk c of a*b (FP64 accumulation)
+// part[c] = sum over chunk c of a*b (FP64 across threads)
 template <typename T>
 __global__ void __launch_bounds__(ST) k_dot(const T *__restrict__ a, const T *__restrict__ b,
                                            const int64_t *__restrict__ lo, const int64_t *__restrict__ hi,
@@ -127,9 +128,12 @@ __global__ void __launch_bounds__(ST) k_dot(const T *__restrict__ a, const T *__
     if (threadIdx.x == 0) part[blockIdx.x] = 0.0;
     return;
   }
-  double s = 0.0;
-  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) s = fma(widen(a[i]), widen(b[i]), s);
-  s = block_sum(s, sh);
+  // each thread's eight terms in T (binary32 vectors: binary32 partials, one
+  // widening per thread, so the FP64 pipe adds 256 partials per chunk instead
+  // of 2048 terms), then the fixed FP64 block tree
+  T t = T(0);
+  for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) t = fma(a[i], b[i], t);
+  const double s = block_sum(widen(t), sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(ST) k_update(T *__restrict__ x, T *__restrict_
   }
   const double a = sc[prob[blockIdx.x]].alpha;
   const T at = (T) a;
-  double srz = 0.0, srr = 0.0;
+  T trz = T(0), trr = T(0);   // each thread's terms in T, as in k_dot
   for (int64_t i = lo[blockIdx.x] + threadIdx.x; i < hi[blockIdx.x]; i += ST) {
     T ri = r[i];
     if (a != 0.0) {
@@ -190,12 +194,11 @@ __global__ void __launch_bounds__(ST) k_update(T *__restrict__ x, T *__restrict_
     }
     const T zi = dinv ? ri * dinv[i] : ri;
     z[i] = zi;
-    const double rd = widen(ri);
-    srz = fma(rd, widen(zi), srz);
-    srr = fma(rd, rd, srr);
+    trz = fma(ri, zi, trz);
+    trr = fma(ri, ri, trr);
   }
-  srz = block_sum(srz, sh);
-  srr = block_sum(srr, sh);
+  const double srz = block_sum(widen(trz), sh);
+  const double srr = block_sum(widen(trr), sh);
   if (threadIdx.x == 0) { part[2 * blockIdx.x] = srz; part[2 * blockIdx.x + 1] = srr; }
 }
 
