@@ -29,9 +29,10 @@
 // taken over) restarts its direction.  Convergence is only ever declared on
 // the FP64 residual.  Each mesh of a batch is judged on its own: one whose
 // true residual stopped falling while its recursion says it fell, or that 512
-// iterations did not move (the system is beyond binary32, condition number
-// near 1/eps32), is frozen in the binary32 sequence and finished with FP64
-// PCG from its current x once the others are done.
+// iterations did not move, twice in a row (the system is beyond binary32,
+// condition number near 1/eps32; the first time only restarts its
+// direction), is frozen in the binary32 sequence and finished with FP64 PCG
+// from its current x once the others are done.
 #include <algorithm>
 #include <cmath>
 #include "dkt_internal.cuh"
@@ -543,6 +544,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
       // meshes whose true residual stopped following their binary32
       // recursion: frozen in the binary32 sequence, finished by FP64 PCG
       std::vector<int> beyond(P, 0);
+      std::vector<int> stalls(P, 0);   // consecutive updates that found the mesh stalled
       const double delta = 1e-2;      // update once the recursive residual fell by this much
       int since = 0, updates = 0;
       DKT_CUDA(cudaMemsetAsync(xc.p, 0, n * sizeof(float), s));
@@ -610,16 +612,22 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           since = 0;
           for (int p = 0; p < P; p++) outer[p] += h_active[p];
           if (true_residual() == 0) { rc = 0; break; }
-          // per mesh: a true residual that stopped falling while the
-          // recursion says it fell, one that 512 binary32 iterations did not
-          // lower by a tenth, or a recursion gone NaN, is beyond binary32;
-          // the other meshes of a batch carry on, whatever stage of their
-          // convergence this update finds them at
+          // per mesh: a stall is a true residual that stopped falling while
+          // the recursion says it fell, or one that 512 binary32 iterations did
+          // not lower by a tenth.  A first stall restarts the mesh's direction
+          // (binary32 rounding can throw one sequence off, and the product's
+          // float atomics make runs differ); a second in a row, or a recursion
+          // gone NaN, means the mesh is beyond binary32.  The other meshes of a
+          // batch carry on, whatever stage of their convergence this update
+          // finds them at.
           int n_mixed = 0;
           bool newly = false;
           for (int p = 0; p < P; p++) {
-            if (h_active[p] && (!(rec[p] == rec[p]) || (rec[p] <= 0.1 * hsig[p] && hr[p] > 0.5 * hsig[p]) ||
-                                (long_run && hr[p] > 0.9 * hsig[p]))) {
+            if (!h_active[p]) continue;
+            const bool stalled = (rec[p] <= 0.1 * hsig[p] && hr[p] > 0.5 * hsig[p]) ||
+                                 (long_run && hr[p] > 0.9 * hsig[p]);
+            stalls[p] = stalled ? stalls[p] + 1 : 0;
+            if (!(rec[p] == rec[p]) || stalls[p] >= 2) {
               beyond[p] = 1;
               h_active[p] = 0;
               newly = true;
@@ -645,7 +653,7 @@ int pcg_solve(Plan &pl, const double *b, double *x, int precision, int max_iter,
           std::vector<int> rs(P, 0);
           bool any = false;
           for (int p = 0; p < P; p++)
-            if (h_active[p] && !(hr[p] <= 10.0 * rec[p])) rs[p] = 1, any = true;
+            if (h_active[p] && (stalls[p] > 0 || !(hr[p] <= 10.0 * rec[p]))) rs[p] = 1, any = true;
           if (any) {
             rflag.upload(rs.data(), P, s);
             k_restart<<<nb, ST, 0, s>>>(cg.p.p, cg.z.p, ch.lo.p, ch.hi.p, ch.prob.p, rflag.p);
