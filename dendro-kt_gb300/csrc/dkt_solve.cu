@@ -8,9 +8,10 @@
 // one-block-per-mesh kernel adds each mesh's partials in a fixed order (thread
 // sums over a fixed stride, then a fixed reduction tree), so every dot product
 // accumulates in FP64 across threads and is bitwise reproducible (a thread's
-// eight terms of a binary32 vector are first added in binary32).  Chunks are small (2048
-// nodes, eight per thread) because FP64 additions are long-latency on this
-// part: a thread's chain of dependent FP64 accumulations must stay short.  All
+// eight terms of a binary32 vector are first added in binary32).  Chunks are
+// small (2048 nodes, eight per thread) because FP64 additions are
+// long-latency on this part: a thread's chain of dependent FP64
+// accumulations must stay short.  All
 // scalars (alpha, beta, r.z, r.r, a converged flag) stay on the device, so a
 // block of iterations has no host synchronisation and is captured once into
 // a CUDA graph that is relaunched until every mesh has converged.  A
